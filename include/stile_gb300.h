@@ -1,0 +1,188 @@
+/*
+ * stile_gb300 -- C ABI of the GB300 (sm_103a) hybrid sparse-tile SpMM / SDDMM
+ * path.  Plain pointers and sizes only; every entry point returns 0 on
+ * success or a negative status (STILE_E_*), never aborts, and records a
+ * message readable through stile_last_error().
+ *
+ * Reference interfaces replaced (STile, paths relative to the project root):
+ *   stile_spmm_plan_upload / stile_sddmm_plan_upload
+ *       -- prepare_inputs_BSPMM / prepare_inputs_BSDDMM upload the packed
+ *          format arrays with tvm.nd.array(..., device=dev)
+ *          (MY_sparse/my_fuse_formats.py:3321-3332, :3544-3678)
+ *   stile_spmm_run
+ *       -- the fused SpMM PackedFunc f(*args_nd) launched by
+ *          measure_latency_BSPMM (MY_sparse/my_fuse_formats.py:4152-4173)
+ *   stile_sddmm_run
+ *       -- the fused SDDMM PackedFunc launched by measure_latency_BSDDMM
+ *          (MY_sparse/my_fuse_formats.py:4292-4330) plus the host-side
+ *          output reorder order_output_BSDDMM (:4247-4288), done on device
+ *   stile_spmm_dvals
+ *       -- no counterpart: value gradient of the SpMM (SDDMM on A's pattern
+ *          walking the forward tile layout), used by the autograd backward
+ *   stile_csr_spmm_run
+ *       -- the plain CSR SpMM comparator (the reference times cuSPARSE CSR
+ *          through torch.sparse_csr_tensor @ B, gen_formats_v2.py:3079-3106)
+ *   stile_plan_free / stile_last_error / stile_plan_error_flag
+ *       -- ownership and error reporting (the reference relies on TVM
+ *          NDArray lifetimes and asserts)
+ *
+ * Streams are passed as void* (a cudaStream_t; NULL = legacy default
+ * stream).  All device pointers are caller-owned except the plan arrays,
+ * which the plan handle owns.
+ */
+#ifndef STILE_GB300_H_
+#define STILE_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STILE_OK 0
+#define STILE_E_INVALID (-1)   /* bad argument or malformed plan */
+#define STILE_E_CUDA (-2)      /* a CUDA runtime call failed */
+#define STILE_E_DEVICE (-3)    /* a kernel reported a device-side error */
+#define STILE_E_UNSUPPORTED (-4)
+
+/* element types of dense operands / tensor-tile values */
+#define STILE_F32 0
+#define STILE_BF16 1
+#define STILE_F16 2
+#define STILE_FP8E4M3 3
+/* tensor-tile precision modes */
+#define STILE_TC_BF16 1        /* A, B rounded to bf16, fp32 accumulate */
+#define STILE_TC_F16 2         /* A, B rounded to fp16, fp32 accumulate */
+#define STILE_TC_SPLIT_BF16 4  /* hi+lo bf16 split of A and B, 3 products */
+#define STILE_TC_FP8 3         /* A e4m3 with per-tile scale, B e4m3, fp32 acc. */
+
+/*
+ * SpMM plan, device-ready host arrays (built by the emitter).
+ *
+ * Tensor-core items: one per (format, compressed 16-row block).  Each item
+ * owns k-steps [tc_item_kbeg[i], tc_item_kbeg[i+1]) of 16 columns.
+ * tc_vals holds, per k-step, the 16x16 block values as the shared-memory
+ * image of one tcgen05.mma B operand (K-major, no swizzle):
+ *   element (row n, col k) at byte (n/8)*256 + (k/8)*128 + (n%8)*16 + (k%8)*2
+ * for 16-bit modes (bf16 / fp16); STILE_TC_SPLIT_BF16 stores the hi image
+ * followed by the lo image (1024 B per k-step).
+ *
+ * ELL items: one per row-bucket tile; rows [ell_item_row0[i],
+ * ell_item_row0[i+1]), every row with ell_item_K[i] slots starting at
+ * ell_item_slot0[i] + r*K (the reference's indices_k layout).
+ *
+ * out rows equal to -1 are never written.  zero_rows lists the output rows
+ * that no owned (non-atomic) tile stores; stile_spmm_run zeroes them before
+ * the fused kernel so atomic tiles can accumulate.
+ */
+typedef struct StileSpmmPlanHost {
+  int32_t M, K;
+  int32_t tc_mode;
+  int32_t tc_n_items, tc_n_ksteps;
+  const int32_t* tc_item_kbeg;   /* [tc_n_items + 1] */
+  const int32_t* tc_item_flags;  /* [tc_n_items] bit0: atomic */
+  const int32_t* tc_out_rows;    /* [tc_n_items * 16] */
+  const int32_t* tc_cols;        /* [tc_n_ksteps * 16] */
+  const void* tc_vals;           /* [tc_n_ksteps * tc_kstep_bytes] */
+  int32_t tc_kstep_bytes;        /* 512 (bf16/fp16), 1024 (split), 256 (fp8) */
+  const float* tc_scales;        /* [tc_n_ksteps] fp8 per-tile scale, else NULL */
+  const int32_t* tc_nnz_id;      /* [tc_n_ksteps * 256] row-major (n,k); -1: empty */
+  int32_t ell_n_items, ell_n_rows, ell_n_slots;
+  const int32_t* ell_item_row0;  /* [ell_n_items + 1] */
+  const int32_t* ell_item_K;     /* [ell_n_items] */
+  const int32_t* ell_item_slot0; /* [ell_n_items] */
+  const int32_t* ell_item_flags; /* [ell_n_items] bit0: atomic */
+  const int32_t* ell_out_row;    /* [ell_n_rows] */
+  const int32_t* ell_row_len;    /* [ell_n_rows] live slots */
+  const float* ell_vals;         /* [ell_n_slots] */
+  const int32_t* ell_kidx;       /* [ell_n_slots] original column */
+  const int32_t* ell_nnz_id;     /* [ell_n_slots] -1: padding */
+  int32_t n_zero_rows;
+  const int32_t* zero_rows;      /* [n_zero_rows] */
+  int64_t nnz;                   /* nonzeros of the pattern (dvals length) */
+} StileSpmmPlanHost;
+
+/*
+ * SDDMM plan.  1D items: flattened nonzeros (mid_idx, j_idx, remap of the
+ * reference, my_fuse_formats.py:3568-3600).  Block items: TC_sddmm tiles
+ * (i_indices, j_indices, indptr, indicesDense, indices, :3607-3661);
+ * block width = bn (16), block height = bm (16).
+ */
+typedef struct StileSddmmPlanHost {
+  int32_t M, K;
+  int64_t nnz;
+  int32_t n_1d;
+  const int32_t* mid_idx;        /* [n_1d] */
+  const int32_t* j_idx;          /* [n_1d] */
+  const int32_t* remap;          /* [n_1d] output nonzero id */
+  int32_t n_blk, bm, bn, n_blk_nnz;
+  const int32_t* blk_i;          /* [n_blk * bm] */
+  const int32_t* blk_j;          /* [n_blk * bn] */
+  const int32_t* blk_indptr;     /* [n_blk + 1] */
+  const int32_t* blk_dense_pos;  /* [n_blk_nnz] m*bn + n */
+  const int32_t* blk_out;        /* [n_blk_nnz] output nonzero id */
+} StileSddmmPlanHost;
+
+typedef struct StileSpmmPlan StileSpmmPlan;
+typedef struct StileSddmmPlan StileSddmmPlan;
+
+/* Copy a host plan to the current device; the handle owns the copies. */
+int stile_spmm_plan_upload(const StileSpmmPlanHost* host, StileSpmmPlan** out);
+int stile_sddmm_plan_upload(const StileSddmmPlanHost* host, StileSddmmPlan** out);
+int stile_spmm_plan_free(StileSpmmPlan* plan);
+int stile_sddmm_plan_free(StileSddmmPlan* plan);
+
+/*
+ * C[M, N] = A @ B[K, N] (fp32 in / fp32 out; row strides ldb, ldc in
+ * elements, multiples of 4).  C is fully written (rows without nonzeros
+ * become 0).  Stream-ordered; returns after enqueueing.
+ */
+int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb,
+                   float* C, int64_t ldc, int32_t N, void* stream);
+
+/* dvals[nnz] = <dY[row(t)], B[col(t)]> for every nonzero t of A (CSR order),
+ * walking the forward plan's tiles. */
+int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy,
+                     const float* B, int64_t ldb, float* dvals, int32_t N,
+                     void* stream);
+
+/* out[nnz] = <X[row(t)], Y[col(t)]> (fp32), CSR order of the mask. */
+int stile_sddmm_run(const StileSddmmPlan* plan, const float* X, int64_t ldx,
+                    const float* Y, int64_t ldy, float* out, int32_t F,
+                    void* stream);
+
+/* Plain CSR-row SpMM (fp32): one warp group per row, vectorised B loads. */
+int stile_csr_spmm_run(int32_t M, const int32_t* indptr, const int32_t* indices,
+                       const float* vals, const float* B, int64_t ldb,
+                       float* C, int64_t ldc, int32_t N, void* stream);
+
+/* Refresh the tile values of a plan from vals[nnz] (device, CSR order of the
+ * pattern the plan was built for); the pattern and index arrays are kept.
+ * Used when A's values change between calls (training the values). */
+int stile_spmm_plan_set_values(StileSpmmPlan* plan, const float* vals, void* stream);
+
+/* Device-side error flag of a plan's kernels (bounded waits that gave up):
+ * synchronises the stream, returns the flag (0 = none) and clears it. */
+int stile_spmm_plan_error_flag(StileSpmmPlan* plan, void* stream, int32_t* flag);
+
+/* Tensor-core layout self-check (no counterpart in the reference): runs one
+ * tcgen05.mma (M=128, N=16, K=16, kind::f16, fp32 accumulate) on two 8 KB
+ * shared-memory images copied verbatim from a_img / b_img, with descriptor
+ * fields desc6 = {a_lbo, a_sbo, a_layout, b_lbo, b_sbo, b_layout} (bytes,
+ * multiples of 16, <= 2048) and instruction descriptor idesc; writes the
+ * 128x16 fp32 accumulator row-major to out.  *err is set if the MMA did not
+ * complete within the bounded wait. */
+int stile_debug_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
+                           uint32_t idesc, float* out, int32_t* err, void* stream);
+
+/* Copy the last error message of the calling thread into buf. */
+int stile_last_error(char* buf, size_t n);
+
+/* Number of kernels launched by this library since load (for accounting). */
+int64_t stile_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STILE_GB300_H_ */

@@ -1,0 +1,430 @@
+// C ABI: plan upload / free, entry points, error reporting.
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "spmm.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<int64_t> g_launches{0};
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(STILE_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// One device arena per plan: every array is copied into a 256-byte aligned
+// slot of a single allocation.
+struct Arena {
+  std::vector<std::pair<const void*, size_t>> parts;
+  std::vector<size_t> offs;
+  size_t total = 0;
+  size_t add(const void* p, size_t bytes) {
+    total = (total + 255) & ~size_t(255);
+    offs.push_back(total);
+    parts.push_back({p, bytes});
+    total += bytes;
+    return parts.size() - 1;
+  }
+};
+
+template <typename T>
+bool in_range(const T* a, long n, long lo, long hi) {
+  for (long i = 0; i < n; ++i)
+    if (a[i] < lo || a[i] >= hi) return false;
+  return true;
+}
+
+}  // namespace
+
+struct StileSpmmPlan {
+  void* arena = nullptr;
+  int* err_flag = nullptr;
+  stile::SpmmArgs args{};
+  int M = 0, K = 0;
+  long nnz = 0, ell_n_slots = 0;
+  int n_zero_rows = 0;
+  const int* zero_rows = nullptr;
+};
+
+struct StileSddmmPlan {
+  void* arena = nullptr;
+  stile::SddmmArgs args{};
+  int M = 0, K = 0;
+  long nnz = 0;
+};
+
+extern "C" {
+
+int stile_last_error(char* buf, size_t n) {
+  if (!buf || n == 0) return STILE_E_INVALID;
+  std::snprintf(buf, n, "%s", g_last_error.c_str());
+  return STILE_OK;
+}
+
+int64_t stile_launch_count(void) { return g_launches.load(); }
+
+int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
+  if (!h || !out) return fail(STILE_E_INVALID, "null argument");
+  *out = nullptr;
+  if (h->M < 0 || h->K < 0) return fail(STILE_E_INVALID, "negative shape");
+  if (h->tc_n_items < 0 || h->tc_n_ksteps < 0 || h->ell_n_items < 0 || h->ell_n_rows < 0 ||
+      h->ell_n_slots < 0 || h->n_zero_rows < 0)
+    return fail(STILE_E_INVALID, "negative count");
+  const int mode = h->tc_mode;
+  if (h->tc_n_items > 0) {
+    if (mode != STILE_TC_BF16 && mode != STILE_TC_F16 && mode != STILE_TC_SPLIT_BF16)
+      return fail(STILE_E_UNSUPPORTED, "tensor-tile mode not supported by this build");
+    const int want = (mode == STILE_TC_SPLIT_BF16) ? 1024 : 512;
+    if (h->tc_kstep_bytes != want) return fail(STILE_E_INVALID, "tc_kstep_bytes does not match mode");
+    if (!h->tc_item_kbeg || !h->tc_item_flags || !h->tc_out_rows || !h->tc_cols || !h->tc_vals)
+      return fail(STILE_E_INVALID, "missing tensor-tile array");
+    // host-side validation: monotone k-step ranges, indices in range
+    if (h->tc_item_kbeg[0] != 0 || h->tc_item_kbeg[h->tc_n_items] != h->tc_n_ksteps)
+      return fail(STILE_E_INVALID, "tc_item_kbeg does not span the k-steps");
+    for (int i = 0; i < h->tc_n_items; ++i)
+      if (h->tc_item_kbeg[i + 1] < h->tc_item_kbeg[i])
+        return fail(STILE_E_INVALID, "tc_item_kbeg not monotone");
+    if (!in_range(h->tc_cols, (long)h->tc_n_ksteps * 16, 0, h->K))
+      return fail(STILE_E_INVALID, "tc_cols out of range");
+    if (!in_range(h->tc_out_rows, (long)h->tc_n_items * 16, -1, h->M))
+      return fail(STILE_E_INVALID, "tc_out_rows out of range");
+    if (h->tc_nnz_id && !in_range(h->tc_nnz_id, (long)h->tc_n_ksteps * 256, -1, h->nnz))
+      return fail(STILE_E_INVALID, "tc_nnz_id out of range");
+  }
+  if (h->ell_n_items > 0) {
+    if (!h->ell_item_row0 || !h->ell_item_K || !h->ell_item_slot0 || !h->ell_item_flags ||
+        !h->ell_out_row || !h->ell_row_len || !h->ell_vals || !h->ell_kidx)
+      return fail(STILE_E_INVALID, "missing ELL array");
+    if (h->ell_item_row0[0] != 0 || h->ell_item_row0[h->ell_n_items] != h->ell_n_rows)
+      return fail(STILE_E_INVALID, "ell_item_row0 does not span the rows");
+    for (int i = 0; i < h->ell_n_items; ++i) {
+      const long nr = h->ell_item_row0[i + 1] - h->ell_item_row0[i];
+      if (nr < 0 || h->ell_item_K[i] <= 0) return fail(STILE_E_INVALID, "bad ELL item shape");
+      if (h->ell_item_slot0[i] < 0 || h->ell_item_slot0[i] + nr * h->ell_item_K[i] > h->ell_n_slots)
+        return fail(STILE_E_INVALID, "ELL item slots out of range");
+      for (long r = 0; r < nr; ++r) {
+        const int len = h->ell_row_len[h->ell_item_row0[i] + r];
+        if (len < 0 || len > h->ell_item_K[i]) return fail(STILE_E_INVALID, "ell_row_len > K");
+      }
+    }
+    if (!in_range(h->ell_kidx, h->ell_n_slots, 0, h->K))
+      return fail(STILE_E_INVALID, "ell_kidx out of range");
+    if (!in_range(h->ell_out_row, h->ell_n_rows, -1, h->M))
+      return fail(STILE_E_INVALID, "ell_out_row out of range");
+    if (h->ell_nnz_id && !in_range(h->ell_nnz_id, h->ell_n_slots, -1, h->nnz))
+      return fail(STILE_E_INVALID, "ell_nnz_id out of range");
+  }
+  if (h->n_zero_rows > 0 && (!h->zero_rows || !in_range(h->zero_rows, h->n_zero_rows, 0, h->M)))
+    return fail(STILE_E_INVALID, "zero_rows out of range");
+
+  Arena ar;
+  const long ti = h->tc_n_items, tk = h->tc_n_ksteps;
+  const long ei = h->ell_n_items, er = h->ell_n_rows, es = h->ell_n_slots;
+  size_t i_kbeg = ar.add(h->tc_item_kbeg, ti ? (ti + 1) * 4 : 0);
+  size_t i_flags = ar.add(h->tc_item_flags, ti * 4);
+  size_t i_orows = ar.add(h->tc_out_rows, ti * 16 * 4);
+  size_t i_cols = ar.add(h->tc_cols, tk * 16 * 4);
+  size_t i_vals = ar.add(h->tc_vals, tk * (size_t)h->tc_kstep_bytes);
+  size_t i_tnid = ar.add(h->tc_nnz_id, h->tc_nnz_id ? tk * 256 * 4 : 0);
+  size_t i_erow0 = ar.add(h->ell_item_row0, ei ? (ei + 1) * 4 : 0);
+  size_t i_eK = ar.add(h->ell_item_K, ei * 4);
+  size_t i_eslot = ar.add(h->ell_item_slot0, ei * 4);
+  size_t i_eflag = ar.add(h->ell_item_flags, ei * 4);
+  size_t i_eout = ar.add(h->ell_out_row, er * 4);
+  size_t i_elen = ar.add(h->ell_row_len, er * 4);
+  size_t i_evals = ar.add(h->ell_vals, es * 4);
+  size_t i_ekidx = ar.add(h->ell_kidx, es * 4);
+  size_t i_enid = ar.add(h->ell_nnz_id, h->ell_nnz_id ? es * 4 : 0);
+  size_t i_zero = ar.add(h->zero_rows, (size_t)h->n_zero_rows * 4);
+  size_t i_err = ar.add(nullptr, 16);
+
+  auto* plan = new StileSpmmPlan();
+  cudaError_t e = cudaMalloc(&plan->arena, ar.total ? ar.total : 256);
+  if (e != cudaSuccess) {
+    delete plan;
+    return cuda_fail(e, "cudaMalloc(plan)");
+  }
+  char* base = static_cast<char*>(plan->arena);
+  for (size_t i = 0; i < ar.parts.size(); ++i) {
+    if (ar.parts[i].first && ar.parts[i].second) {
+      e = cudaMemcpy(base + ar.offs[i], ar.parts[i].first, ar.parts[i].second, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        cudaFree(plan->arena);
+        delete plan;
+        return cuda_fail(e, "cudaMemcpy(plan)");
+      }
+    }
+  }
+  plan->err_flag = reinterpret_cast<int*>(base + ar.offs[i_err]);
+  e = cudaMemset(plan->err_flag, 0, 16);
+  if (e != cudaSuccess) {
+    cudaFree(plan->arena);
+    delete plan;
+    return cuda_fail(e, "cudaMemset(plan)");
+  }
+  auto P = [&](size_t idx) { return (const void*)(base + ar.offs[idx]); };
+  stile::SpmmArgs& a = plan->args;
+  a.tc_mode = mode;
+  a.tc_n_items = h->tc_n_items;
+  a.tc_n_ksteps = h->tc_n_ksteps;
+  a.tc_item_kbeg = (const int*)P(i_kbeg);
+  a.tc_item_flags = (const int*)P(i_flags);
+  a.tc_out_rows = (const int*)P(i_orows);
+  a.tc_cols = (const int*)P(i_cols);
+  a.tc_vals = P(i_vals);
+  a.tc_scales = nullptr;
+  a.tc_nnz_id = h->tc_nnz_id ? (const int*)P(i_tnid) : nullptr;
+  a.ell_n_items = h->ell_n_items;
+  a.ell_item_row0 = (const int*)P(i_erow0);
+  a.ell_item_K = (const int*)P(i_eK);
+  a.ell_item_slot0 = (const int*)P(i_eslot);
+  a.ell_item_flags = (const int*)P(i_eflag);
+  a.ell_out_row = (const int*)P(i_eout);
+  a.ell_row_len = (const int*)P(i_elen);
+  a.ell_vals = (const float*)P(i_evals);
+  a.ell_kidx = (const int*)P(i_ekidx);
+  a.ell_nnz_id = h->ell_nnz_id ? (const int*)P(i_enid) : nullptr;
+  a.err_flag = plan->err_flag;
+  plan->M = h->M;
+  plan->K = h->K;
+  plan->nnz = h->nnz;
+  plan->ell_n_slots = h->ell_n_slots;
+  plan->n_zero_rows = h->n_zero_rows;
+  plan->zero_rows = (const int*)P(i_zero);
+  *out = plan;
+  return STILE_OK;
+}
+
+int stile_spmm_plan_free(StileSpmmPlan* plan) {
+  if (!plan) return STILE_OK;
+  cudaError_t e = cudaFree(plan->arena);
+  delete plan;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFree(plan)");
+  return STILE_OK;
+}
+
+static int check_dense(long ld, int N, const void* ptr, const char* name) {
+  if (!ptr) return fail(STILE_E_INVALID, std::string("null ") + name);
+  if (ld < N || (ld % 4) != 0)
+    return fail(STILE_E_INVALID, std::string(name) + ": row stride must be >= N and a multiple of 4");
+  if ((reinterpret_cast<uintptr_t>(ptr) & 15) != 0)
+    return fail(STILE_E_INVALID, std::string(name) + ": must be 16-byte aligned");
+  return STILE_OK;
+}
+
+int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float* C, int64_t ldc,
+                   int32_t N, void* stream) {
+  if (!plan) return fail(STILE_E_INVALID, "null plan");
+  if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
+  int rc;
+  if ((rc = check_dense(ldb, N, B, "B")) != 0) return rc;
+  if ((rc = check_dense(ldc, N, C, "C")) != 0) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = stile::launch_zero_rows(plan->zero_rows, plan->n_zero_rows, C, ldc, N, st);
+  if (e != cudaSuccess) return cuda_fail(e, "zero_rows launch");
+  if (plan->n_zero_rows) g_launches++;
+  stile::SpmmArgs a = plan->args;
+  a.B = B;
+  a.ldb = ldb;
+  a.C = C;
+  a.ldc = ldc;
+  a.N = N;
+  a.n_fchunks = (N + 127) / 128;
+  a.tc_ctas = a.tc_n_items * a.n_fchunks;
+  e = stile::launch_fused(a, st);
+  if (e != cudaSuccess) return cuda_fail(e, "fused SpMM launch");
+  if (a.tc_ctas + a.ell_n_items) g_launches++;
+  return STILE_OK;
+}
+
+int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, const float* B,
+                     int64_t ldb, float* dvals, int32_t N, void* stream) {
+  if (!plan) return fail(STILE_E_INVALID, "null plan");
+  if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
+  if (!dvals) return fail(STILE_E_INVALID, "null dvals");
+  if ((plan->args.tc_n_items && !plan->args.tc_nnz_id) ||
+      (plan->args.ell_n_items && !plan->args.ell_nnz_id))
+    return fail(STILE_E_INVALID, "plan was uploaded without nonzero ids");
+  int rc;
+  if ((rc = check_dense(ldb, N, B, "B")) != 0) return rc;
+  if ((rc = check_dense(lddy, N, dY, "dY")) != 0) return rc;
+  stile::SpmmArgs a = plan->args;
+  a.B = B;
+  a.ldb = ldb;
+  a.N = N;
+  cudaError_t e = stile::launch_dvals(a, dY, lddy, dvals, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
+  if (a.tc_n_ksteps + a.ell_n_items) g_launches++;
+  return STILE_OK;
+}
+
+int stile_spmm_plan_set_values(StileSpmmPlan* plan, const float* vals, void* stream) {
+  if (!plan || !vals) return fail(STILE_E_INVALID, "null argument");
+  if ((plan->args.tc_n_items && !plan->args.tc_nnz_id) ||
+      (plan->args.ell_n_items && !plan->args.ell_nnz_id))
+    return fail(STILE_E_INVALID, "plan was uploaded without nonzero ids");
+  cudaError_t e = stile::launch_repack(plan->args, vals, plan->ell_n_slots,
+                                       static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "value re-pack launch");
+  g_launches++;
+  return STILE_OK;
+}
+
+int stile_spmm_plan_error_flag(StileSpmmPlan* plan, void* stream, int32_t* flag) {
+  if (!plan || !flag) return fail(STILE_E_INVALID, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int host = 0;
+  cudaError_t e = cudaMemcpyAsync(&host, plan->err_flag, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(plan->err_flag, 0, 4, st);
+  if (e != cudaSuccess) return cuda_fail(e, "error flag readback");
+  *flag = host;
+  return STILE_OK;
+}
+
+int stile_csr_spmm_run(int32_t M, const int32_t* indptr, const int32_t* indices, const float* vals,
+                       const float* B, int64_t ldb, float* C, int64_t ldc, int32_t N, void* stream) {
+  if (M < 0 || N <= 0) return fail(STILE_E_INVALID, "bad shape");
+  if (M == 0) return STILE_OK;
+  if (!indptr || !indices || !vals) return fail(STILE_E_INVALID, "null CSR array");
+  int rc;
+  if ((rc = check_dense(ldb, N, B, "B")) != 0) return rc;
+  if ((rc = check_dense(ldc, N, C, "C")) != 0) return rc;
+  cudaError_t e = stile::launch_csr_spmm(M, indptr, indices, vals, B, ldb, C, ldc, N,
+                                         static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "CSR SpMM launch");
+  g_launches++;
+  return STILE_OK;
+}
+
+int stile_sddmm_plan_upload(const StileSddmmPlanHost* h, StileSddmmPlan** out) {
+  if (!h || !out) return fail(STILE_E_INVALID, "null argument");
+  *out = nullptr;
+  if (h->n_1d < 0 || h->n_blk < 0 || h->n_blk_nnz < 0) return fail(STILE_E_INVALID, "negative count");
+  if (h->n_1d > 0) {
+    if (!h->mid_idx || !h->j_idx || !h->remap) return fail(STILE_E_INVALID, "missing 1D array");
+    if (!in_range(h->mid_idx, h->n_1d, 0, h->M) || !in_range(h->j_idx, h->n_1d, 0, h->K) ||
+        !in_range(h->remap, h->n_1d, 0, h->nnz))
+      return fail(STILE_E_INVALID, "1D index out of range");
+  }
+  if (h->n_blk > 0) {
+    if (h->bm <= 0 || h->bn <= 0 || h->bm > 16 || h->bn > 16)
+      return fail(STILE_E_UNSUPPORTED, "block tiles larger than 16x16");
+    if (!h->blk_i || !h->blk_j || !h->blk_indptr || !h->blk_dense_pos || !h->blk_out)
+      return fail(STILE_E_INVALID, "missing block array");
+    if (h->blk_indptr[0] != 0 || h->blk_indptr[h->n_blk] != h->n_blk_nnz)
+      return fail(STILE_E_INVALID, "blk_indptr does not span the entries");
+    for (int b = 0; b < h->n_blk; ++b) {
+      const int n = h->blk_indptr[b + 1] - h->blk_indptr[b];
+      if (n < 0 || n > h->bm * h->bn) return fail(STILE_E_INVALID, "bad blk_indptr");
+    }
+    if (!in_range(h->blk_i, (long)h->n_blk * h->bm, 0, h->M) ||
+        !in_range(h->blk_j, (long)h->n_blk * h->bn, 0, h->K) ||
+        !in_range(h->blk_dense_pos, h->n_blk_nnz, 0, h->bm * h->bn) ||
+        !in_range(h->blk_out, h->n_blk_nnz, 0, h->nnz))
+      return fail(STILE_E_INVALID, "block index out of range");
+  }
+  Arena ar;
+  size_t a0 = ar.add(h->mid_idx, (size_t)h->n_1d * 4);
+  size_t a1 = ar.add(h->j_idx, (size_t)h->n_1d * 4);
+  size_t a2 = ar.add(h->remap, (size_t)h->n_1d * 4);
+  size_t a3 = ar.add(h->blk_i, (size_t)h->n_blk * h->bm * 4);
+  size_t a4 = ar.add(h->blk_j, (size_t)h->n_blk * h->bn * 4);
+  size_t a5 = ar.add(h->blk_indptr, h->n_blk ? (size_t)(h->n_blk + 1) * 4 : 0);
+  size_t a6 = ar.add(h->blk_dense_pos, (size_t)h->n_blk_nnz * 4);
+  size_t a7 = ar.add(h->blk_out, (size_t)h->n_blk_nnz * 4);
+  auto* plan = new StileSddmmPlan();
+  cudaError_t e = cudaMalloc(&plan->arena, ar.total ? ar.total : 256);
+  if (e != cudaSuccess) {
+    delete plan;
+    return cuda_fail(e, "cudaMalloc(plan)");
+  }
+  char* base = static_cast<char*>(plan->arena);
+  for (size_t i = 0; i < ar.parts.size(); ++i) {
+    if (ar.parts[i].first && ar.parts[i].second) {
+      e = cudaMemcpy(base + ar.offs[i], ar.parts[i].first, ar.parts[i].second, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        cudaFree(plan->arena);
+        delete plan;
+        return cuda_fail(e, "cudaMemcpy(plan)");
+      }
+    }
+  }
+  auto P = [&](size_t idx) { return (const int*)(base + ar.offs[idx]); };
+  stile::SddmmArgs& a = plan->args;
+  a.n_1d = h->n_1d;
+  a.mid_idx = P(a0);
+  a.j_idx = P(a1);
+  a.remap = P(a2);
+  a.n_blk = h->n_blk;
+  a.bm = h->bm;
+  a.bn = h->bn;
+  a.blk_i = P(a3);
+  a.blk_j = P(a4);
+  a.blk_indptr = P(a5);
+  a.blk_dense_pos = P(a6);
+  a.blk_out = P(a7);
+  plan->M = h->M;
+  plan->K = h->K;
+  plan->nnz = h->nnz;
+  *out = plan;
+  return STILE_OK;
+}
+
+int stile_sddmm_plan_free(StileSddmmPlan* plan) {
+  if (!plan) return STILE_OK;
+  cudaError_t e = cudaFree(plan->arena);
+  delete plan;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFree(plan)");
+  return STILE_OK;
+}
+
+int stile_sddmm_run(const StileSddmmPlan* plan, const float* X, int64_t ldx, const float* Y,
+                    int64_t ldy, float* out, int32_t F, void* stream) {
+  if (!plan) return fail(STILE_E_INVALID, "null plan");
+  if (F <= 0) return fail(STILE_E_INVALID, "F must be positive");
+  if (!out) return fail(STILE_E_INVALID, "null out");
+  int rc;
+  if ((rc = check_dense(ldx, F, X, "X")) != 0) return rc;
+  if ((rc = check_dense(ldy, F, Y, "Y")) != 0) return rc;
+  stile::SddmmArgs a = plan->args;
+  a.X = X;
+  a.ldx = ldx;
+  a.Y = Y;
+  a.ldy = ldy;
+  a.out = out;
+  a.F = F;
+  cudaError_t e = stile::launch_sddmm(a, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "SDDMM launch");
+  g_launches += (a.n_blk > 0) + (a.n_1d > 0);
+  return STILE_OK;
+}
+
+int stile_debug_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
+                           uint32_t idesc, float* out, int32_t* err, void* stream) {
+  if (!a_img || !b_img || !desc6 || !out || !err) return fail(STILE_E_INVALID, "null argument");
+  // every address the descriptors can form must stay inside the 8 KB images:
+  // at most 16 core-matrix groups along either direction
+  for (int i = 0; i < 2; ++i) {
+    const uint32_t lbo = desc6[3 * i], sbo = desc6[3 * i + 1], lay = desc6[3 * i + 2];
+    if (lbo > 2048 || sbo > 2048 || (lbo & 15) || (sbo & 15))
+      return fail(STILE_E_INVALID, "probe strides must be multiples of 16 and <= 2048");
+    if (lay != 0 && lay != 2 && lay != 4 && lay != 6) return fail(STILE_E_INVALID, "bad layout type");
+  }
+  cudaError_t e = stile::launch_umma_probe(a_img, b_img, desc6, idesc, out, err,
+                                           static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "probe launch");
+  g_launches++;
+  return STILE_OK;
+}
+
+}  // extern "C"

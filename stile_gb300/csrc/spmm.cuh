@@ -1,0 +1,78 @@
+// Kernel argument block and launchers of the SpMM kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/stile_gb300.h"
+
+namespace stile {
+
+struct SpmmArgs {
+  // dense operands
+  const float* B;
+  long ldb;
+  float* C;
+  long ldc;
+  int N;
+  int n_fchunks;  // ceil(N / 128): tensor-core feature chunks
+  int tc_ctas;    // tc_n_items * n_fchunks
+  int tc_mode;
+  // tensor-core items
+  int tc_n_items, tc_n_ksteps;
+  const int* tc_item_kbeg;
+  const int* tc_item_flags;
+  const int* tc_out_rows;
+  const int* tc_cols;
+  const void* tc_vals;
+  const float* tc_scales;
+  const int* tc_nnz_id;
+  // ELL items
+  int ell_n_items;
+  const int* ell_item_row0;
+  const int* ell_item_K;
+  const int* ell_item_slot0;
+  const int* ell_item_flags;
+  const int* ell_out_row;
+  const int* ell_row_len;
+  const float* ell_vals;
+  const int* ell_kidx;
+  const int* ell_nnz_id;
+  // device error flag (bounded waits that gave up)
+  int* err_flag;
+};
+
+cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const float* vals,
+                            const float* B, long ldb, float* C, long ldc, int N, cudaStream_t st);
+cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st);
+cudaError_t launch_fused(const SpmmArgs& p, cudaStream_t st);
+cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals,
+                         cudaStream_t st);
+size_t fused_smem_bytes(int mode);
+cudaError_t launch_repack(const SpmmArgs& p, const float* vals, long n_ell_slots, cudaStream_t st);
+
+struct SddmmArgs {
+  const float* X;
+  long ldx;
+  const float* Y;
+  long ldy;
+  float* out;
+  int F;
+  int n_1d;
+  const int* mid_idx;
+  const int* j_idx;
+  const int* remap;
+  int n_blk, bm, bn;
+  const int* blk_i;
+  const int* blk_j;
+  const int* blk_indptr;
+  const int* blk_dense_pos;
+  const int* blk_out;
+};
+
+cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st);
+
+cudaError_t launch_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
+                              uint32_t idesc, float* out, int* err, cudaStream_t st);
+
+}  // namespace stile

@@ -1,0 +1,216 @@
+"""Torch-facing wrappers over the C ABI (device memory, streams and the
+autograd plumbing; the computation is in the sm_103a kernels)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import SddmmDevice, SpmmDevice
+
+
+def _ptr(a: np.ndarray, ct=ctypes.c_int32):
+    return a.ctypes.data_as(ctypes.POINTER(ct)) if a is not None and a.size else None
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _require_cuda(t: torch.Tensor, name: str):
+    if not t.is_cuda:
+        raise RuntimeError(f"{name} must be a CUDA tensor (there is no CPU path)")
+
+
+def dense_operand(x: torch.Tensor, name="B"):
+    """fp32, CUDA, row-major with a row stride that is a multiple of 4 and
+    a 16-byte aligned base; copies only when needed."""
+    _require_cuda(x, name)
+    if x.dtype != torch.float32:
+        x = x.float()
+    if x.dim() != 2:
+        raise ValueError(f"{name} must be 2-D")
+    rows, cols = x.shape
+    ld = x.stride(0)
+    ok = x.stride(1) == 1 and ld >= cols and ld % 4 == 0 and x.data_ptr() % 16 == 0
+    if not ok:
+        ldp = (cols + 3) // 4 * 4
+        buf = torch.zeros((rows, ldp), dtype=torch.float32, device=x.device)
+        buf[:, :cols] = x
+        x = buf[:, :cols]
+        ld = ldp
+    return x, ld
+
+
+def new_output(rows, cols, device):
+    ldp = (cols + 3) // 4 * 4
+    buf = torch.empty((rows, ldp), dtype=torch.float32, device=device)
+    return buf[:, :cols], ldp
+
+
+class DeviceSpmmPlan:
+    """A packed SpMM plan resident on the current CUDA device."""
+
+    def __init__(self, dev: SpmmDevice):
+        self.lib = _lib.load()
+        self.dev = dev
+        self.M, self.K, self.nnz = dev.M, dev.K, dev.nnz
+        h = _lib.SpmmPlanHost()
+        h.M, h.K, h.nnz = dev.M, dev.K, dev.nnz
+        h.tc_mode = dev.tc_mode
+        h.tc_n_items = len(dev.tc_item_flags)
+        h.tc_n_ksteps = len(dev.tc_cols) // 16
+        self._keep = [dev.tc_item_kbeg, dev.tc_item_flags, dev.tc_out_rows, dev.tc_cols, dev.tc_vals,
+                      dev.tc_nnz_id, dev.ell_item_row0, dev.ell_item_K, dev.ell_item_slot0,
+                      dev.ell_item_flags, dev.ell_out_row, dev.ell_row_len, dev.ell_vals, dev.ell_kidx,
+                      dev.ell_nnz_id, dev.zero_rows]
+        h.tc_item_kbeg = _ptr(dev.tc_item_kbeg)
+        h.tc_item_flags = _ptr(dev.tc_item_flags)
+        h.tc_out_rows = _ptr(dev.tc_out_rows)
+        h.tc_cols = _ptr(dev.tc_cols)
+        h.tc_vals = dev.tc_vals.ctypes.data if dev.tc_vals.size else None
+        h.tc_kstep_bytes = dev.tc_kstep_bytes
+        h.tc_scales = None
+        h.tc_nnz_id = _ptr(dev.tc_nnz_id)
+        h.ell_n_items = len(dev.ell_item_K)
+        h.ell_n_rows = len(dev.ell_out_row)
+        h.ell_n_slots = len(dev.ell_kidx)
+        h.ell_item_row0 = _ptr(dev.ell_item_row0)
+        h.ell_item_K = _ptr(dev.ell_item_K)
+        h.ell_item_slot0 = _ptr(dev.ell_item_slot0)
+        h.ell_item_flags = _ptr(dev.ell_item_flags)
+        h.ell_out_row = _ptr(dev.ell_out_row)
+        h.ell_row_len = _ptr(dev.ell_row_len)
+        h.ell_vals = _ptr(dev.ell_vals, ctypes.c_float)
+        h.ell_kidx = _ptr(dev.ell_kidx)
+        h.ell_nnz_id = _ptr(dev.ell_nnz_id)
+        h.n_zero_rows = len(dev.zero_rows)
+        h.zero_rows = _ptr(dev.zero_rows)
+        handle = ctypes.c_void_p()
+        _lib.check(self.lib.stile_spmm_plan_upload(ctypes.byref(h), ctypes.byref(handle)),
+                   "stile_spmm_plan_upload")
+        self.handle = handle
+
+    def run(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        B, ldb = dense_operand(B, "B")
+        if B.shape[0] != self.K:
+            raise ValueError(f"B has {B.shape[0]} rows, the plan has K={self.K}")
+        N = B.shape[1]
+        if out is None:
+            out, ldc = new_output(self.M, N, B.device)
+        else:
+            ldc = out.stride(0)
+        _lib.check(self.lib.stile_spmm_run(self.handle, B.data_ptr(), ldb, out.data_ptr(), ldc, N, _stream()),
+                   "stile_spmm_run")
+        return out
+
+    def dvals(self, dY: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+        dY, lddy = dense_operand(dY, "dY")
+        B, ldb = dense_operand(B, "B")
+        out = torch.zeros(self.nnz, dtype=torch.float32, device=B.device)
+        _lib.check(self.lib.stile_spmm_dvals(self.handle, dY.data_ptr(), lddy, B.data_ptr(), ldb,
+                                             out.data_ptr(), B.shape[1], _stream()), "stile_spmm_dvals")
+        return out
+
+    def set_values(self, vals: torch.Tensor):
+        _require_cuda(vals, "vals")
+        vals = vals.float().contiguous()
+        if vals.numel() != self.nnz:
+            raise ValueError("vals must have one entry per nonzero")
+        _lib.check(self.lib.stile_spmm_plan_set_values(self.handle, vals.data_ptr(), _stream()),
+                   "stile_spmm_plan_set_values")
+
+    def error_flag(self) -> int:
+        f = ctypes.c_int32(0)
+        _lib.check(self.lib.stile_spmm_plan_error_flag(self.handle, _stream(), ctypes.byref(f)),
+                   "stile_spmm_plan_error_flag")
+        return int(f.value)
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.stile_spmm_plan_free(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceSddmmPlan:
+    def __init__(self, dev: SddmmDevice):
+        self.lib = _lib.load()
+        self.dev = dev
+        self.M, self.K, self.nnz = dev.M, dev.K, dev.nnz
+        h = _lib.SddmmPlanHost()
+        h.M, h.K, h.nnz = dev.M, dev.K, dev.nnz
+        h.n_1d = len(dev.mid_idx)
+        h.mid_idx, h.j_idx, h.remap = _ptr(dev.mid_idx), _ptr(dev.j_idx), _ptr(dev.remap)
+        h.n_blk = len(dev.blk_indptr) - 1
+        h.bm, h.bn = dev.bm, dev.bn
+        h.n_blk_nnz = len(dev.blk_out)
+        h.blk_i, h.blk_j = _ptr(dev.blk_i), _ptr(dev.blk_j)
+        h.blk_indptr = _ptr(dev.blk_indptr)
+        h.blk_dense_pos, h.blk_out = _ptr(dev.blk_dense_pos), _ptr(dev.blk_out)
+        self._keep = [dev.mid_idx, dev.j_idx, dev.remap, dev.blk_i, dev.blk_j, dev.blk_indptr,
+                      dev.blk_dense_pos, dev.blk_out]
+        handle = ctypes.c_void_p()
+        _lib.check(self.lib.stile_sddmm_plan_upload(ctypes.byref(h), ctypes.byref(handle)),
+                   "stile_sddmm_plan_upload")
+        self.handle = handle
+
+    def run(self, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        X, ldx = dense_operand(X, "X")
+        Y, ldy = dense_operand(Y, "Y")
+        if X.shape[1] != Y.shape[1]:
+            raise ValueError("X and Y must have the same feature count")
+        if out is None:
+            out = torch.zeros(self.nnz, dtype=torch.float32, device=X.device)
+        _lib.check(self.lib.stile_sddmm_run(self.handle, X.data_ptr(), ldx, Y.data_ptr(), ldy,
+                                            out.data_ptr(), X.shape[1], _stream()), "stile_sddmm_run")
+        return out
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.stile_sddmm_plan_free(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CsrMatrix:
+    """A CSR matrix resident on the device for the plain CSR-row kernel."""
+
+    def __init__(self, A, device="cuda"):
+        import scipy.sparse as sp
+        A = sp.csr_matrix(A)
+        A.sort_indices()
+        self.shape = A.shape
+        self.nnz = A.nnz
+        self.indptr = torch.as_tensor(A.indptr.astype(np.int32), device=device)
+        self.indices = torch.as_tensor(A.indices.astype(np.int32), device=device)
+        self.vals = torch.as_tensor(A.data.astype(np.float32), device=device)
+        self.lib = _lib.load()
+
+    def spmm(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        B, ldb = dense_operand(B, "B")
+        N = B.shape[1]
+        if out is None:
+            out, ldc = new_output(self.shape[0], N, B.device)
+        else:
+            ldc = out.stride(0)
+        _lib.check(self.lib.stile_csr_spmm_run(self.shape[0], self.indptr.data_ptr(), self.indices.data_ptr(),
+                                               self.vals.data_ptr(), B.data_ptr(), ldb, out.data_ptr(), ldc,
+                                               N, _stream()), "stile_csr_spmm_run")
+        return out
+
+
+def launch_count() -> int:
+    return int(_lib.load().stile_launch_count())

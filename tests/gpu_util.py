@@ -1,0 +1,71 @@
+"""Helpers shared by the GPU tests."""
+import ctypes
+import functools
+
+import numpy as np
+import scipy.sparse as sp
+
+# layout the fused kernel uses (see stile_gb300/csrc/spmm.cu):
+# A operand MN-major 128B-swizzle, LBO = 2048 (between 64-wide MN atoms),
+# SBO = 1024 (between 8-row K groups); B operand K-major no-swizzle,
+# LBO = 128 (K direction), SBO = 256 (row direction)
+KERNEL_DESC = (2048, 1024, 2, 128, 256, 0)
+
+
+def bf16_round(x):
+    from stile_gb300.device import _to_bf16_bits, _bf16_bits_to_f32
+    return _bf16_bits_to_f32(_to_bf16_bits(np.asarray(x, np.float32)))
+
+
+def a_image(A, lbo=2048, sbo=1024):
+    """A [128 (m) x 16 (k)] -> 8 KB MN-major 128B-swizzled image (bf16)."""
+    from stile_gb300.device import _to_bf16_bits
+    img = np.zeros(4096, dtype=np.uint16)
+    bits = _to_bf16_bits(A.astype(np.float32))
+    for m in range(128):
+        for k in range(16):
+            off = (m // 64) * lbo + (k // 8) * sbo + (k % 8) * 128 + ((((m % 64) // 8) ^ (k % 8)) << 4) + (m % 8) * 2
+            img[off // 2] = bits[m, k]
+    return img
+
+
+def b_image(Bm):
+    """B [16 (n) x 16 (k)] -> K-major no-swizzle image (bf16), as the plan stores it."""
+    from stile_gb300.device import _to_bf16_bits, operand_image_16bit
+    img = np.zeros(4096, dtype=np.uint16)
+    img[:256] = operand_image_16bit(_to_bf16_bits(Bm.astype(np.float32)).reshape(1, 16, 16))[0]
+    return img
+
+
+def run_probe(A, Bm, desc6):
+    import torch
+    from stile_gb300 import _lib
+    lib = _lib.load()
+    ai = torch.as_tensor(a_image(A, desc6[0], desc6[1]).view(np.int16).copy(), device="cuda")
+    bi = torch.as_tensor(b_image(Bm).view(np.int16).copy(), device="cuda")
+    out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    d = (ctypes.c_uint32 * 6)(*desc6)
+    idesc = (1 << 4) | (1 << 7) | (1 << 10) | (1 << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
+    rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, out.data_ptr(), err.data_ptr(),
+                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc, "probe")
+    torch.cuda.synchronize()
+    return out.cpu().numpy().reshape(128, 16), int(err.item())
+
+
+@functools.lru_cache(maxsize=None)
+def umma_layout_ok():
+    rng = np.random.default_rng(5)
+    A = bf16_round(rng.standard_normal((128, 16)))
+    Bm = bf16_round(rng.standard_normal((16, 16)))
+    D, err = run_probe(A, Bm, KERNEL_DESC)
+    ref = A.astype(np.float64) @ Bm.astype(np.float64).T
+    return err == 0 and np.allclose(D, ref, rtol=1e-5, atol=1e-4)
+
+
+def random_values(A, seed=0, dist="uniform"):
+    A = sp.csr_matrix(A, dtype=np.float64).copy()
+    rng = np.random.default_rng(seed)
+    A.data = rng.uniform(-1, 1, size=A.nnz) if dist == "uniform" else rng.standard_normal(A.nnz)
+    return A

@@ -1,0 +1,26 @@
+"""Tensor-core layout self-check: one tcgen05.mma on operand images laid out
+the way the fused kernel lays them out must equal A @ B^T.  The probe keeps
+every possible descriptor interpretation inside its shared memory, so this
+test runs before any fused-kernel test."""
+import numpy as np
+import pytest
+
+from gpu_util import KERNEL_DESC, bf16_round, run_probe
+
+pytestmark = pytest.mark.gpu
+
+
+def test_umma_layout_matches_kernel_convention():
+    rng = np.random.default_rng(5)
+    A = bf16_round(rng.standard_normal((128, 16)))
+    Bm = bf16_round(rng.standard_normal((16, 16)))
+    ref = A.astype(np.float64) @ Bm.astype(np.float64).T
+    report = {}
+    for a_lbo, a_sbo in [(2048, 1024), (1024, 2048)]:
+        for b_lbo, b_sbo in [(128, 256), (256, 128)]:
+            desc = (a_lbo, a_sbo, 2, b_lbo, b_sbo, 0)
+            D, err = run_probe(A, Bm, desc)
+            report[desc] = (err, float(np.abs(D - ref).max()))
+    print("probe report:", report)
+    err, maxdiff = report[KERNEL_DESC]
+    assert err == 0 and maxdiff < 1e-3, report
