@@ -160,6 +160,12 @@ def _cases():
                                     A=lambda: syn.community_graph(n=8192, target_nnz=60000, seed=9,
                                                                   values="ones", max_deg=1024),
                                     N=128, only_TC=False, only_ELL=False),
+        # dense blocks next to hub rows (atomic TC tiles, then withdraw)
+        "spmm_hubblocks_4096": dict(op="spmm", A=lambda: _hub_blocks(4096, 4, 60, 1500), N=64,
+                                    only_TC=False, only_ELL=False),
+        # power-law rows + dense blocks (atomic ELL tiles next to TC tiles)
+        "spmm_mixed_2048": dict(op="spmm", A=lambda: _mixed_blocks(2048, 1, 40, 8, 256), N=64,
+                                only_TC=False, only_ELL=False),
         # block + unstructured pruned weight (scaled-down)
         "spmm_pruned_256x192": dict(op="spmm",
                                     A=lambda: _ones(syn.pruned_weight(256, 192, seed=5)),
@@ -175,6 +181,33 @@ def _cases():
                                 A=lambda: syn.sddmm_mask(n=2048, target_nnz=40000, seed=8, max_len=512),
                                 N=32, only_TC=False, only_ELL=False),
     }
+
+
+def _hub_blocks(n, seed, nblk, hub_len, bw=64):
+    """Power-law rows plus dense 16 x bw blocks, each sharing its 16-row
+    window with one long (hub) row: atomic tensor-core tiles are selected
+    first and later withdrawn in favour of whole-row tiles."""
+    from stile_gb300 import synthetic as syn
+    rng = np.random.default_rng(seed)
+    A = syn.power_law_rows(n, n, min_len=2, max_len=64, seed=seed, values="ones").tolil()
+    for _ in range(nblk):
+        r = rng.integers(0, n // 16) * 16
+        c = rng.integers(0, n - bw)
+        A[r:r + 16, c:c + bw] = 1
+        A[r + rng.integers(0, 16), rng.choice(n, size=hub_len, replace=False)] = 1
+    return _ones(sp.csr_matrix(A))
+
+
+def _mixed_blocks(n, seed, nblk, min_len, max_len, bw=64):
+    """Power-law rows plus dense 16 x bw blocks anywhere."""
+    from stile_gb300 import synthetic as syn
+    rng = np.random.default_rng(seed)
+    A = syn.power_law_rows(n, n, min_len=min_len, max_len=max_len, seed=seed, values="ones").tolil()
+    for _ in range(nblk):
+        r = rng.integers(0, n // 16) * 16
+        c = rng.integers(0, n - bw)
+        A[r:r + 16, c:c + bw] = 1
+    return _ones(sp.csr_matrix(A))
 
 
 def _ones(A):

@@ -1,0 +1,35 @@
+"""The planner (tile generation + greedy/local search + withdraw over the
+reference's A100 cost calibration) selects the same plan as the reference on
+every golden case: packing both plans gives bit-identical arrays."""
+import numpy as np
+import pytest
+
+from conftest import golden_files
+import oracle.semantics as S
+from stile_gb300 import emit
+from stile_gb300.planner import plan_spmm
+
+
+@pytest.mark.parametrize("path", golden_files("spmm"), ids=lambda p: p.split("/")[-1][:-4])
+def test_spmm_plan_matches_reference(path):
+    meta, arr = S.load_fixture(path)
+    A = S.fixture_matrix(meta, arr)
+    plan = plan_spmm(A, meta["N"], max_bucket_size=meta["max_bucket_size"], only_TC=meta["only_TC"],
+                     only_ELL=meta["only_ELL"])
+    fm, args, out_shape = emit.emit_spmm_reference(plan.tiles, meta["idx_lens"][0], meta["N"])
+    assert list(out_shape) == meta["out_shape"]
+    assert [f.template for f in fm] == [f["template"] for f in meta["formats"]]
+    assert [len(f.tiles) for f in fm] == [f["n_tiles"] for f in meta["formats"]]
+    for a, r in zip(args, S.fixture_args(meta, arr)):
+        for x, y in zip(a, r):
+            x, y = np.asarray(x), np.asarray(y)
+            assert x.shape == y.shape
+            assert np.array_equal(x.astype(y.dtype), y)
+
+
+def test_max_bucket_size_estimate():
+    from stile_gb300.planner import estimate_max_bucket_size
+    # my_search_formats.py:965-981 with SM_num 108
+    assert estimate_max_bucket_size(14687) == 8
+    assert estimate_max_bucket_size(160081) == 32
+    assert estimate_max_bucket_size(1_000) == 4
