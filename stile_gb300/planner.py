@@ -956,3 +956,292 @@ def plan_spmm(A, N, cost: CostModel = A100_FP16, **kw) -> Plan:
     with warnings.catch_warnings():
         warnings.simplefilter("ignore", RuntimeWarning)
         return SpmmPlanner(A, N, cost=cost, **kw).search()
+
+
+# ---------------------------------------------------------------------------
+# SDDMM
+# ---------------------------------------------------------------------------
+class SddmmPlanner:
+    """SDDMM branch of the same search: 1D nonzero-chunk tiles against
+    16x16 tensor-core blocks (gen_candidate_formats_BSDDMM :1837-1900; the
+    SDDMM paths of search_best_TC_tile_given_csr / _given_op,
+    local_search_TC_tiles*, search_best_tile_given_op_BSDDMM,
+    local_search_1D_BSDDMM; post_process_for_withdraw_BSDDMM :1709-1751)."""
+
+    def __init__(self, A, F, cost: CostModel = A100_FP16, max_bucket_size=32, only_TC=False, only_ELL=False,
+                 max_avg_cost_diff=0.2, max_level_num=float("inf"), single_level=False):
+        self.pat = Pattern(A)
+        self.F = int(F)
+        self.cost = cost
+        self.mbs = max_bucket_size
+        self.only_TC, self.only_ELL = only_TC, only_ELL
+        self.max_avg_cost_diff = float("inf") if (only_TC or only_ELL) else max_avg_cost_diff
+        self.max_level_num = max_level_num
+        self.single_level = single_level
+        self.uncovered = np.ones(self.pat.nnz, dtype=bool)
+        js = [j for j in (16, 32, 64) if j <= self.F]
+        self.tile_j = max(js) if js else None
+
+    def _ts(self):
+        return ((None, 16), (None, self.tile_j), (None, 16))
+
+    def _tc_cost(self):
+        return self.cost.tc_sddmm_cost(self.tile_j, 16)
+
+    def _scale(self):
+        return math.ceil(self.F / self.tile_j)
+
+    def search(self):
+        pat = self.pat
+        F = self.F
+        oned = OneDOp(pat, np.arange(pat.nnz), self.mbs, 0)
+        tc = None
+        nid = 1
+        if not self.only_ELL and self.tile_j is not None:
+            ident = np.arange(pat.M, dtype=np.int64)
+            by_len = np.argsort(-pat.row_nnz, kind="stable")
+            cands = [TcOp(pat, ident, nid, op_type="sddmm")]
+            if not np.array_equal(by_len, ident):
+                cands.append(TcOp(pat, by_len, nid, op_type="sddmm"))
+            best, bd = None, 0
+            for c in cands:
+                d = c.density()
+                if d > bd:
+                    best, bd = c, d
+            tc = best if best is not None else cands[0]
+            nid += 1
+        self.tc = tc
+        self.next_id = nid
+        all_subops = [] if self.only_TC else [oned]
+        best_possible = self.cost.one_d_lower_bound(F, self.mbs) if all_subops else float("inf")
+        selected = []
+        level_num = 1
+        if tc is not None and all_subops and not self.only_TC:
+            selected = self._rows_pass(best_possible)
+            if not self.single_level:
+                all_subops = [self._next_1d()]
+        guard = 0
+        while self.uncovered.any():
+            guard += 1
+            if guard > 100000:
+                raise RuntimeError("SDDMM format search did not converge")
+            good_tc = []
+            if tc is not None:
+                key, best_tc = self._search_tc_op()
+                if key is not None:
+                    b, kp = key
+                    t = self._tc_tile(b, kp)
+                    t.nnz_unc = F * len(tc.tile_entries(b, t.k_rng[0], t.k_rng[1], self.uncovered)[2])
+                    t.pred_cost = best_tc * t.nnz_unc
+                    with np.errstate(divide="ignore", invalid="ignore"):
+                        t.pred_avg = t.pred_cost / np.float32(t.nnz_unc)
+                    good_tc = [t]
+            init_avg = good_tc[0].pred_avg if good_tc else float("inf")
+            chosen = good_tc
+            if not (init_avg < best_possible) and all_subops:
+                t = self._search_1d(all_subops, init_avg)
+                if t is not None:
+                    chosen = [t]
+            if not chosen:
+                raise RuntimeError("no tile can cover the remaining SDDMM elements")
+            best_avg = chosen[0].pred_avg
+            target = best_avg * (1 + self.max_avg_cost_diff) if best_avg >= 0 else \
+                best_avg * (1 - self.max_avg_cost_diff)
+            if chosen[0].kind == TC_SDDMM:
+                good = self._local_tc(chosen[0], target)
+            else:
+                good = self._local_1d(chosen[0], target)
+            for t in good:
+                self._finalise(t)
+            selected.extend(good)
+            for t in good:
+                self.uncovered[t.cov_ids] = False
+            if not self.uncovered.any():
+                break
+            nxt = level_num < self.max_level_num and chosen[0].kind == TC_SDDMM
+            if self.single_level:
+                nxt = level_num < 1
+            if nxt:
+                level_num += 1
+                all_subops = [self._next_1d()]
+        return self._post_process(selected, level_num)
+
+    # ---------------- operators / tiles ----------------
+    def _next_1d(self):
+        op = OneDOp(self.pat, np.nonzero(self.uncovered)[0], self.mbs, self.next_id)
+        self.next_id += 1
+        return op
+
+    def _tc_tile(self, b, kpos):
+        Kt = 16
+        r0 = 16 * b
+        r1 = min(16 * (b + 1), self.pat.M) - 1
+        k0 = int(Kt * kpos)
+        k1 = min(int(Kt * (kpos + 1)), self.pat.K) - 1
+        return _Sel(op=self.tc, kind=TC_SDDMM, ts=self._ts(), pos=(int(b), 0, kpos), atomic=False,
+                    j_num=self.F, i_rng=(r0, r1), k_rng=(k0, k1), best_ts=self._ts(), params=dict(TC_PARAMS))
+
+    def _finalise(self, t):
+        if t.kind == TC_SDDMM:
+            lr, lc, ids = self.tc.tile_entries(t.pos[0], t.k_rng[0], t.k_rng[1], self.uncovered)
+            t.cov_rows, t.cov_cols, t.cov_ids = lr, lc, ids
+            t.cov_shape = (t.i_rng[1] - t.i_rng[0] + 1, t.k_rng[1] - t.k_rng[0] + 1)
+        else:
+            op = t.op
+            s = t.pos[0] * self.mbs
+            e = min(s + self.mbs, op.n)
+            ids = op.ids[s:e]
+            flags = self.uncovered[ids]
+            t.cov_ids = ids[flags]
+            t.cov_rows = flags.astype(np.float64)
+
+    # ---------------- tensor-core blocks ----------------
+    def _rows_pass(self, best_possible):
+        tc = self.tc
+        F = self.F
+        cost = self._tc_cost()
+        scale = self._scale()
+        selected = []
+        for b in range(tc.n_blk):
+            counts = tc.block_position_counts(b, self.uncovered)
+            while counts.sum() > 0:
+                L = math.ceil(len(counts) / 16)
+                padc = np.zeros(L * 16, dtype=np.int64)
+                padc[:len(counts)] = counts
+                base = padc.reshape(L, 16).sum(axis=1)
+                mp = int(np.argmax(base))
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    pavg = cost * scale / base[mp] / F
+                if not (pavg < float("inf") and pavg < best_possible):
+                    break
+                target = pavg * (1 + self.max_avg_cost_diff)
+                nz = np.nonzero(counts)[0]
+                neb = int(nz[0]) // 16
+                nwin = max(1, math.ceil((len(counts) - neb * 16) / 16))
+                full = np.zeros(neb * 16 + nwin * 16, dtype=np.int64)
+                full[:len(counts)] = counts
+                nnz_upd = full[neb * 16:].reshape(nwin, 16).sum(axis=1)
+                good = []
+                for i in np.nonzero(cost * scale <= nnz_upd * F * target)[0]:
+                    t = self._tc_tile(b, int(i) + neb)
+                    t.pred_cost = cost * scale
+                    good.append(t)
+                for t in good:
+                    self._finalise(t)
+                for t in good:
+                    self.uncovered[t.cov_ids] = False
+                selected.extend(good)
+                counts = tc.block_position_counts(b, self.uncovered)
+        return selected
+
+    def _search_tc_op(self):
+        tc = self.tc
+        blk, pos = tc.uncovered_entries(self.uncovered)
+        if len(blk) == 0:
+            return None, float("inf")
+        first = tc.first_chunks(blk, pos)
+        if self.single_level:
+            first = first * 0
+        win = pos // 16 - first[blk]
+        span = int(win.max()) + 1
+        code, cnt = np.unique(blk * span + win, return_counts=True)
+        mp = int(np.argmax(cnt))
+        r, c = int(code[mp] // span), int(code[mp] % span)
+        pavg = self._tc_cost() * self._scale() / cnt[mp] / self.F
+        return (r, c + int(first[r])), pavg
+
+    def _local_tc(self, sel, target):
+        tc = self.tc
+        cost = self._tc_cost()
+        scale = self._scale()
+        blk, pos = tc.uncovered_entries(self.uncovered)
+        first = tc.first_chunks(blk, pos)
+        if self.single_level:
+            first = first * 0
+        win = (pos - first[blk] * 16) // 16
+        span = int(win.max()) + 1
+        code, cnt = np.unique(blk * span + win, return_counts=True)
+        ok = cost * scale / cnt / self.F <= target
+        good = []
+        for cd in code[ok]:
+            r, i = int(cd // span), int(cd % span)
+            t = self._tc_tile(r, i + int(first[r]))
+            t.pred_cost = cost * scale
+            good.append(t)
+        return good
+
+    # ---------------- 1D chunks ----------------
+    def _search_1d(self, ops, best_avg):
+        best = None
+        self._avg_cache = {}
+        for op in ops:
+            if op.n == 0:
+                continue
+            rn, cn = op.row_col_nums()
+            costs = self.cost.one_d_costs(rn, cn, self.F, self.mbs)
+            nn = op.chunk_uncovered(self.uncovered)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                avg = costs / nn / self.F
+            self._avg_cache[op.op_id] = (op, avg)
+            mp = int(np.argmin(avg))
+            if avg[mp] < best_avg:
+                best_avg = avg[mp]
+                best = (op, mp, int(nn[mp]) * self.F)
+        if best is None:
+            return None
+        op, mp, nnz_key = best
+        t = self._one_d_tile(op, mp)
+        t.pred_cost = nnz_key * best_avg
+        with np.errstate(divide="ignore", invalid="ignore"):
+            t.pred_avg = t.pred_cost / np.float32(t.nnz_unc)
+        return t
+
+    def _one_d_tile(self, op, p):
+        nn = op.chunk_uncovered(self.uncovered)
+        return _Sel(op=op, kind=ONE_D, ts=(self.mbs,), pos=(int(p),), atomic=False, j_num=self.F,
+                    nnz_unc=self.F * int(nn[p]), best_ts=(self.mbs,), params=dict(ONE_D_PARAMS))
+
+    def _local_1d(self, sel, target):
+        op, avg = self._avg_cache[sel.op.op_id]
+        good = []
+        for p in np.nonzero(avg <= target)[0]:
+            t = self._one_d_tile(op, int(p))
+            t.pred_cost = avg[p] * t.nnz_unc
+            good.append(t)
+        return good
+
+    # ---------------- post-processing ----------------
+    def _post_process(self, selected, level_num):
+        spaces = {}
+        pat = self.pat
+        tiles_1d, tiles_tc = [], []
+        for t in selected:
+            if t.op.op_id not in spaces:
+                sp_ = t.op.space()
+                if t.kind == TC_SDDMM:
+                    inv = t.op.inv
+                    sp_.nnz_id_matrix = sp.csr_matrix(
+                        (np.arange(1, pat.nnz + 1), (inv[pat.row_of], pat.indices)), shape=(pat.M, pat.K))
+                spaces[t.op.op_id] = sp_
+            if t.kind == TC_SDDMM:
+                cov = sp.csr_matrix((np.ones(len(t.cov_ids)), (t.cov_rows, t.cov_cols)), shape=t.cov_shape)
+                tiles_tc.append(Tile(op=spaces[t.op.op_id], tile_sizes=t.ts, tile_pos=t.pos, params=dict(TC_PARAMS),
+                                     best_tile_sizes=t.best_ts, best_params=dict(TC_PARAMS), is_atomic=False,
+                                     tile_i_rng=t.i_rng, tile_k_rng=t.k_rng, covered=cov,
+                                     pred_cost=float(t.pred_cost), nnz_when_selected=int(self.F * len(t.cov_ids)),
+                                     j_num=self.F))
+            else:
+                tiles_1d.append(Tile(op=spaces[t.op.op_id], tile_sizes=t.ts, tile_pos=t.pos,
+                                     params=dict(ONE_D_PARAMS), best_tile_sizes=t.best_ts,
+                                     best_params=dict(ONE_D_PARAMS), is_atomic=False, covered=t.cov_rows,
+                                     pred_cost=float(t.pred_cost), nnz_when_selected=int(self.F * len(t.cov_ids)),
+                                     j_num=self.F))
+        return Plan(op_type="sddmm", shape=(pat.M, pat.K), tiles=tiles_1d + tiles_tc, max_bucket_size=self.mbs,
+                    level_num=level_num, meta={"cost_model": self.cost.name})
+
+
+def plan_sddmm(A, F, cost: CostModel = A100_FP16, **kw) -> Plan:
+    """Select a hybrid tile plan for out = (X @ Y^T) sampled on A's pattern."""
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", RuntimeWarning)
+        return SddmmPlanner(A, F, cost=cost, **kw).search()

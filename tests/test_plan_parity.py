@@ -33,3 +33,19 @@ def test_max_bucket_size_estimate():
     assert estimate_max_bucket_size(14687) == 8
     assert estimate_max_bucket_size(160081) == 32
     assert estimate_max_bucket_size(1_000) == 4
+
+
+@pytest.mark.parametrize("path", golden_files("sddmm"), ids=lambda p: p.split("/")[-1][:-4])
+def test_sddmm_plan_matches_reference(path):
+    from stile_gb300.planner import plan_sddmm
+    meta, arr = S.load_fixture(path)
+    A = S.fixture_matrix(meta, arr)
+    plan = plan_sddmm(A, meta["N"], max_bucket_size=meta["max_bucket_size"])
+    fm, args = emit.emit_sddmm_reference(plan.tiles)
+    assert [f.template for f in fm] == [f["template"] for f in meta["formats"]]
+    assert [len(f.tiles) for f in fm] == [f["n_tiles"] for f in meta["formats"]]
+    for a, r in zip(args, S.fixture_args(meta, arr)):
+        for x, y in zip(a, r):
+            x, y = np.asarray(x), np.asarray(y)
+            assert x.shape == y.shape
+            assert np.array_equal(x.astype(y.dtype), y)
