@@ -1,0 +1,429 @@
+"""Benchmark: hybrid-tile SpMM forward + backward on the graph workload.
+
+Workload (one step): a 169,343 x 169,343 symmetric power-law graph
+(degree exponent 2.0, ~1.17M nonzeros, ~30% of them in planted 16x16 blocks
+of density >= 0.5, values 1/deg), B = 169,343 x 128 fp32:
+    forward   C     = A @ B                (fused hybrid kernel)
+    backward  dvals = <dC[row], B[col]>    (SDDMM over the forward tiles)
+              dB    = A^T @ dC             (transposed plan)
+FLOPs per step = 3 * 2 * nnz * N.  The dense operands are synthetic N(0,1).
+
+Output: one JSON line (metric / value / e2e / roofline / cpu_baseline / ...).
+`--impl reference` times the CPU restatement of the same step on the host
+cores instead (the reference has no runnable GPU path here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SpMM/SDDMM GFLOP/s and %HBM roofline: hybrid-TC vs plain CSR, fwd+bwd, GB300"
+WORKLOAD = "hybrid_graph_169343_nnz1.17M_N128_fwd_bwd"
+N_FEAT = 128
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def make_workload(seed=0):
+    from stile_gb300 import synthetic as syn
+    A = syn.community_graph(n=169_343, target_nnz=1_170_000, exponent=2.0, block_frac=0.30, seed=seed)
+    B = syn.dense_operand(A.shape[1], N_FEAT, seed=1)
+    dC = syn.dense_operand(A.shape[0], N_FEAT, seed=2)
+    return A, B, dC
+
+
+def algorithmic_bytes_spmm(A, N, s_a=4, s_b=4, s_c=4):
+    """Format-independent lower bound on the bytes of one SpMM: row pointers,
+    (index, value) per nonzero, every touched B row once, C written once."""
+    M = A.shape[0]
+    k_touched = int(np.count_nonzero(np.bincount(A.indices, minlength=A.shape[1])))
+    return (M + 1) * 4 + A.nnz * (4 + s_a) + k_touched * N * s_b + M * N * s_c
+
+
+def algorithmic_bytes_sddmm(A, F, s=4):
+    m_t = int(np.count_nonzero(np.diff(A.indptr)))
+    n_t = int(np.count_nonzero(np.bincount(A.indices, minlength=A.shape[1])))
+    return (A.shape[0] + 1) * 4 + A.nnz * 4 + (m_t + n_t) * F * s + A.nnz * s
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch recorded from an ncu capture (profiles/)."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU (oracle) step
+# ---------------------------------------------------------------------------
+def cpu_step_fn(A, AT, B, dC, threads):
+    from oracle import cpu as ocpu
+    rows = np.repeat(np.arange(A.shape[0], dtype=np.int32), np.diff(A.indptr))
+    ip, ix, vv = A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data.astype(np.float32)
+    ipt, ixt, vvt = AT.indptr.astype(np.int32), AT.indices.astype(np.int32), AT.data.astype(np.float32)
+    C = np.empty((A.shape[0], B.shape[1]), np.float32)
+    dB = np.empty((A.shape[1], B.shape[1]), np.float32)
+    dv = np.empty(A.nnz, np.float32)
+    cols = A.indices.astype(np.int32)
+
+    def step():
+        ocpu.csr_spmm(ip, ix, vv, B, threads=threads, out=C)
+        ocpu.sddmm(rows, cols, dC, B, threads=threads, out=dv)
+        ocpu.csr_spmm(ipt, ixt, vvt, dC, threads=threads, out=dB)
+        return C, dv, dB
+    return step
+
+
+def run_cpu_baseline(A, B, dC, flops_per_step, budget_s=12.0):
+    from oracle import cpu as ocpu
+    ocpu.build()
+    AT = A.T.tocsr()
+    AT.sort_indices()
+    threads = os.cpu_count() or 1
+    step = cpu_step_fn(A, AT, B, dC, threads)
+    step()
+    n, t0 = 0, time.perf_counter()
+    while True:
+        step()
+        n += 1
+        if time.perf_counter() - t0 > budget_s or n >= 50:
+            break
+    dt = (time.perf_counter() - t0) / n
+    return {"value": flops_per_step / dt / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+            "sample": f"{n} full fwd+bwd steps (C restatement of CSR SpMM x2 + gather-dot SDDMM, fp32, "
+                      f"pthreads) on the whole workload"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import cpu as ocpu
+    ocpu.build()
+    A, B, dC = make_workload()
+    AT = A.T.tocsr()
+    AT.sort_indices()
+    threads = os.cpu_count() or 1
+    step = cpu_step_fn(A, AT, B, dC, threads)
+    flops = 3 * 2 * A.nnz * N_FEAT
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t0) / args.steps
+    val = flops / dt / 1e9
+    out = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GFLOP/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "nnz": int(A.nnz), "N": N_FEAT},
+           "cpu_baseline": {"value": val, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                            "sample": "the whole fwd+bwd step per iteration (C restatement of the "
+                                      "reference's CPU path: CSR SpMM x2 + gather-dot SDDMM)"},
+           "e2e": {"value": val, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from stile_gb300 import device as D
+    from stile_gb300.api import HybridSpMMFunction, PlanConfig, SpmmOperator
+    from stile_gb300.ops import CsrMatrix, DeviceSddmmPlan, launch_count
+
+    t0 = time.time()
+    A, B_np, dC_np = make_workload()
+    log(f"[bench] workload {A.shape} nnz={A.nnz} ({time.time() - t0:.1f}s)")
+    t0 = time.time()
+    cfg = PlanConfig(tc_mode=D.TC_BF16)
+    op = SpmmOperator(A, N_FEAT, cfg)
+    opT, perm = op.transposed
+    t_plan = time.time() - t0
+    log(f"[bench] plan {op.plan.summary()} levels={op.plan.level_num} ({t_plan:.1f}s)")
+    nnz = A.nnz
+    flops = 3 * 2 * nnz * N_FEAT
+    B = torch.as_tensor(B_np, device=dev)
+    dC = torch.as_tensor(dC_np, device=dev)
+    C = torch.empty((A.shape[0], N_FEAT), device=dev)
+    dB = torch.empty((A.shape[1], N_FEAT), device=dev)
+
+    # plain CSR comparator: CSR-row SpMM for A and A^T, gather-dot SDDMM
+    csrA = CsrMatrix(A)
+    AT = opT.A
+    csrAT = CsrMatrix(AT)
+    ids = np.arange(nnz, dtype=np.int64)
+    plain_dev = D.SddmmDevice(M=A.shape[0], K=A.shape[1], nnz=nnz,
+                              mid_idx=np.repeat(np.arange(A.shape[0]), np.diff(A.indptr)).astype(np.int32),
+                              j_idx=A.indices.astype(np.int32), remap=ids.astype(np.int32), bm=16, bn=16,
+                              blk_i=np.zeros(0, np.int32), blk_j=np.zeros(0, np.int32),
+                              blk_indptr=np.zeros(1, np.int32), blk_dense_pos=np.zeros(0, np.int32),
+                              blk_out=np.zeros(0, np.int32))
+    plain_sddmm = DeviceSddmmPlan(plain_dev)
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def hybrid_step(ev=None):
+        if ev is not None:
+            ev[0].record()
+        op(B, out=C)
+        if ev is not None:
+            ev[1].record()
+        dv = op.dvals(dC, B)
+        opT(dC, out=dB)
+        if ev is not None:
+            ev[2].record()
+        return dv
+
+    def plain_step():
+        csrA.spmm(B, out=C)
+        plain_sddmm.run(dC, B)
+        csrAT.spmm(dC, out=dB)
+
+    # accuracy against the FP64 oracle (outside the timed region)
+    import oracle.semantics as S
+    hybrid_step()
+    torch.cuda.synchronize()
+    dv = op.dvals(dC, B)
+    acc = {"C_rel_fro": S.rel_fro(C.cpu().numpy(), S.spmm_fp64(A, B_np)),
+           "dvals_rel_fro": S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC_np, B_np)),
+           "dB_rel_fro": S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(AT, dC_np))}
+    acc["C_max_abs"] = float(np.abs(C.cpu().numpy() - S.spmm_fp64(A, B_np)).max())
+    log(f"[bench] accuracy {acc}")
+
+    def timed(fn, steps, per_step_events=False):
+        times, fwd = [], []
+        for _ in range(steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            if per_step_events:
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+                s.record()
+                fn(ev)
+                e.record()
+                e.synchronize()
+                times.append(s.elapsed_time(e))
+                fwd.append(ev[0].elapsed_time(ev[1]))
+            else:
+                s.record()
+                fn()
+                e.record()
+                e.synchronize()
+                times.append(s.elapsed_time(e))
+        return times, fwd
+
+    for _ in range(max(args.warmup, 3)):
+        hybrid_step()
+        plain_step()
+    torch.cuda.synchronize()
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = launch_count()
+    wall0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        times, fwd_times = timed(hybrid_step, args.steps, per_step_events=True)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = launch_count() - launches0
+    ms = float(np.sum(times)) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * flops / (ms * 1e-3) / 1e9
+
+    plain_times, _ = timed(plain_step, args.steps)
+    plain_ms = float(np.sum(plain_times)) / args.steps
+    plain_value = flops / (plain_ms * 1e-3) / 1e9
+
+    # roofline of the dominant kernel: the fused forward SpMM
+    fwd_ms = float(np.mean(fwd_times))
+    alg = algorithmic_bytes_spmm(A, N_FEAT)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (fwd_ms * 1e-3) / 1e9
+    traffic = profile_traffic("fused_spmm_hybrid_graph.md")
+    step_bytes = 2 * alg + algorithmic_bytes_sddmm(A, N_FEAT)
+
+    # end to end through the public autograd API with host buffers
+    vals = torch.as_tensor(A.data.astype(np.float32), device=dev)
+    hB = torch.empty((A.shape[1], N_FEAT), dtype=torch.float32, pin_memory=True)
+    hB.copy_(torch.as_tensor(B_np))
+    hdC = torch.empty((A.shape[0], N_FEAT), dtype=torch.float32, pin_memory=True)
+    hdC.copy_(torch.as_tensor(dC_np))
+    hC = torch.empty((A.shape[0], N_FEAT), dtype=torch.float32, pin_memory=True)
+    hdB = torch.empty((A.shape[1], N_FEAT), dtype=torch.float32, pin_memory=True)
+    hdv = torch.empty(nnz, dtype=torch.float32, pin_memory=True)
+
+    def e2e_step():
+        dB_in = hB.to(dev, non_blocking=True).requires_grad_(True)
+        dC_in = hdC.to(dev, non_blocking=True)
+        v = vals.detach().requires_grad_(True)
+        Cc = HybridSpMMFunction.apply(v, dB_in, op)
+        gv, gB = torch.autograd.grad(Cc, [v, dB_in], grad_outputs=dC_in)
+        hC.copy_(Cc.detach(), non_blocking=True)
+        hdv.copy_(gv, non_blocking=True)
+        hdB.copy_(gB, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_times, _ = timed(e2e_step, args.steps)
+    e2e_ms = float(np.sum(e2e_times)) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_val = world * flops / (e2e_ms * 1e-3) / 1e9
+    h2d = hB.numel() * 4 + hdC.numel() * 4
+    d2h = hC.numel() * 4 + hdv.numel() * 4 + hdB.numel() * 4
+
+    cpu = run_cpu_baseline(A, B_np, dC_np, flops) if (rank == 0 and world == 1) else None
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "M": int(A.shape[0]), "K": int(A.shape[1]), "nnz": int(nnz),
+                       "N": N_FEAT, "tc_tiles": "bf16 operands, fp32 accumulate (tcgen05, TMEM)",
+                       "row_tiles": "fp32 (CUDA cores)", "plan": {f"{k[0]}{'/atomic' if k[1] else ''}": v
+                                                                for k, v in op.plan.summary().items()},
+                       "plan_levels": int(op.plan.level_num), "plan_search_s": round(t_plan, 2),
+                       "cost_model": op.plan.meta.get("cost_model"),
+                       "l2": "flushed between steps (256 MiB write, untimed)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e_val, "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+                    "path": "HybridSpMMFunction forward + torch.autograd.grad, pinned host buffers"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "forward SpMM (zero-rows + fused hybrid kernel)",
+                         "algorithmic_bytes_per_launch": int(alg), "ms_per_launch": fwd_ms,
+                         "peak_source": peak_kind},
+            "step_roofline": {"algorithmic_bytes_per_step": int(step_bytes),
+                              "achieved_gbs": step_bytes / (ms * 1e-3) / 1e9,
+                              "frac": step_bytes / (ms * 1e-3) / 1e9 / peak},
+            "csr_baseline": {"value": plain_value, "unit": "GFLOP/s", "ms_per_step": plain_ms,
+                             "speedup_hybrid_over_csr": value / plain_value},
+            "accuracy": acc,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+            "wall_s_timed_region": wall,
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="stile", choices=["stile", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -131,61 +131,65 @@ def build_spmm_device(tiles, A, N=32, tc_mode=TC_BF16, emitted=None):
     formats, args, _ = emitted
 
     # ---------------- tensor-core items ----------------
-    kbeg = [0]
-    flags, out_rows, cols, vals16, nnz_ids = [], [], [], [], []
+    kbeg_parts, flags, out_rows = [np.zeros(1, np.int64)], [], []
+    cols_l, vals_l, live_l, srcr_l = [], [], [], []
     n_ks = 0
     for f, arr in zip(formats, args):
         if f.template != TC:
             continue
         a, i_idx, indptr, indices = arr
         tsz = int(f.tile_sizes[0][1])
-        kw = indices.shape[1]
+        nnzb, _, kw = a.shape
         assert tsz == 16 and kw % 16 == 0, "tensor-core blocks are 16 rows x 16k columns"
+        nsub = kw // 16
         tiles_sorted = sorted(f.tiles, key=lambda t: tuple(t.tile_pos))
         atomic = bool(f.params["real_atomic"])
-        for io in range(len(indptr) - 1):
-            b0, b1 = int(indptr[io]), int(indptr[io + 1])
-            first = tiles_sorted[b0]
-            r0, r1 = first.tile_i_rng
-            n_real = r1 - r0 + 1
-            if i_idx.ndim == 2:
-                rows = i_idx[io].astype(np.int64).copy()
-                src_rows = first.op.i_perm[r0:r1 + 1]
-            else:
-                rows = int(i_idx[io]) * 16 + np.arange(16, dtype=np.int64)
-                src_rows = first.op.i_perm[r0:r1 + 1]
-            rows[n_real:] = -1
-            rows[rows >= M] = -1
-            out_rows.append(rows)
-            flags.append(1 if atomic else 0)
-            for blk in range(b0, b1):
-                live = a[blk] != 0                     # [16, kw]
-                for s in range(kw // 16):
-                    c = indices[blk, s * 16:(s + 1) * 16].astype(np.int64)
-                    lv = live[:, s * 16:(s + 1) * 16].copy()
-                    lv[n_real:, :] = False
-                    rr = np.full(16, -1, dtype=np.int64)
-                    rr[:n_real] = src_rows
-                    R = np.repeat(rr[:, None], 16, axis=1)
-                    Cc = np.repeat(c[None, :], 16, axis=0)
-                    ids, v = vidx.lookup(np.where(lv, R, 0), np.where(lv, Cc, 0))
-                    ids = np.where(lv, ids, -1)
-                    v = np.where(lv, v, 0.0)
-                    if np.any(lv & (ids < 0)):
-                        raise ValueError("plan covers an entry that is not a nonzero of A")
-                    cols.append(c)
-                    vals16.append(v)
-                    nnz_ids.append(ids)
-                    n_ks += 1
-            kbeg.append(n_ks)
+        mb = len(indptr) - 1
+        # rows of every block (from its tile's row range), -1 past the end
+        src = np.full((nnzb, 16), -1, dtype=np.int64)
+        n_real_blk = np.zeros(nnzb, dtype=np.int64)
+        for j, t in enumerate(tiles_sorted):
+            r0, r1 = t.tile_i_rng
+            src[j, :r1 - r0 + 1] = t.op.i_perm[r0:r1 + 1]
+            n_real_blk[j] = r1 - r0 + 1
+        firsts = indptr[:-1].astype(np.int64)
+        if i_idx.ndim == 2:
+            rows = i_idx.astype(np.int64).copy()
+        else:
+            rows = i_idx.astype(np.int64)[:, None] * 16 + np.arange(16, dtype=np.int64)[None, :]
+        rows[np.arange(16)[None, :] >= n_real_blk[firsts][:, None]] = -1
+        rows[rows >= M] = -1
+        out_rows.append(rows)
+        flags.append(np.full(mb, 1 if atomic else 0, dtype=np.int64))
+        steps_per_item = np.diff(indptr).astype(np.int64) * nsub
+        kbeg_parts.append(n_ks + np.cumsum(steps_per_item))
+        n_ks += int(nnzb * nsub)
+        cols_l.append(indices.reshape(nnzb * nsub, 16).astype(np.int64))
+        v = a.reshape(nnzb, 16, nsub, 16).transpose(0, 2, 1, 3).reshape(nnzb * nsub, 16, 16)
+        lv = v != 0
+        lv &= (np.arange(16)[None, :] < np.repeat(n_real_blk, nsub)[:, None])[:, :, None]
+        live_l.append(lv)
+        srcr_l.append(np.repeat(src, nsub, axis=0))
+    kbeg = np.concatenate(kbeg_parts)
     if n_ks:
-        cols = np.stack(cols).astype(np.int32)
-        vals_f = np.stack(vals16).astype(np.float32)           # [n_ks, 16, 16]
-        nnz_ids = np.stack(nnz_ids).reshape(n_ks, 256).astype(np.int32)
+        cols = np.concatenate(cols_l)
+        live = np.concatenate(live_l)
+        srcr = np.concatenate(srcr_l)
+        R = np.broadcast_to(srcr[:, :, None], (n_ks, 16, 16))
+        Cc = np.broadcast_to(cols[:, None, :], (n_ks, 16, 16))
+        ids, v = vidx.lookup(np.where(live, R, 0).reshape(-1), np.where(live, Cc, 0).reshape(-1))
+        ids = ids.reshape(n_ks, 16, 16)
+        v = v.reshape(n_ks, 16, 16)
+        if np.any(live & (ids < 0)):
+            raise ValueError("plan covers an entry that is not a nonzero of A")
+        nnz_ids = np.where(live, ids, -1).reshape(n_ks, 256).astype(np.int32)
+        vals_f = np.where(live, v, 0.0).astype(np.float32)
+        cols = cols.astype(np.int32)
     else:
         cols = np.zeros((0, 16), np.int32)
         vals_f = np.zeros((0, 16, 16), np.float32)
         nnz_ids = np.zeros((0, 256), np.int32)
+    flags = np.concatenate(flags) if flags else np.zeros(0, np.int64)
     if tc_mode == TC_BF16:
         img = operand_image_16bit(_to_bf16_bits(vals_f).reshape(n_ks, 16, 16))
         tc_bytes = 512
@@ -251,7 +255,7 @@ def build_spmm_device(tiles, A, N=32, tc_mode=TC_BF16, emitted=None):
         return np.concatenate(xs).astype(dt) if xs else np.zeros(0, dt)
 
     ell_out = cat(eout, np.int32)
-    tc_rows = np.concatenate(out_rows).astype(np.int32) if out_rows else np.zeros(0, np.int32)
+    tc_rows = np.concatenate(out_rows).reshape(-1).astype(np.int32) if out_rows else np.zeros(0, np.int32)
     tc_flags = np.asarray(flags, dtype=np.int32)
     ell_flags = np.asarray(eflags, dtype=np.int32)
     # owned rows: stored by exactly one non-atomic writer

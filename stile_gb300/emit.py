@@ -167,15 +167,17 @@ def _emit_tc_sddmm(fmt):
     ts_i, ts_k = int(fmt.tile_sizes[0][1]), int(fmt.tile_sizes[2][1])
     op = tiles[0].op
     i_indices = np.asarray([op.i_perm[t.tile_i_rng[0]:t.tile_i_rng[1] + 1] for t in tiles])
-    j_indices = np.asarray([op.k_perm[op.blk_k_vals[int(t.tile_pos[0])]][t.tile_k_rng[0]:t.tile_k_rng[1] + 1]
+    j_indices = np.asarray([op.k_perm[op.blk_k_vals[int(t.tile_pos[0])][t.tile_k_rng[0]:t.tile_k_rng[1] + 1]]
                             for t in tiles])
     cache = {}
     dense_pos, ids, counts = [], [], []
     for t in tiles:
         r = int(t.tile_pos[0])
         if r not in cache:
-            cache[r] = op.nnz_id_matrix[r * ts_i:(r + 1) * ts_i, :][:, op.blk_k_vals[r]].tocsc()
-        csc = cache[r][:, t.tile_k_rng[0]:t.tile_k_rng[1] + 1]
+            cache[r] = op.nnz_id_matrix[r * ts_i:(r + 1) * ts_i, :]
+        # selecting the tile's columns of the block's order is the
+        # reference's "permute every column, then slice the range"
+        csc = cache[r][:, op.blk_k_vals[r][t.tile_k_rng[0]:t.tile_k_rng[1] + 1]].tocsc()
         dense_pos.append(np.repeat(np.arange(csc.shape[1]), csc.getnnz(axis=0)) + csc.indices * ts_k)
         ids.append(csc.data - 1)
         counts.append(csc.nnz)

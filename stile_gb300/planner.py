@@ -244,25 +244,17 @@ class TcOp:
         """Columns at ``positions`` of block b's order (non-empty columns, then
         the remaining columns ascending)."""
         positions = np.asarray(positions, dtype=np.int64)
-        ne = self.nonempty[b]
+        ne = int(self.nonempty[b])
         head = self.kord_cols[self.kstart[b]:self.kstart[b + 1]]
-        out = np.empty(len(positions), dtype=np.int64)
+        out = np.empty(positions.shape, dtype=np.int64)
         m = positions < ne
         out[m] = head[positions[m]]
         if np.any(~m):
-            # j-th column not in head: smallest c with c - #(head <= c) == j
+            # the j-th column absent from the head is j + #{i : hs[i] - i <= j}
             hs = np.sort(head)
+            gaps = hs - np.arange(ne)
             j = positions[~m] - ne
-            # binary search on c
-            lo = np.zeros_like(j)
-            hi = np.full_like(j, self.pat.K - 1)
-            while np.any(lo < hi):
-                mid = (lo + hi) // 2
-                miss = mid + 1 - np.searchsorted(hs, mid, side="right")
-                go = miss <= j
-                lo = np.where(go, mid + 1, lo)
-                hi = np.where(go, hi, mid)
-            out[~m] = lo
+            out[~m] = j + np.searchsorted(gaps, j, side="right")
         return out
 
     def uncovered_entries(self, uncovered):
@@ -309,16 +301,37 @@ class TcOp:
                        blk_k_vals=_LazyKvals(self))
 
 
+class _BlockOrder:
+    """Column order of one block, evaluated only at the requested positions
+    (integer, integer array or slice)."""
+
+    def __init__(self, op: TcOp, b):
+        self.op, self.b = op, int(b)
+
+    def __len__(self):
+        return self.op.pat.K
+
+    def __getitem__(self, idx):
+        if isinstance(idx, slice):
+            idx = np.arange(*idx.indices(len(self)))
+        scalar = np.ndim(idx) == 0
+        out = self.op.kvals(self.b, np.atleast_1d(idx))
+        return out[0] if scalar else out
+
+    def __array__(self, dtype=None, copy=None):
+        return self.op.kvals(self.b, np.arange(len(self)))
+
+
 class _LazyKvals(dict):
-    """``blk_k_vals[b]`` materialised on demand: the full column order of a
-    block (non-empty columns then the empty ones ascending)."""
+    """``blk_k_vals[b]``: the column order of block b (non-empty columns,
+    then the empty ones ascending), evaluated lazily."""
 
     def __init__(self, op: TcOp):
         super().__init__()
         self.op = op
 
     def __missing__(self, b):
-        v = self.op.kvals(int(b), np.arange(self.op.pat.K))
+        v = _BlockOrder(self.op, b)
         self[b] = v
         return v
 
@@ -951,7 +964,7 @@ class SpmmPlanner:
                     level_num=self.level_num, meta={"cost_model": self.cost.name})
 
 
-def plan_spmm(A, N, cost: CostModel = A100_FP16, **kw) -> Plan:
+def search_spmm(A, N, cost: CostModel = A100_FP16, **kw) -> Plan:
     """Select a hybrid tile plan for C = A @ B with B of N columns."""
     with warnings.catch_warnings():
         warnings.simplefilter("ignore", RuntimeWarning)
@@ -1240,8 +1253,12 @@ class SddmmPlanner:
                     level_num=level_num, meta={"cost_model": self.cost.name})
 
 
-def plan_sddmm(A, F, cost: CostModel = A100_FP16, **kw) -> Plan:
+def search_sddmm(A, F, cost: CostModel = A100_FP16, **kw) -> Plan:
     """Select a hybrid tile plan for out = (X @ Y^T) sampled on A's pattern."""
     with warnings.catch_warnings():
         warnings.simplefilter("ignore", RuntimeWarning)
         return SddmmPlanner(A, F, cost=cost, **kw).search()
+
+
+plan_spmm = search_spmm
+plan_sddmm = search_sddmm

@@ -7,7 +7,7 @@ import pytest
 from conftest import golden_files
 import oracle.semantics as S
 from stile_gb300 import emit
-from stile_gb300.planner import plan_spmm
+from stile_gb300.planner import search_spmm as plan_spmm
 
 
 @pytest.mark.parametrize("path", golden_files("spmm"), ids=lambda p: p.split("/")[-1][:-4])
