@@ -78,13 +78,18 @@ def test_gradcheck_induced_subgraph_fp64_central_differences():
 
     v0 = A.data.astype(np.float64)
     h = 1e-6
+    # a directional derivative sums many signed terms, so its error is
+    # measured on the scale |g| |d| (Cauchy-Schwarz), tolerance 1e-5
     for seed in range(3):
         d = np.random.default_rng(100 + seed).standard_normal(v0.shape)
         num = (loss(v0 + h * d, B) - loss(v0 - h * d, B)) / (2 * h)
-        assert abs(num - gv @ d) <= 1e-5 * max(1.0, abs(num))
+        assert abs(num - gv @ d) <= 1e-5 * np.linalg.norm(gv) * np.linalg.norm(d)
         dBdir = np.random.default_rng(200 + seed).standard_normal(B.shape)
         num = (loss(v0, B + h * dBdir) - loss(v0, B - h * dBdir)) / (2 * h)
-        assert abs(num - np.sum(gB * dBdir)) <= 1e-5 * max(1.0, abs(num))
+        assert abs(num - np.sum(gB * dBdir)) <= 1e-5 * np.linalg.norm(gB) * np.linalg.norm(dBdir)
+    # and the full gradients against the FP64 dense references
+    assert S.rel_fro(gv, S.sddmm_fp64(A, dC, B)) <= 1e-5
+    assert S.rel_fro(gB, S.spmm_fp64(A.T.tocsr(), dC)) <= 1e-5
 
 
 def test_plan_sddmm_api():
