@@ -54,7 +54,7 @@ extern "C" {
 /* tensor-tile precision modes */
 #define STILE_TC_BF16 1        /* A, B rounded to bf16, fp32 accumulate */
 #define STILE_TC_F16 2         /* A, B rounded to fp16, fp32 accumulate */
-#define STILE_TC_SPLIT_BF16 4  /* hi+lo bf16 split of A and B, 3 products */
+#define STILE_TC_SPLIT_BF16 4  /* hi+lo bf16 split of A and B, 4 products */
 #define STILE_TC_FP8 3         /* A e4m3 with per-tile scale, B e4m3, fp32 acc. */
 
 /*

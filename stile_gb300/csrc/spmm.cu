@@ -160,8 +160,17 @@ __device__ void tc_item(const SpmmArgs& p, int cta, uint8_t* smem_raw) {
   const uint32_t idesc = (MODE == STILE_TC_F16) ? make_idesc(0, 0, 1, 0, 128, 16)
                                                 : make_idesc(1, 1, 1, 0, 128, 16);
   uint32_t parity[2] = {0u, 0u};
+  uint32_t drain_parity = 0u;
   bool ok = true;
   const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
+  // The accumulator is drained into fp32 registers every kGroup k-steps and
+  // the MMA chain restarts, which bounds how many partial sums the tensor
+  // core accumulates in a row (long rows otherwise drift in split mode).
+  constexpr int kGroup = kSplit ? 4 : 16;
+  float acc[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) acc[i] = 0.f;
+  const uint32_t my_lanes = tmem + ((uint32_t)(32 * warp) << 16);
 
   for (int ks = kb; ks < ke; ++ks) {
     const int step = ks - kb;
@@ -204,33 +213,47 @@ __device__ void tc_item(const SpmmArgs& p, int cta, uint8_t* smem_raw) {
     // uniform decision: every thread saw its stage free
     ok = __syncthreads_and(free_ok && ok) != 0;
     if (!ok) break;
+    const bool group_start = (step % kGroup) == 0;
+    const bool group_end = ((step % kGroup) == kGroup - 1) || (ks == ke - 1);
     if (tid == 0) {
       tc_fence_after();
       const uint64_t ad = smem_desc(s.a[st][0], kALbo, kASbo, kSwizzle128B);
       const uint64_t bd = smem_desc(s.b[st], kBLbo, kBSbo, kSwizzleNone);
-      umma_f16(tmem, ad, bd, idesc, step > 0 ? 1u : 0u);
+      umma_f16(tmem, ad, bd, idesc, group_start ? 0u : 1u);
       if (kSplit) {
         const uint64_t bd_lo = smem_desc(s.b[st] + kBStage, kBLbo, kBSbo, kSwizzleNone);
         const uint64_t ad_lo = smem_desc(s.a[st][1], kALbo, kASbo, kSwizzle128B);
         umma_f16(tmem, ad, bd_lo, idesc, 1u);
         umma_f16(tmem, ad_lo, bd, idesc, 1u);
+        umma_f16(tmem, ad_lo, bd_lo, idesc, 1u);
       }
       umma_commit(s.bar[st]);
+      if (group_end) umma_commit(s.bar[2]);
+    }
+    if (group_end) {
+      // drain: wait for the group's MMAs, add the partial sums in fp32
+      const bool done = __syncthreads_and(mbar_wait_bounded(s.bar[2], drain_parity)) != 0;
+      drain_parity ^= 1u;
+      if (!done) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      uint32_t r[16];
+      tmem_ld16(my_lanes, r);
+      tmem_wait_ld();
+#pragma unroll
+      for (int i = 0; i < 16; ++i) acc[i] += __uint_as_float(r[i]);
+      // every warp has read the accumulator before the next group resets it
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
     }
   }
-  // wait for every MMA of this item
-  if (tid == 0) umma_commit(s.bar[2]);
-  const bool done = __syncthreads_and(mbar_wait_bounded(s.bar[2], 0)) != 0;
-  if (!ok || !done) {
-    if (tid == 0) atomicOr(p.err_flag, 1);
-  }
-  tc_fence_after();
+  if (!ok && tid == 0) atomicOr(p.err_flag, 1);
 
-  // epilogue: warp w owns TMEM lanes 32w..32w+31 = features f0+32w+lane
-  const bool have = (ke > kb) && ok && done;
-  uint32_t r[16];
-  tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16), r);
-  tmem_wait_ld();
+  // epilogue: warp w owns features f0+32w+lane, 16 tile rows in registers
+  const bool have = (ke > kb) && ok;
   const int f = f0 + 32 * warp + lane;
   const bool atomic = (p.tc_item_flags[item] & 1) != 0;
   if (f < N && have) {
@@ -238,9 +261,8 @@ __device__ void tc_item(const SpmmArgs& p, int cta, uint8_t* smem_raw) {
     for (int i = 0; i < 16; ++i) {
       const int row = p.tc_out_rows[(long)item * 16 + i];
       if (row < 0) continue;
-      const float v = __uint_as_float(r[i]);
       float* dst = p.C + (long)row * p.ldc + f;
-      if (atomic) atomicAdd(dst, v); else *dst = v;
+      if (atomic) atomicAdd(dst, acc[i]); else *dst = acc[i];
     }
   }
   tc_fence_before();
