@@ -152,8 +152,9 @@ int stile_sddmm_run(const StileSddmmPlan* plan, const float* X, int64_t ldx,
                     const float* Y, int64_t ldy, float* out, int32_t F,
                     void* stream);
 
-/* Plain CSR-row SpMM (fp32): one warp group per row, vectorised B loads. */
-int stile_csr_spmm_run(int32_t M, const int32_t* indptr, const int32_t* indices,
+/* Plain CSR SpMM (fp32) with nonzero-balanced ranges per warp group,
+ * vectorised B loads; nnz = indptr[M] (passed so no device read is needed). */
+int stile_csr_spmm_run(int32_t M, int64_t nnz, const int32_t* indptr, const int32_t* indices,
                        const float* vals, const float* B, int64_t ldb,
                        float* C, int64_t ldc, int32_t N, void* stream);
 

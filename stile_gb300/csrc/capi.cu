@@ -1,4 +1,5 @@
 // C ABI: plan upload / free, entry points, error reporting.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -126,6 +127,31 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   if (h->n_zero_rows > 0 && (!h->zero_rows || !in_range(h->zero_rows, h->n_zero_rows, 0, h->M)))
     return fail(STILE_E_INVALID, "zero_rows out of range");
 
+  // tensor-core work chunks: items longer than kChunkSteps k-steps are split
+  // into balanced runs that accumulate atomically; the rows of split owned
+  // items join the rows zeroed before the kernels
+  std::vector<int32_t> ck_kbeg{0}, ck_item, ck_flags;
+  std::vector<int32_t> zero(h->zero_rows, h->zero_rows + h->n_zero_rows);
+  for (int i = 0; i < h->tc_n_items; ++i) {
+    const int kb = h->tc_item_kbeg[i], ke = h->tc_item_kbeg[i + 1];
+    const int n = ke - kb;
+    const int nch = n > stile::kChunkSteps ? (n + stile::kChunkSteps - 1) / stile::kChunkSteps : 1;
+    const int per = (n + nch - 1) / nch;
+    const bool split = nch > 1;
+    const int atomic = (h->tc_item_flags[i] & 1) || split ? 1 : 0;
+    for (int c = 0; c < nch; ++c) {
+      ck_kbeg.push_back(std::min(kb + (c + 1) * per, ke));
+      ck_item.push_back(i);
+      ck_flags.push_back(atomic);
+    }
+    if (split && !(h->tc_item_flags[i] & 1))
+      for (int r = 0; r < 16; ++r)
+        if (h->tc_out_rows[(long)i * 16 + r] >= 0) zero.push_back(h->tc_out_rows[(long)i * 16 + r]);
+  }
+  std::sort(zero.begin(), zero.end());
+  zero.erase(std::unique(zero.begin(), zero.end()), zero.end());
+  const long nck = (long)ck_item.size();
+
   Arena ar;
   const long ti = h->tc_n_items, tk = h->tc_n_ksteps;
   const long ei = h->ell_n_items, er = h->ell_n_rows, es = h->ell_n_slots;
@@ -144,7 +170,10 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   size_t i_evals = ar.add(h->ell_vals, es * 4);
   size_t i_ekidx = ar.add(h->ell_kidx, es * 4);
   size_t i_enid = ar.add(h->ell_nnz_id, h->ell_nnz_id ? es * 4 : 0);
-  size_t i_zero = ar.add(h->zero_rows, (size_t)h->n_zero_rows * 4);
+  size_t i_zero = ar.add(zero.data(), zero.size() * 4);
+  size_t i_ckb = ar.add(ck_kbeg.data(), ck_kbeg.size() * 4);
+  size_t i_cki = ar.add(ck_item.data(), (size_t)nck * 4);
+  size_t i_ckf = ar.add(ck_flags.data(), (size_t)nck * 4);
   size_t i_err = ar.add(nullptr, 16);
 
   auto* plan = new StileSpmmPlan();
@@ -198,8 +227,12 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   plan->K = h->K;
   plan->nnz = h->nnz;
   plan->ell_n_slots = h->ell_n_slots;
-  plan->n_zero_rows = h->n_zero_rows;
+  plan->n_zero_rows = (int)zero.size();
   plan->zero_rows = (const int*)P(i_zero);
+  a.tc_n_chunks = h->tc_n_items > 0 ? (int)nck : 0;
+  a.tc_chunk_kbeg = (const int*)P(i_ckb);
+  a.tc_chunk_item = (const int*)P(i_cki);
+  a.tc_chunk_flags = (const int*)P(i_ckf);
   *out = plan;
   return STILE_OK;
 }
@@ -239,10 +272,12 @@ int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float
   a.ldc = ldc;
   a.N = N;
   a.n_fchunks = (N + 127) / 128;
-  a.tc_ctas = a.tc_n_items * a.n_fchunks;
-  e = stile::launch_fused(a, st);
-  if (e != cudaSuccess) return cuda_fail(e, "fused SpMM launch");
-  if (a.tc_ctas + a.ell_n_items) g_launches++;
+  e = stile::launch_tc(a, st);
+  if (e != cudaSuccess) return cuda_fail(e, "tensor-core SpMM launch");
+  if (a.tc_n_chunks) g_launches++;
+  e = stile::launch_ell(a, st);
+  if (e != cudaSuccess) return cuda_fail(e, "ELL SpMM launch");
+  if (a.ell_n_items) g_launches++;
   return STILE_OK;
 }
 
@@ -263,7 +298,7 @@ int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, c
   a.N = N;
   cudaError_t e = stile::launch_dvals(a, dY, lddy, dvals, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
-  if (a.tc_n_ksteps + a.ell_n_items) g_launches++;
+  g_launches += (a.tc_n_ksteps > 0) + (a.ell_n_items > 0);
   return STILE_OK;
 }
 
@@ -291,7 +326,7 @@ int stile_spmm_plan_error_flag(StileSpmmPlan* plan, void* stream, int32_t* flag)
   return STILE_OK;
 }
 
-int stile_csr_spmm_run(int32_t M, const int32_t* indptr, const int32_t* indices, const float* vals,
+int stile_csr_spmm_run(int32_t M, int64_t nnz, const int32_t* indptr, const int32_t* indices, const float* vals,
                        const float* B, int64_t ldb, float* C, int64_t ldc, int32_t N, void* stream) {
   if (M < 0 || N <= 0) return fail(STILE_E_INVALID, "bad shape");
   if (M == 0) return STILE_OK;
@@ -299,7 +334,8 @@ int stile_csr_spmm_run(int32_t M, const int32_t* indptr, const int32_t* indices,
   int rc;
   if ((rc = check_dense(ldb, N, B, "B")) != 0) return rc;
   if ((rc = check_dense(ldc, N, C, "C")) != 0) return rc;
-  cudaError_t e = stile::launch_csr_spmm(M, indptr, indices, vals, B, ldb, C, ldc, N,
+  if (nnz < 0) return fail(STILE_E_INVALID, "negative nnz");
+  cudaError_t e = stile::launch_csr_spmm(M, indptr, indices, vals, B, ldb, C, ldc, N, nnz,
                                          static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "CSR SpMM launch");
   g_launches++;

@@ -2,12 +2,13 @@
 //
 //  * csr_spmm_kernel     plain CSR-row SpMM (the comparator)
 //  * zero_rows_kernel    zeroes output rows that no owned tile stores
-//  * spmm_fused_kernel   one launch for every tile of a plan: the first
-//                        tc_ctas CTAs run dense 16-row block tiles on the
-//                        tensor cores (tcgen05.mma, accumulator in TMEM), the
-//                        rest run ELL row-bucket tiles on CUDA cores.  This is
-//                        the reference's horizontally fused kernel
-//                        (my_fuse_formats.py:2437, blockIdx-range dispatch).
+//  * spmm_tc_kernel      dense 16-row block tiles on the tensor cores
+//                        (tcgen05.mma, accumulator in TMEM), cp.async ring
+//  * spmm_ell_kernel     ELL row-bucket tiles on CUDA cores
+//                        The two launches together are the reference's
+//                        horizontally fused kernel (my_fuse_formats.py:2437):
+//                        the same tiles, split by template into two grids so
+//                        that each gets its own block shape and shared memory.
 //  * spmm_dvals_kernel   value gradient <dY[row], B[col]> for every nonzero,
 //                        walking the same tiles.
 #include "common.cuh"
@@ -16,45 +17,73 @@
 namespace stile {
 
 // ===========================================================================
-// plain CSR-row kernel
+// plain CSR SpMM (the comparator)
 // ===========================================================================
-// LPR lanes per row (each lane owns 4 consecutive features per chunk); a warp
-// handles 32/LPR rows at once.  Column indices / values of a row are loaded
-// cooperatively 32 at a time and broadcast with shuffles.
+// Nonzero-balanced CSR: every LPR-lane group owns kCsrNnz consecutive
+// nonzeros, finds its first row by binary search in indptr and walks the
+// rows it touches (4 B rows in flight per lane).  A row lying wholly inside
+// the range is stored; a row that straddles a range boundary is accumulated
+// with atomics into a row that csr_prezero_kernel zeroed first.
+constexpr int kCsrNnz = 64;
+
+__device__ __forceinline__ int row_of_nnz(const int* __restrict__ indptr, int M, long t) {
+  // largest r with indptr[r] <= t
+  int lo = 0, hi = M;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (indptr[mid] <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void csr_prezero_kernel(int M, const int* __restrict__ indptr, float* __restrict__ C, long ldc,
+                                   int N) {
+  // one thread per row: rows without nonzeros and rows that straddle a
+  // range boundary (accumulated with atomics) start at zero
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= M) return;
+  const long rb = indptr[r], re = indptr[r + 1];
+  const bool empty = rb == re;
+  const bool split = !empty && (rb / kCsrNnz) != ((re - 1) / kCsrNnz);
+  if (!empty && !split) return;
+  float* row = C + (long)r * ldc;
+  for (int f = 0; f < N; f += 4) st_row4(row, f, N, make_float4(0.f, 0.f, 0.f, 0.f));
+}
+
 template <int LPR>
 __global__ void __launch_bounds__(256) csr_spmm_kernel(int M, const int* __restrict__ indptr,
                                                        const int* __restrict__ indices,
                                                        const float* __restrict__ vals,
                                                        const float* __restrict__ B, long ldb,
-                                                       float* __restrict__ C, long ldc, int N) {
-  constexpr int RPW = kWarp / LPR;
+                                                       float* __restrict__ C, long ldc, int N,
+                                                       int n_groups) {
   const int lane = threadIdx.x & 31;
-  const int sub = lane / LPR;
-  const int sl = lane % LPR;
-  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int row = warp_global * RPW + sub;
-  const bool valid = row < M;
-  const int beg = valid ? indptr[row] : 0;
-  const int end = valid ? indptr[row + 1] : 0;
-  const unsigned gmask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
-  for (int fc = 0; fc < N; fc += 4 * LPR) {
-    const int f = fc + 4 * sl;
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int base = beg; base < end; base += LPR) {
-      const int my = base + sl;
-      const int mcol = (my < end) ? indices[my] : 0;
-      const float mval = (my < end) ? vals[my] : 0.f;
-      const int cnt = min(LPR, end - base);
-      int j = 0;
-      for (; j + 4 <= cnt; j += 4) {
-        const int c0 = __shfl_sync(gmask, mcol, sub * LPR + j);
-        const int c1 = __shfl_sync(gmask, mcol, sub * LPR + j + 1);
-        const int c2 = __shfl_sync(gmask, mcol, sub * LPR + j + 2);
-        const int c3 = __shfl_sync(gmask, mcol, sub * LPR + j + 3);
-        const float v0 = __shfl_sync(gmask, mval, sub * LPR + j);
-        const float v1 = __shfl_sync(gmask, mval, sub * LPR + j + 1);
-        const float v2 = __shfl_sync(gmask, mval, sub * LPR + j + 2);
-        const float v3 = __shfl_sync(gmask, mval, sub * LPR + j + 3);
+  const int sub = lane / LPR, sl = lane % LPR;
+  const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
+  if (g >= n_groups) return;
+  const long nnz = indptr[M];
+  const long t0 = (long)g * kCsrNnz;
+  const long t1 = min(t0 + kCsrNnz, nnz);
+  int r = row_of_nnz(indptr, M, t0);
+  long t = t0;
+  while (r < M && t < t1) {
+    const long rb = indptr[r], re = indptr[r + 1];
+    const long a = max(rb, t0), b = min(re, t1);
+    if (a >= b) {  // empty row (already zero)
+      t = re;
+      ++r;
+      continue;
+    }
+    const bool whole = (rb >= t0) && (re <= t1);
+    for (int fc = 0; fc < N; fc += 4 * LPR) {
+      const int f = fc + 4 * sl;
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      long k = a;
+      for (; k + 4 <= b; k += 4) {
+        const int c0 = __ldg(indices + k), c1 = __ldg(indices + k + 1), c2 = __ldg(indices + k + 2),
+                  c3 = __ldg(indices + k + 3);
+        const float v0 = __ldg(vals + k), v1 = __ldg(vals + k + 1), v2 = __ldg(vals + k + 2),
+                    v3 = __ldg(vals + k + 3);
         const float4 b0 = ld_row4(B + (long)c0 * ldb, f, N);
         const float4 b1 = ld_row4(B + (long)c1 * ldb, f, N);
         const float4 b2 = ld_row4(B + (long)c2 * ldb, f, N);
@@ -64,13 +93,11 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int M, const int* __restr
         fma4(acc, v2, b2);
         fma4(acc, v3, b3);
       }
-      for (; j < cnt; ++j) {
-        const int c = __shfl_sync(gmask, mcol, sub * LPR + j);
-        const float v = __shfl_sync(gmask, mval, sub * LPR + j);
-        fma4(acc, v, ld_row4(B + (long)c * ldb, f, N));
-      }
+      for (; k < b; ++k) fma4(acc, __ldg(vals + k), ld_row4(B + (long)__ldg(indices + k) * ldb, f, N));
+      if (whole) st_row4(C + (long)r * ldc, f, N, acc); else red_row4(C + (long)r * ldc, f, N, acc);
     }
-    if (valid) st_row4(C + (long)row * ldc, f, N, acc);
+    t = re;
+    ++r;
   }
 }
 
@@ -88,21 +115,28 @@ __global__ void zero_rows_kernel(const int* __restrict__ rows, int n_rows, float
 }
 
 // ===========================================================================
-// fused hybrid kernel
+// hybrid SpMM: tensor-core kernel + ELL kernel (launched back to back)
 // ===========================================================================
-// Tensor-core item layout in shared memory (per pipeline stage):
-//   A operand: gathered B rows, transposed -> [128 features (M) x 16 k (K)],
-//              MN-major, 128-byte swizzle: two 64-feature atoms (LBO 2048 B),
-//              two 8-row k groups (SBO 1024 B).
-//   B operand: the 16x16 block values (N = 16 tile rows x K = 16), K-major,
-//              no swizzle: core matrices 8 rows x 16 B, LBO 128 B (k
-//              direction), SBO 256 B (row direction); copied verbatim from
-//              the plan (the host writes this image).
-constexpr uint32_t kAStage = 4096;   // bytes of one A image
+// Tensor-core chunks.  A chunk is a run of at most kChunkSteps k-steps of
+// one item (items longer than that are split; the split parts accumulate
+// with atomics into pre-zeroed rows).  Per k-step the CTA gathers the 16
+// referenced B rows (fp32, 128 features) with cp.async into a 4-stage ring
+// together with the step's 16x16 value image, converts its own copies to the
+// bf16 / fp16 A-operand image and one thread issues the tcgen05.mma.
+//
+// Shared-memory operand layouts (checked by the layout probe):
+//   A: [128 features (M) x 16 k (K)], MN-major, 128-byte swizzle: two
+//      64-feature atoms (LBO 2048 B), two 8-row k groups (SBO 1024 B)
+//   B: the 16x16 block values (N = 16 rows x K = 16), K-major, no swizzle:
+//      core matrices 8 rows x 16 B, LBO 128 B (k), SBO 256 B (rows); the
+//      plan stores this image and it is used in place.
+constexpr uint32_t kAStage = 4096;   // bytes of one A image (16-bit)
 constexpr uint32_t kBStage = 512;    // bytes of one B image (16-bit)
 constexpr uint32_t kALbo = 2048, kASbo = 1024;
 constexpr uint32_t kBLbo = 128, kBSbo = 256;
 constexpr int kTcThreads = 128;
+constexpr int kStages = 4;           // cp.async ring depth
+constexpr uint32_t kRawRows = 8192;  // 16 rows x 128 fp32 per stage
 
 __device__ __forceinline__ uint32_t a_img_off(int m, int k) {
   // m: feature (0..127), k: column within the k-step (0..15)
@@ -110,130 +144,135 @@ __device__ __forceinline__ uint32_t a_img_off(int m, int k) {
   return (uint32_t)(atom * kALbo + grp * kASbo + r * 128 + ((chunk ^ r) << 4) + (m & 7) * 2);
 }
 
-struct TcSmem {
-  uint32_t a[2][2];   // [stage][hi/lo] A image addresses
-  uint32_t b[2];      // [stage] B image(s) address
-  uint32_t bar[3];    // stage 0, stage 1, final
-  uint32_t tmem_slot;
+template <bool kSplit>
+struct TcLayout {
+  static constexpr uint32_t kVals = kSplit ? 2 * kBStage : kBStage;
+  static constexpr uint32_t kStage = kRawRows + kVals;
+  static constexpr uint32_t kAImg = kSplit ? 2 * kAStage : kAStage;
+  static constexpr uint32_t kRing = kStages * kStage;                 // multiple of 1024
+  static constexpr uint32_t kBytes = 1024 + kRing + 2 * kAImg + 64;  // + alignment slack
 };
 
 template <int MODE>
-__device__ void tc_item(const SpmmArgs& p, int cta, uint8_t* smem_raw) {
+__global__ void __launch_bounds__(kTcThreads) spmm_tc_kernel(SpmmArgs p) {
   constexpr bool kSplit = (MODE == STILE_TC_SPLIT_BF16);
-  constexpr uint32_t kBBytes = kSplit ? 2 * kBStage : kBStage;
-  const int item = cta / p.n_fchunks;
-  const int f0 = (cta % p.n_fchunks) * 128;
+  using L = TcLayout<kSplit>;
+  extern __shared__ uint8_t smem_raw[];
+  const int chunk = blockIdx.x / p.n_fchunks;
+  const int f0 = (blockIdx.x % p.n_fchunks) * 128;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  // carve shared memory (1024-byte aligned for the 128B swizzle atoms)
-  const uint32_t raw = smem_u32(smem_raw);
-  const uint32_t base = (raw + 1023u) & ~1023u;
-  TcSmem s;
-  uint32_t off = base;
-  for (int st = 0; st < 2; ++st) {
-    s.a[st][0] = off; off += kAStage;
-    s.a[st][1] = off; if (kSplit) off += kAStage;
-  }
-  for (int st = 0; st < 2; ++st) { s.b[st] = off; off += kBBytes; }
-  s.bar[0] = off; s.bar[1] = off + 8; s.bar[2] = off + 16;
-  s.tmem_slot = off + 24;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const uint32_t ring = base;
+  const uint32_t aimg = base + L::kRing;
+  const uint32_t bar = aimg + 2 * L::kAImg;
+  const uint32_t tmem_slot = bar + 8;
 
   if (tid == 0) {
-    mbar_init(s.bar[0], 1);
-    mbar_init(s.bar[1], 1);
-    mbar_init(s.bar[2], 1);
+    mbar_init(bar, 1);
     fence_mbar_init();
   }
   if (warp == 0) {
-    tmem_alloc(s.tmem_slot, 32);
+    tmem_alloc(tmem_slot, 32);
     tmem_relinquish();
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   uint32_t tmem;
-  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(s.tmem_slot) : "memory");
+  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
 
-  const int kb = p.tc_item_kbeg[item];
-  const int ke = p.tc_item_kbeg[item + 1];
+  const int kb = p.tc_chunk_kbeg[chunk];
+  const int n = p.tc_chunk_kbeg[chunk + 1] - kb;
+  const int item = p.tc_chunk_item[chunk];
   const int N = p.N;
+  const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
   const uint32_t idesc = (MODE == STILE_TC_F16) ? make_idesc(0, 0, 1, 0, 128, 16)
                                                 : make_idesc(1, 1, 1, 0, 128, 16);
-  uint32_t parity[2] = {0u, 0u};
-  uint32_t drain_parity = 0u;
-  bool ok = true;
-  const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
-  // The accumulator is drained into fp32 registers every kGroup k-steps and
-  // the MMA chain restarts, which bounds how many partial sums the tensor
-  // core accumulates in a row (long rows otherwise drift in split mode).
+
+  // this thread's 4 copies per stage: rows warp + 4j, features 4*lane..+3
+  auto issue = [&](int ks, int stg) {
+    const uint32_t sb = ring + stg * L::kStage;
+    const int f = f0 + 4 * lane;
+    const uint32_t bytes = (f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int kk = warp + 4 * j;
+      const float* row = p.B + (long)p.tc_cols[(long)ks * 16 + kk] * p.ldb;
+      cp_async16(sb + kk * 512 + lane * 16, bytes ? (const void*)(row + f) : (const void*)row, bytes);
+    }
+    if (tid < (int)(L::kVals / 16))
+      cp_async16(sb + kRawRows + tid * 16, vals + (long)ks * L::kVals + tid * 16, 16u);
+  };
+
+  // k-steps per accumulation chain before the accumulator is drained into
+  // fp32 registers (bounds the tensor core's accumulation chain)
   constexpr int kGroup = kSplit ? 4 : 16;
   float acc[16];
 #pragma unroll
   for (int i = 0; i < 16; ++i) acc[i] = 0.f;
   const uint32_t my_lanes = tmem + ((uint32_t)(32 * warp) << 16);
+  bool ok = true;
 
-  for (int ks = kb; ks < ke; ++ks) {
-    const int step = ks - kb;
-    const int st = step & 1;
-    bool free_ok = true;
-    if (step >= 2) {
-      // the MMA that read this stage two steps ago must be finished
-      free_ok = mbar_wait_bounded(s.bar[st], parity[st]);
-      parity[st] ^= 1u;
-    }
-    if (free_ok) {
-      // gather 16 rows of B (this k-step's columns) for features [f0, f0+128)
-      // warp w handles columns 4w..4w+3, lane l handles features 4l..4l+3
+#pragma unroll 1
+  for (int j = 0; j < kStages - 1; ++j) {
+    if (j < n) issue(kb + j, j);
+    cp_async_commit();
+  }
+#pragma unroll 1
+  for (int step = 0; step < n; ++step) {
+    // the MMA of the previous step has read the stage the next copy overwrites
+    bool w_ok = true;
+    if (step >= 1) w_ok = mbar_wait_bounded(bar, (uint32_t)(step - 1) & 1u);
+    if (w_ok && step + kStages - 1 < n) issue(kb + step + kStages - 1, (step + kStages - 1) % kStages);
+    cp_async_commit();
+    cp_async_wait<kStages - 1>();
+    const uint32_t sb = ring + (step % kStages) * L::kStage;
+    const uint32_t ai = aimg + (step & 1) * L::kAImg;
+    if (w_ok) {
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const int kk = warp * 4 + r;
-        const int col = p.tc_cols[(long)ks * 16 + kk];
-        const int f = f0 + 4 * lane;
-        const float4 v = ld_row4(p.B + (long)col * p.ldb, f, N);
+      for (int j = 0; j < 4; ++j) {
+        const int kk = warp + 4 * j;
+        const uint4 raw = ld_shared_v4(sb + kk * 512 + lane * 16);
+        const float4 v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y),
+                                     __uint_as_float(raw.z), __uint_as_float(raw.w));
         const uint32_t o = a_img_off(4 * lane, kk);
         if (MODE == STILE_TC_F16) {
-          st_shared_v2(s.a[st][0] + o, pack_f16x2(v.x, v.y), pack_f16x2(v.z, v.w));
+          st_shared_v2(ai + o, pack_f16x2(v.x, v.y), pack_f16x2(v.z, v.w));
         } else {
           const uint32_t h0 = pack_bf16x2(v.x, v.y), h1 = pack_bf16x2(v.z, v.w);
-          st_shared_v2(s.a[st][0] + o, h0, h1);
+          st_shared_v2(ai + o, h0, h1);
           if (kSplit) {
             const __nv_bfloat162 b0 = *reinterpret_cast<const __nv_bfloat162*>(&h0);
             const __nv_bfloat162 b1 = *reinterpret_cast<const __nv_bfloat162*>(&h1);
             const float2 r0 = __bfloat1622float2(b0), r1 = __bfloat1622float2(b1);
-            st_shared_v2(s.a[st][1] + o, pack_bf16x2(v.x - r0.x, v.y - r0.y),
+            st_shared_v2(ai + kAStage + o, pack_bf16x2(v.x - r0.x, v.y - r0.y),
                          pack_bf16x2(v.z - r1.x, v.w - r1.y));
           }
         }
       }
-      // block values: verbatim copy of the operand image(s)
-      const uint4* src = reinterpret_cast<const uint4*>(vals + (long)ks * kBBytes);
-      for (int i = tid; i < (int)(kBBytes / 16); i += kTcThreads) st_shared_v4(s.b[st] + 16 * i, src[i]);
     }
     fence_proxy_async_smem();
-    // uniform decision: every thread saw its stage free
-    ok = __syncthreads_and(free_ok && ok) != 0;
+    ok = __syncthreads_and(w_ok && ok) != 0;
     if (!ok) break;
     const bool group_start = (step % kGroup) == 0;
-    const bool group_end = ((step % kGroup) == kGroup - 1) || (ks == ke - 1);
+    const bool group_end = ((step % kGroup) == kGroup - 1) || (step == n - 1);
     if (tid == 0) {
       tc_fence_after();
-      const uint64_t ad = smem_desc(s.a[st][0], kALbo, kASbo, kSwizzle128B);
-      const uint64_t bd = smem_desc(s.b[st], kBLbo, kBSbo, kSwizzleNone);
+      const uint64_t ad = smem_desc(ai, kALbo, kASbo, kSwizzle128B);
+      const uint64_t bd = smem_desc(sb + kRawRows, kBLbo, kBSbo, kSwizzleNone);
       umma_f16(tmem, ad, bd, idesc, group_start ? 0u : 1u);
       if (kSplit) {
-        const uint64_t bd_lo = smem_desc(s.b[st] + kBStage, kBLbo, kBSbo, kSwizzleNone);
-        const uint64_t ad_lo = smem_desc(s.a[st][1], kALbo, kASbo, kSwizzle128B);
+        const uint64_t ad_lo = smem_desc(ai + kAStage, kALbo, kASbo, kSwizzle128B);
+        const uint64_t bd_lo = smem_desc(sb + kRawRows + kBStage, kBLbo, kBSbo, kSwizzleNone);
         umma_f16(tmem, ad, bd_lo, idesc, 1u);
         umma_f16(tmem, ad_lo, bd, idesc, 1u);
         umma_f16(tmem, ad_lo, bd_lo, idesc, 1u);
       }
-      umma_commit(s.bar[st]);
-      if (group_end) umma_commit(s.bar[2]);
+      umma_commit(bar);
     }
     if (group_end) {
-      // drain: wait for the group's MMAs, add the partial sums in fp32
-      const bool done = __syncthreads_and(mbar_wait_bounded(s.bar[2], drain_parity)) != 0;
-      drain_parity ^= 1u;
+      const bool done = __syncthreads_and(mbar_wait_bounded(bar, (uint32_t)step & 1u)) != 0;
       if (!done) {
         ok = false;
         break;
@@ -244,19 +283,18 @@ __device__ void tc_item(const SpmmArgs& p, int cta, uint8_t* smem_raw) {
       tmem_wait_ld();
 #pragma unroll
       for (int i = 0; i < 16; ++i) acc[i] += __uint_as_float(r[i]);
-      // every warp has read the accumulator before the next group resets it
       tc_fence_before();
       __syncthreads();
       tc_fence_after();
     }
   }
+  cp_async_wait<0>();
   if (!ok && tid == 0) atomicOr(p.err_flag, 1);
 
   // epilogue: warp w owns features f0+32w+lane, 16 tile rows in registers
-  const bool have = (ke > kb) && ok;
   const int f = f0 + 32 * warp + lane;
-  const bool atomic = (p.tc_item_flags[item] & 1) != 0;
-  if (f < N && have) {
+  const bool atomic = (p.tc_chunk_flags[chunk] & 1) != 0;
+  if (f < N && n > 0 && ok) {
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
       const int row = p.tc_out_rows[(long)item * 16 + i];
@@ -270,11 +308,17 @@ __device__ void tc_item(const SpmmArgs& p, int cta, uint8_t* smem_raw) {
   if (warp == 0) tmem_dealloc(tmem, 32);
 }
 
-// ELL tile: 4 warps; LPR lanes per row own 4 features each, rows of the tile
-// are distributed round-robin over the 32/LPR row slots of every warp.
+// ELL tiles: one CTA (8 warps) per tile.  An LPR-lane group owns 4 rows at a
+// time (4 x 4 features per lane in flight per slot), so short rows still
+// keep many B-row loads in flight.
+constexpr int kEllThreads = 256;
+constexpr int kEllRows = 4;
+
 template <int LPR>
-__device__ void ell_item(const SpmmArgs& p, int item) {
+__global__ void __launch_bounds__(kEllThreads, 4) spmm_ell_kernel(SpmmArgs p) {
   constexpr int RPW = kWarp / LPR;
+  constexpr int kGroups = (kEllThreads / kWarp) * RPW;
+  const int item = blockIdx.x;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int sub = lane / LPR, sl = lane % LPR;
   const int row0 = p.ell_item_row0[item];
@@ -283,112 +327,166 @@ __device__ void ell_item(const SpmmArgs& p, int item) {
   const long slot0 = p.ell_item_slot0[item];
   const bool atomic = (p.ell_item_flags[item] & 1) != 0;
   const int N = p.N;
-  for (int r = warp * RPW + sub; r < nrows; r += (kTcThreads / kWarp) * RPW) {
-    const int gr = row0 + r;
-    const int orow = p.ell_out_row[gr];
-    if (orow < 0) continue;
-    const int len = p.ell_row_len[gr];
-    const float* vr = p.ell_vals + slot0 + (long)r * K;
-    const int* kr = p.ell_kidx + slot0 + (long)r * K;
-    float* crow = p.C + (long)orow * p.ldc;
+  const int g = warp * RPW + sub;
+  for (int rb = g * kEllRows; rb < nrows; rb += kGroups * kEllRows) {
+    int orow[kEllRows], len[kEllRows];
+    int maxlen = 0;
+#pragma unroll
+    for (int q = 0; q < kEllRows; ++q) {
+      const int r = rb + q;
+      orow[q] = -1;
+      len[q] = 0;
+      if (r < nrows) {
+        orow[q] = p.ell_out_row[row0 + r];
+        len[q] = orow[q] >= 0 ? p.ell_row_len[row0 + r] : 0;
+      }
+      maxlen = max(maxlen, len[q]);
+    }
+    if (maxlen == 0) continue;
     for (int fc = 0; fc < N; fc += 4 * LPR) {
       const int f = fc + 4 * sl;
-      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-      int k = 0;
-      for (; k + 4 <= len; k += 4) {
-        const int c0 = __ldg(kr + k), c1 = __ldg(kr + k + 1), c2 = __ldg(kr + k + 2),
-                  c3 = __ldg(kr + k + 3);
-        const float v0 = __ldg(vr + k), v1 = __ldg(vr + k + 1), v2 = __ldg(vr + k + 2),
-                    v3 = __ldg(vr + k + 3);
-        const float4 b0 = ld_row4(p.B + (long)c0 * p.ldb, f, N);
-        const float4 b1 = ld_row4(p.B + (long)c1 * p.ldb, f, N);
-        const float4 b2 = ld_row4(p.B + (long)c2 * p.ldb, f, N);
-        const float4 b3 = ld_row4(p.B + (long)c3 * p.ldb, f, N);
-        fma4(acc, v0, b0);
-        fma4(acc, v1, b1);
-        fma4(acc, v2, b2);
-        fma4(acc, v3, b3);
+      float4 acc[kEllRows];
+#pragma unroll
+      for (int q = 0; q < kEllRows; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int k = 0; k < maxlen; ++k) {
+        float4 b[kEllRows];
+        float v[kEllRows];
+#pragma unroll
+        for (int q = 0; q < kEllRows; ++q) {
+          v[q] = 0.f;
+          b[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (k < len[q]) {
+            const long s = slot0 + (long)(rb + q) * K + k;
+            v[q] = __ldg(p.ell_vals + s);
+            b[q] = ld_row4(p.B + (long)__ldg(p.ell_kidx + s) * p.ldb, f, N);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < kEllRows; ++q) fma4(acc[q], v[q], b[q]);
       }
-      for (; k < len; ++k) fma4(acc, __ldg(vr + k), ld_row4(p.B + (long)__ldg(kr + k) * p.ldb, f, N));
-      if (atomic) red_row4(crow, f, N, acc); else st_row4(crow, f, N, acc);
+#pragma unroll
+      for (int q = 0; q < kEllRows; ++q) {
+        if (orow[q] < 0) continue;
+        float* crow = p.C + (long)orow[q] * p.ldc;
+        if (atomic) red_row4(crow, f, N, acc[q]); else st_row4(crow, f, N, acc[q]);
+      }
     }
-  }
-}
-
-template <int MODE, int LPR>
-__global__ void __launch_bounds__(kTcThreads) spmm_fused_kernel(SpmmArgs p) {
-  extern __shared__ uint8_t smem_raw[];
-  const int cta = blockIdx.x;
-  if (cta < p.tc_ctas) {
-    tc_item<MODE>(p, cta, smem_raw);
-  } else {
-    ell_item<LPR>(p, cta - p.tc_ctas);
   }
 }
 
 // ===========================================================================
 // value gradient: dvals[t] = <dY[row(t)], B[col(t)]>
 // ===========================================================================
-// One CTA (4 warps) per ELL item or per TC k-step.  An LPR-lane group computes
-// one dot product, reducing over the features with shuffles.
-template <int LPR>
-__device__ __forceinline__ float group_dot(const float* a, const float* b, int N, int sl,
-                                           unsigned gmask) {
-  float s = 0.f;
-  for (int f = 4 * sl; f < N; f += 4 * LPR) s += dot4(ld_row4(a, f, N), ld_row4(b, f, N));
+// Tensor-core k-steps: one CTA stages the step's 16 dY rows and 16 B rows in
+// shared memory, 128 features at a time, and computes only the live entries
+// (at most 2 per thread).  ELL tiles: an LPR-lane group keeps its row of dY
+// in registers and reduces one slot per iteration with shuffles.
+constexpr int kDvChunk = 128;
+constexpr int kDvPad = kDvChunk + 4;
+
+__global__ void __launch_bounds__(128) dvals_tc_kernel(SpmmArgs p, const float* __restrict__ dY, long lddy,
+                                                       float* __restrict__ dvals) {
+  __shared__ __align__(16) float ys[16 * kDvPad];
+  __shared__ __align__(16) float bs[16 * kDvPad];
+  const int ks = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int N = p.N;
+  int lo = 0, hi = p.tc_n_items;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (p.tc_item_kbeg[mid] <= ks) lo = mid; else hi = mid;
+  }
+  const int item = lo;
+  int id[2], e[2];
+  float acc[2] = {0.f, 0.f};
 #pragma unroll
-  for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
-  return s;
+  for (int q = 0; q < 2; ++q) {
+    e[q] = tid + 128 * q;
+    id[q] = p.tc_nnz_id[(long)ks * 256 + e[q]];
+  }
+  if (!__syncthreads_or(id[0] >= 0 || id[1] >= 0)) return;
+  for (int fc = 0; fc < N; fc += kDvChunk) {
+    __syncthreads();
+    for (int i = tid; i < 16 * (kDvChunk / 4); i += 128) {
+      const int r = i / (kDvChunk / 4), c = (i % (kDvChunk / 4)) * 4;
+      const int orow = p.tc_out_rows[(long)item * 16 + r];
+      const int col = p.tc_cols[(long)ks * 16 + r];
+      const float4 vy = orow >= 0 ? ld_row4(dY + (long)orow * lddy, fc + c, N) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 vb = ld_row4(p.B + (long)col * p.ldb, fc + c, N);
+      *reinterpret_cast<float4*>(&ys[r * kDvPad + c]) = vy;
+      *reinterpret_cast<float4*>(&bs[r * kDvPad + c]) = vb;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (id[q] < 0) continue;
+      const float* yr = &ys[(e[q] >> 4) * kDvPad];
+      const float* br = &bs[(e[q] & 15) * kDvPad];
+      float sum = 0.f;
+#pragma unroll 8
+      for (int c = 0; c < kDvChunk; c += 4)
+        sum += dot4(*reinterpret_cast<const float4*>(yr + c), *reinterpret_cast<const float4*>(br + c));
+      acc[q] += sum;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    if (id[q] >= 0) dvals[id[q]] = acc[q];
 }
 
 template <int LPR>
-__global__ void __launch_bounds__(128) spmm_dvals_kernel(SpmmArgs p, const float* __restrict__ dY,
-                                                         long lddy, float* __restrict__ dvals) {
+__global__ void __launch_bounds__(256, 4) dvals_ell_kernel(SpmmArgs p, const float* __restrict__ dY, long lddy,
+                                                           float* __restrict__ dvals) {
   constexpr int RPW = kWarp / LPR;
+  constexpr int kGroups = 8 * RPW;
+  const int item = blockIdx.x;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int sub = lane / LPR, sl = lane % LPR;
   const unsigned gmask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
+  const int row0 = p.ell_item_row0[item];
+  const int nrows = p.ell_item_row0[item + 1] - row0;
+  const int K = p.ell_item_K[item];
+  const long slot0 = p.ell_item_slot0[item];
   const int N = p.N;
-  const int cta = blockIdx.x;
-  const int groups = 4 * RPW;
-  const int g = warp * RPW + sub;
-  if (cta < p.tc_n_ksteps) {
-    // TC k-step: 16 rows x 16 columns, entries with a nonzero id
-    const int ks = cta;
-    // which item owns this k-step: binary search in tc_item_kbeg
-    int lo = 0, hi = p.tc_n_items;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (p.tc_item_kbeg[mid] <= ks) lo = mid; else hi = mid;
-    }
-    const int item = lo;
-    for (int e = g; e < 256; e += groups) {
-      const int id = p.tc_nnz_id[(long)ks * 256 + e];  // uniform within the group
-      if (id < 0) continue;
-      const int n = e >> 4, k = e & 15;
-      const int row = p.tc_out_rows[(long)item * 16 + n];
-      const int col = p.tc_cols[(long)ks * 16 + k];
-      const float d = group_dot<LPR>(dY + (long)row * lddy, p.B + (long)col * p.ldb, N, sl, gmask);
-      if (sl == 0) dvals[id] = d;
-    }
-  } else {
-    const int item = cta - p.tc_n_ksteps;
-    const int row0 = p.ell_item_row0[item];
-    const int nrows = p.ell_item_row0[item + 1] - row0;
-    const int K = p.ell_item_K[item];
-    const long slot0 = p.ell_item_slot0[item];
-    const int total = nrows * K;
-    for (int e = g; e < total; e += groups) {
-      const int r = e / K, k = e - r * K;
-      const int gr = row0 + r;
-      const int orow = p.ell_out_row[gr];
-      if (orow < 0 || k >= p.ell_row_len[gr]) continue;
-      const long s = slot0 + (long)r * K + k;
-      const int id = p.ell_nnz_id[s];
-      if (id < 0) continue;
-      const float d =
-          group_dot<LPR>(dY + (long)orow * lddy, p.B + (long)p.ell_kidx[s] * p.ldb, N, sl, gmask);
-      if (sl == 0) dvals[id] = d;
+  for (int r = warp * RPW + sub; r < nrows; r += kGroups) {
+    const int orow = p.ell_out_row[row0 + r];
+    const int len = orow >= 0 ? p.ell_row_len[row0 + r] : 0;
+    if (len == 0) continue;
+    const float* yrow = dY + (long)orow * lddy;
+    const long s0 = slot0 + (long)r * K;
+    if (N <= 4 * LPR) {
+      const float4 y = ld_row4(yrow, 4 * sl, N);
+      int k = 0;
+      for (; k + 2 <= len; k += 2) {
+        const float4 b0 = ld_row4(p.B + (long)__ldg(p.ell_kidx + s0 + k) * p.ldb, 4 * sl, N);
+        const float4 b1 = ld_row4(p.B + (long)__ldg(p.ell_kidx + s0 + k + 1) * p.ldb, 4 * sl, N);
+        float d0 = dot4(y, b0), d1 = dot4(y, b1);
+#pragma unroll
+        for (int o = LPR / 2; o > 0; o >>= 1) {
+          d0 += __shfl_xor_sync(gmask, d0, o);
+          d1 += __shfl_xor_sync(gmask, d1, o);
+        }
+        if (sl == 0) {
+          dvals[p.ell_nnz_id[s0 + k]] = d0;
+          dvals[p.ell_nnz_id[s0 + k + 1]] = d1;
+        }
+      }
+      if (k < len) {
+        const float4 b0 = ld_row4(p.B + (long)__ldg(p.ell_kidx + s0 + k) * p.ldb, 4 * sl, N);
+        float d0 = dot4(y, b0);
+#pragma unroll
+        for (int o = LPR / 2; o > 0; o >>= 1) d0 += __shfl_xor_sync(gmask, d0, o);
+        if (sl == 0) dvals[p.ell_nnz_id[s0 + k]] = d0;
+      }
+    } else {
+      for (int k = 0; k < len; ++k) {
+        const float* brow = p.B + (long)__ldg(p.ell_kidx + s0 + k) * p.ldb;
+        float d = 0.f;
+        for (int f = 4 * sl; f < N; f += 4 * LPR) d += dot4(ld_row4(yrow, f, N), ld_row4(brow, f, N));
+#pragma unroll
+        for (int o = LPR / 2; o > 0; o >>= 1) d += __shfl_xor_sync(gmask, d, o);
+        if (sl == 0) dvals[p.ell_nnz_id[s0 + k]] = d;
+      }
     }
   }
 }
@@ -460,20 +558,23 @@ static cudaError_t dispatch_lpr(int lpr, Args... args) {
 
 template <int LPR>
 struct CsrLaunch {
-  static cudaError_t run(int M, const int* indptr, const int* indices, const float* vals,
-                         const float* B, long ldb, float* C, long ldc, int N, cudaStream_t st) {
-    constexpr int RPW = kWarp / LPR;
-    const int rows_per_cta = 8 * RPW;
-    const int grid = (M + rows_per_cta - 1) / rows_per_cta;
+  static cudaError_t run(int M, const int* indptr, const int* indices, const float* vals, const float* B,
+                         long ldb, float* C, long ldc, int N, long nnz, cudaStream_t st) {
+    const int n_groups = (int)((nnz + kCsrNnz - 1) / kCsrNnz);
+    csr_prezero_kernel<<<(M + 255) / 256, 256, 0, st>>>(M, indptr, C, ldc, N);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    constexpr int GPB = 256 / LPR;
+    const int grid = (n_groups + GPB - 1) / GPB;
     if (grid == 0) return cudaSuccess;
-    csr_spmm_kernel<LPR><<<grid, 256, 0, st>>>(M, indptr, indices, vals, B, ldb, C, ldc, N);
+    csr_spmm_kernel<LPR><<<grid, 256, 0, st>>>(M, indptr, indices, vals, B, ldb, C, ldc, N, n_groups);
     return cudaGetLastError();
   }
 };
 
 cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const float* vals,
-                            const float* B, long ldb, float* C, long ldc, int N, cudaStream_t st) {
-  return dispatch_lpr<CsrLaunch>(lpr_for(N), M, indptr, indices, vals, B, ldb, C, ldc, N, st);
+                            const float* B, long ldb, float* C, long ldc, int N, long nnz, cudaStream_t st) {
+  return dispatch_lpr<CsrLaunch>(lpr_for(N), M, indptr, indices, vals, B, ldb, C, ldc, N, nnz, st);
 }
 
 cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st) {
@@ -483,53 +584,60 @@ cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, 
   return cudaGetLastError();
 }
 
-size_t fused_smem_bytes(int mode) {
-  const bool split = mode == STILE_TC_SPLIT_BF16;
-  const size_t a = 2 * (split ? 2 : 1) * kAStage;
-  const size_t b = 2 * (split ? 2 : 1) * kBStage;
-  return 1024 + a + b + 64;
+size_t tc_smem_bytes(int mode) {
+  return mode == STILE_TC_SPLIT_BF16 ? TcLayout<true>::kBytes : TcLayout<false>::kBytes;
 }
 
-template <int MODE, int LPR>
-static cudaError_t launch_fused_t(const SpmmArgs& p, cudaStream_t st) {
-  const size_t smem = fused_smem_bytes(MODE);
-  auto k = spmm_fused_kernel<MODE, LPR>;
+template <int MODE>
+static cudaError_t launch_tc_t(const SpmmArgs& p, cudaStream_t st) {
+  const size_t smem = tc_smem_bytes(MODE);
+  auto k = spmm_tc_kernel<MODE>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const int grid = p.tc_ctas + p.ell_n_items;
+  const int grid = p.tc_n_chunks * p.n_fchunks;
   if (grid == 0) return cudaSuccess;
   k<<<grid, kTcThreads, smem, st>>>(p);
   return cudaGetLastError();
 }
 
-template <int LPR>
-struct FusedLaunch {
-  static cudaError_t run(int mode, const SpmmArgs& p, cudaStream_t st) {
-    switch (mode) {
-      case STILE_TC_F16: return launch_fused_t<STILE_TC_F16, LPR>(p, st);
-      case STILE_TC_SPLIT_BF16: return launch_fused_t<STILE_TC_SPLIT_BF16, LPR>(p, st);
-      default: return launch_fused_t<STILE_TC_BF16, LPR>(p, st);
-    }
+cudaError_t launch_tc(const SpmmArgs& p, cudaStream_t st) {
+  switch (p.tc_mode) {
+    case STILE_TC_F16: return launch_tc_t<STILE_TC_F16>(p, st);
+    case STILE_TC_SPLIT_BF16: return launch_tc_t<STILE_TC_SPLIT_BF16>(p, st);
+    default: return launch_tc_t<STILE_TC_BF16>(p, st);
   }
-};
-
-cudaError_t launch_fused(const SpmmArgs& p, cudaStream_t st) {
-  return dispatch_lpr<FusedLaunch>(lpr_for(p.N), p.tc_mode, p, st);
 }
 
 template <int LPR>
-struct DvalsLaunch {
-  static cudaError_t run(const SpmmArgs& p, const float* dY, long lddy, float* dvals,
-                         cudaStream_t st) {
-    const int grid = p.tc_n_ksteps + p.ell_n_items;
-    if (grid == 0) return cudaSuccess;
-    spmm_dvals_kernel<LPR><<<grid, 128, 0, st>>>(p, dY, lddy, dvals);
+struct EllLaunch {
+  static cudaError_t run(const SpmmArgs& p, cudaStream_t st) {
+    if (p.ell_n_items == 0) return cudaSuccess;
+    spmm_ell_kernel<LPR><<<p.ell_n_items, kEllThreads, 0, st>>>(p);
     return cudaGetLastError();
   }
 };
 
-cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals,
-                         cudaStream_t st) {
+cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st) {
+  return dispatch_lpr<EllLaunch>(lpr_for(p.N), p, st);
+}
+
+template <int LPR>
+struct DvalsLaunch {
+  static cudaError_t run(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {
+    if (p.tc_n_ksteps > 0) {
+      dvals_tc_kernel<<<p.tc_n_ksteps, 128, 0, st>>>(p, dY, lddy, dvals);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    if (p.ell_n_items > 0) {
+      dvals_ell_kernel<LPR><<<p.ell_n_items, 256, 0, st>>>(p, dY, lddy, dvals);
+      return cudaGetLastError();
+    }
+    return cudaSuccess;
+  }
+};
+
+cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {
   return dispatch_lpr<DvalsLaunch>(lpr_for(p.N), p, dY, lddy, dvals, st);
 }
 

@@ -16,8 +16,12 @@ struct SpmmArgs {
   long ldc;
   int N;
   int n_fchunks;  // ceil(N / 128): tensor-core feature chunks
-  int tc_ctas;    // tc_n_items * n_fchunks
   int tc_mode;
+  // tensor-core work chunks (items split into runs of <= kChunkSteps k-steps)
+  int tc_n_chunks;
+  const int* tc_chunk_kbeg;   // [tc_n_chunks + 1]
+  const int* tc_chunk_item;   // [tc_n_chunks]
+  const int* tc_chunk_flags;  // [tc_n_chunks] bit0: atomic
   // tensor-core items
   int tc_n_items, tc_n_ksteps;
   const int* tc_item_kbeg;
@@ -43,12 +47,14 @@ struct SpmmArgs {
 };
 
 cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const float* vals,
-                            const float* B, long ldb, float* C, long ldc, int N, cudaStream_t st);
+                            const float* B, long ldb, float* C, long ldc, int N, long nnz, cudaStream_t st);
 cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st);
-cudaError_t launch_fused(const SpmmArgs& p, cudaStream_t st);
+cudaError_t launch_tc(const SpmmArgs& p, cudaStream_t st);
+cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st);
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals,
                          cudaStream_t st);
-size_t fused_smem_bytes(int mode);
+size_t tc_smem_bytes(int mode);
+constexpr int kChunkSteps = 32;
 cudaError_t launch_repack(const SpmmArgs& p, const float* vals, long n_ell_slots, cudaStream_t st);
 
 struct SddmmArgs {

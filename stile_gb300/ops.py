@@ -206,7 +206,7 @@ class CsrMatrix:
             out, ldc = new_output(self.shape[0], N, B.device)
         else:
             ldc = out.stride(0)
-        _lib.check(self.lib.stile_csr_spmm_run(self.shape[0], self.indptr.data_ptr(), self.indices.data_ptr(),
+        _lib.check(self.lib.stile_csr_spmm_run(self.shape[0], self.nnz, self.indptr.data_ptr(), self.indices.data_ptr(),
                                                self.vals.data_ptr(), B.data_ptr(), ldb, out.data_ptr(), ldc,
                                                N, _stream()), "stile_csr_spmm_run")
         return out

@@ -42,4 +42,4 @@ def test_invalid_arguments_are_reported_not_aborted():
     assert rc == -1
     assert "negative" in _lib.last_error()
     assert lib.stile_spmm_run(None, None, 0, None, 0, 4, None) == -1
-    assert lib.stile_csr_spmm_run(-1, None, None, None, None, 4, None, 4, 4, None) == -1
+    assert lib.stile_csr_spmm_run(-1, 0, None, None, None, None, 4, None, 4, 4, None) == -1
