@@ -81,8 +81,40 @@ def profile_traffic(name):
     return None
 
 
+class _Nvml:
+    """Minimal NVML through ctypes (SM clock, max SM clock, throttle reasons)."""
+
+    HW_SLOWDOWN, SW_THERMAL, HW_THERMAL, SW_POWER_CAP = 0x8, 0x20, 0x40, 0x4
+
+    def __init__(self, index):
+        import ctypes
+        self.ct = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.h)) != 0:
+            raise RuntimeError("nvml handle")
+
+    def sm_clock(self):
+        v = self.ct.c_uint()
+        self.lib.nvmlDeviceGetClockInfo(self.h, 1, self.ct.byref(v))
+        return int(v.value)
+
+    def max_sm_clock(self):
+        v = self.ct.c_uint()
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, self.ct.byref(v))
+        return int(v.value)
+
+    def reasons(self):
+        v = self.ct.c_ulonglong()
+        self.lib.nvmlDeviceGetCurrentClocksEventReasons(self.h, self.ct.byref(v))
+        return int(v.value)
+
+
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """Samples the SM clock and clock-event reasons during the timed region:
+    NVML at ~1 kHz (read-only queries), nvidia-smi as the fallback."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -92,23 +124,45 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.lines = []
+        self.samples = []
+        self.reason_bits = 0
+        self.nvml = None
+        self.max_mhz = None
+        self._stop = threading.Event()
 
     def __enter__(self):
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.nvml = _Nvml(self.gpu)
+            self.max_mhz = self.nvml.max_sm_clock()
+            self.thread = threading.Thread(target=self._poll, daemon=True)
             self.thread.start()
         except Exception:
-            self.proc = None
+            self.nvml = None
+            try:
+                self.proc = subprocess.Popen(
+                    ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                     "--format=csv,noheader,nounits", "-lms", "200"],
+                    stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                self.thread = threading.Thread(target=self._read, daemon=True)
+                self.thread.start()
+            except Exception:
+                self.proc = None
         return self
+
+    def _poll(self):
+        while not self._stop.is_set():
+            self.samples.append(self.nvml.sm_clock())
+            self.reason_bits |= self.nvml.reasons()
+            time.sleep(0.001)
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        self._stop.set()
+        if self.nvml is not None:
+            self.thread.join(timeout=2)
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -117,6 +171,14 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None and self.samples:
+            names = []
+            for bit, nm in ((_Nvml.HW_SLOWDOWN, "hw_slowdown"), (_Nvml.HW_THERMAL, "hw_thermal_slowdown"),
+                            (_Nvml.SW_THERMAL, "sw_thermal_slowdown"), (_Nvml.SW_POWER_CAP, "sw_power_cap")):
+                if self.reason_bits & bit:
+                    names.append(nm)
+            return {"sm_mhz": float(np.median(self.samples)), "sm_max_mhz": float(self.max_mhz),
+                    "reasons": names, "samples": len(self.samples), "source": "nvml"}
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
@@ -133,7 +195,8 @@ class ClockSampler:
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+                "source": "nvidia-smi"}
 
 
 # ---------------------------------------------------------------------------
