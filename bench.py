@@ -95,6 +95,10 @@ class _Nvml:
         self.h = ctypes.c_void_p()
         if self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.h)) != 0:
             raise RuntimeError("nvml handle")
+        self._reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(self.lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        self.sm_clock()
+        self.reasons()
 
     def sm_clock(self):
         v = self.ct.c_uint()
@@ -108,7 +112,7 @@ class _Nvml:
 
     def reasons(self):
         v = self.ct.c_ulonglong()
-        self.lib.nvmlDeviceGetCurrentClocksEventReasons(self.h, self.ct.byref(v))
+        self._reasons_fn(self.h, self.ct.byref(v))
         return int(v.value)
 
 
