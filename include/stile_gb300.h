@@ -56,6 +56,8 @@ extern "C" {
 #define STILE_TC_F16 2         /* A, B rounded to fp16, fp32 accumulate */
 #define STILE_TC_SPLIT_BF16 4  /* hi+lo bf16 split of A and B, 4 products */
 #define STILE_TC_FP8 3         /* A e4m3 with per-tile scale, B e4m3, fp32 acc. */
+#define STILE_TC_TF32 5        /* A, B read as tf32 (fp32 storage), fp32 acc.; no
+                                  conversion pass: gathered B rows feed the MMA */
 
 /*
  * SpMM plan, device-ready host arrays (built by the emitter).
@@ -66,7 +68,9 @@ extern "C" {
  * image of one tcgen05.mma B operand (K-major, no swizzle):
  *   element (row n, col k) at byte (n/8)*256 + (k/8)*128 + (n%8)*16 + (k%8)*2
  * for 16-bit modes (bf16 / fp16); STILE_TC_SPLIT_BF16 stores the hi image
- * followed by the lo image (1024 B per k-step).
+ * followed by the lo image (1024 B per k-step); STILE_TC_TF32 stores fp32
+ * values (1024 B per k-step) at 4-byte index
+ *   (k/8)*128 + (n/8)*64 + ((k%8)/4)*32 + (n%8)*4 + k%4.
  *
  * ELL items: one per row-bucket tile; rows [ell_item_row0[i],
  * ell_item_row0[i+1]), every row with ell_item_K[i] slots starting at
@@ -85,7 +89,7 @@ typedef struct StileSpmmPlanHost {
   const int32_t* tc_out_rows;    /* [tc_n_items * 16] */
   const int32_t* tc_cols;        /* [tc_n_ksteps * 16] */
   const void* tc_vals;           /* [tc_n_ksteps * tc_kstep_bytes] */
-  int32_t tc_kstep_bytes;        /* 512 (bf16/fp16), 1024 (split), 256 (fp8) */
+  int32_t tc_kstep_bytes;        /* 512 (bf16/fp16), 1024 (split, tf32) */
   const float* tc_scales;        /* [tc_n_ksteps] fp8 per-tile scale, else NULL */
   const int32_t* tc_nnz_id;      /* [tc_n_ksteps * 256] row-major (n,k); -1: empty */
   int32_t ell_n_items, ell_n_rows, ell_n_slots;
@@ -168,14 +172,14 @@ int stile_spmm_plan_set_values(StileSpmmPlan* plan, const float* vals, void* str
 int stile_spmm_plan_error_flag(StileSpmmPlan* plan, void* stream, int32_t* flag);
 
 /* Tensor-core layout self-check (no counterpart in the reference): runs one
- * tcgen05.mma (M=128, N=16, K=16, kind::f16, fp32 accumulate) on two 8 KB
- * shared-memory images copied verbatim from a_img / b_img, with descriptor
- * fields desc6 = {a_lbo, a_sbo, a_layout, b_lbo, b_sbo, b_layout} (bytes,
- * multiples of 16, <= 2048) and instruction descriptor idesc; writes the
- * 128x16 fp32 accumulator row-major to out.  *err is set if the MMA did not
- * complete within the bounded wait. */
+ * tcgen05.mma (M=128, N=16; kind = 0: kind::f16, K=16; kind = 1:
+ * kind::tf32, K=8; fp32 accumulate) on two 8 KB shared-memory images copied
+ * verbatim from a_img / b_img, with descriptor fields desc6 = {a_lbo, a_sbo,
+ * a_layout, b_lbo, b_sbo, b_layout} (bytes, multiples of 16, <= 2048) and
+ * instruction descriptor idesc; writes the 128x16 fp32 accumulator row-major
+ * to out.  *err is set if the MMA did not complete within the bounded wait. */
 int stile_debug_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
-                           uint32_t idesc, float* out, int32_t* err, void* stream);
+                           uint32_t idesc, int32_t kind, float* out, int32_t* err, void* stream);
 
 /* Copy the last error message of the calling thread into buf. */
 int stile_last_error(char* buf, size_t n);

@@ -120,7 +120,7 @@ EXPORTS = {
     "stile_spmm_plan_set_values": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "stile_spmm_plan_error_flag": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, c_i32p]),
     "stile_debug_umma_probe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
-                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+                                              ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "stile_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "stile_launch_count": (ctypes.c_int64, []),
 }

@@ -82,9 +82,9 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
     return fail(STILE_E_INVALID, "negative count");
   const int mode = h->tc_mode;
   if (h->tc_n_items > 0) {
-    if (mode != STILE_TC_BF16 && mode != STILE_TC_F16 && mode != STILE_TC_SPLIT_BF16)
+    if (mode != STILE_TC_BF16 && mode != STILE_TC_F16 && mode != STILE_TC_SPLIT_BF16 && mode != STILE_TC_TF32)
       return fail(STILE_E_UNSUPPORTED, "tensor-tile mode not supported by this build");
-    const int want = (mode == STILE_TC_SPLIT_BF16) ? 1024 : 512;
+    const int want = (mode == STILE_TC_SPLIT_BF16 || mode == STILE_TC_TF32) ? 1024 : 512;
     if (h->tc_kstep_bytes != want) return fail(STILE_E_INVALID, "tc_kstep_bytes does not match mode");
     if (!h->tc_item_kbeg || !h->tc_item_flags || !h->tc_out_rows || !h->tc_cols || !h->tc_vals)
       return fail(STILE_E_INVALID, "missing tensor-tile array");
@@ -446,7 +446,7 @@ int stile_sddmm_run(const StileSddmmPlan* plan, const float* X, int64_t ldx, con
 }
 
 int stile_debug_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
-                           uint32_t idesc, float* out, int32_t* err, void* stream) {
+                           uint32_t idesc, int32_t kind, float* out, int32_t* err, void* stream) {
   if (!a_img || !b_img || !desc6 || !out || !err) return fail(STILE_E_INVALID, "null argument");
   // every address the descriptors can form must stay inside the 8 KB images:
   // at most 16 core-matrix groups along either direction
@@ -456,7 +456,8 @@ int stile_debug_umma_probe(const void* a_img, const void* b_img, const uint32_t*
       return fail(STILE_E_INVALID, "probe strides must be multiples of 16 and <= 2048");
     if (lay != 0 && lay != 2 && lay != 4 && lay != 6) return fail(STILE_E_INVALID, "bad layout type");
   }
-  cudaError_t e = stile::launch_umma_probe(a_img, b_img, desc6, idesc, out, err,
+  if (kind != 0 && kind != 1) return fail(STILE_E_INVALID, "kind must be 0 (f16) or 1 (tf32)");
+  cudaError_t e = stile::launch_umma_probe(a_img, b_img, desc6, idesc, (uint32_t)kind, out, err,
                                            static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "probe launch");
   g_launches++;

@@ -1,6 +1,7 @@
 // Layout self-check for the tensor-core path: one CTA copies two operand
-// images verbatim into shared memory, issues one tcgen05.mma (M=128, N=16,
-// K=16, kind::f16, fp32 accumulate) with caller-chosen descriptor fields and
+// images verbatim into shared memory, issues one tcgen05.mma (M=128, N=16;
+// kind::f16 with K=16 or kind::tf32 with K=8; fp32 accumulate) with
+// caller-chosen descriptor fields and
 // writes the 128x16 accumulator to global memory.  Every descriptor the
 // caller can pass stays inside the CTA's shared memory: each operand gets a
 // 32 KB zero-filled region, the image occupies its first 8 KB, and the host
@@ -20,8 +21,8 @@ __global__ void __launch_bounds__(128) umma_probe_kernel(const uint4* __restrict
                                                          uint32_t a_lbo, uint32_t a_sbo,
                                                          uint32_t a_layout, uint32_t b_lbo,
                                                          uint32_t b_sbo, uint32_t b_layout,
-                                                         uint32_t idesc, float* __restrict__ out,
-                                                         int* __restrict__ err) {
+                                                         uint32_t idesc, uint32_t kind,
+                                                         float* __restrict__ out, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   const uint32_t sa = base, sb = base + kProbeRegion;
@@ -48,8 +49,8 @@ __global__ void __launch_bounds__(128) umma_probe_kernel(const uint4* __restrict
   uint32_t tmem;
   asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(slot) : "memory");
   if (tid == 0) {
-    umma_f16(tmem, smem_desc(sa, a_lbo, a_sbo, a_layout), smem_desc(sb, b_lbo, b_sbo, b_layout), idesc,
-             0u);
+    const uint64_t ad = smem_desc(sa, a_lbo, a_sbo, a_layout), bd = smem_desc(sb, b_lbo, b_sbo, b_layout);
+    if (kind == 1) umma_tf32(tmem, ad, bd, idesc, 0u); else umma_f16(tmem, ad, bd, idesc, 0u);
     umma_commit(bar);
   }
   const bool done = __syncthreads_and(mbar_wait_bounded(bar, 0)) != 0;
@@ -67,14 +68,14 @@ __global__ void __launch_bounds__(128) umma_probe_kernel(const uint4* __restrict
 }
 
 cudaError_t launch_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
-                              uint32_t idesc, float* out, int* err, cudaStream_t st) {
+                              uint32_t idesc, uint32_t kind, float* out, int* err, cudaStream_t st) {
   const size_t smem = 1024 + 2 * kProbeRegion + 64;
   cudaError_t e = cudaFuncSetAttribute(umma_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
   umma_probe_kernel<<<1, 128, smem, st>>>(static_cast<const uint4*>(a_img),
                                           static_cast<const uint4*>(b_img), desc6[0], desc6[1], desc6[2],
-                                          desc6[3], desc6[4], desc6[5], idesc, out, err);
+                                          desc6[3], desc6[4], desc6[5], idesc, kind, out, err);
   return cudaGetLastError();
 }
 

@@ -308,6 +308,140 @@ __global__ void __launch_bounds__(kTcThreads) spmm_tc_kernel(SpmmArgs p) {
   if (warp == 0) tmem_dealloc(tmem, 32);
 }
 
+// tf32 tensor-core kernel (B in fp32).  No conversion pass: each gathered B
+// row is copied by cp.async straight into the A operand of kind::tf32
+// (features = M = 128, MN-major, 128-byte swizzle, 32-feature atoms,
+// LBO 1024 B; the two 8-row k groups of a k-step are 4096 B apart and feed
+// one MMA each).  The block values sit in the plan as the fp32 B-operand
+// image (K-major, no swizzle, LBO 128 B, SBO 256 B; k halves 512 B apart).
+// Warps 0-3 produce (4 x 16 B copies per thread per k-step, completion
+// signalled on a full barrier by cp.async.mbarrier.arrive) and run the
+// epilogue; warp 4 waits on the full barrier, issues the two MMAs and
+// commits to the stage's empty barrier.
+constexpr int kTfStages = 4;
+constexpr uint32_t kTfA = 8192;                 // 16 k x 128 features x 4 B
+constexpr uint32_t kTfB = 1024;                 // 16 rows x 16 k x 4 B
+constexpr uint32_t kTfStage = kTfA + kTfB;      // 9216 = 9 x 1024
+constexpr uint32_t kTfBytes = 1024 + kTfStages * kTfStage + 128;
+constexpr int kTfThreads = 160;
+
+__global__ void __launch_bounds__(kTfThreads) spmm_tc_tf32_kernel(SpmmArgs p) {
+  extern __shared__ uint8_t smem_raw[];
+  const int chunk = blockIdx.x / p.n_fchunks;
+  const int f0 = (blockIdx.x % p.n_fchunks) * 128;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const uint32_t bars = base + kTfStages * kTfStage;  // full[S], empty[S], done
+  const uint32_t tmem_slot = bars + 8 * (2 * kTfStages + 1);
+  auto full = [&](int s) { return bars + 8 * s; };
+  auto empty = [&](int s) { return bars + 8 * (kTfStages + s); };
+  const uint32_t done = bars + 8 * (2 * kTfStages);
+
+  if (tid == 0) {
+    for (int s = 0; s < kTfStages; ++s) {
+      mbar_init(full(s), 128);
+      mbar_init(empty(s), 1);
+    }
+    mbar_init(done, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(tmem_slot, 32);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  uint32_t tmem;
+  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
+
+  const int kb = p.tc_chunk_kbeg[chunk];
+  const int n = p.tc_chunk_kbeg[chunk + 1] - kb;
+  const int item = p.tc_chunk_item[chunk];
+  const int N = p.N;
+  bool ok = true;
+
+  if (warp < 4) {
+    // ---------------- producers ----------------
+    const int f = f0 + 4 * lane;
+    const uint32_t bytes = (f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u);
+    const int atom = lane >> 3, cic = lane & 7;
+    const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
+#pragma unroll 1
+    for (int step = 0; step < n; ++step) {
+      const int s = step % kTfStages;
+      if (step >= kTfStages) {
+        if (!mbar_wait_bounded(empty(s), (uint32_t)((step / kTfStages) - 1) & 1u)) {
+          ok = false;
+          break;
+        }
+      }
+      const uint32_t sa = base + s * kTfStage;
+      const long ks = kb + step;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int kk = warp + 4 * j;
+        const int g = kk >> 3, r = kk & 7;
+        const float* row = p.B + (long)p.tc_cols[ks * 16 + kk] * p.ldb;
+        const uint32_t dst = sa + g * 4096 + atom * 1024 + r * 128 + ((cic ^ r) << 4);
+        cp_async16(dst, bytes ? (const void*)(row + f) : (const void*)row, bytes);
+      }
+      if (tid < 64) cp_async16(sa + kTfA + tid * 16, vals + ks * kTfB + tid * 16, 16u);
+      cp_async_mbar_arrive_noinc(full(s));
+    }
+  } else if (lane == 0) {
+    // ---------------- MMA issuer ----------------
+    const uint32_t idesc = make_idesc(2, 2, 1, 0, 128, 16);
+#pragma unroll 1
+    for (int step = 0; step < n; ++step) {
+      const int s = step % kTfStages;
+      if (!mbar_wait_bounded(full(s), (uint32_t)(step / kTfStages) & 1u)) {
+        ok = false;
+        break;
+      }
+      fence_proxy_async_smem();
+      tc_fence_after();
+      const uint32_t sa = base + s * kTfStage;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const uint64_t ad = smem_desc(sa + h * 4096, 1024, 4096, kSwizzle128B);
+        const uint64_t bd = smem_desc(sa + kTfA + h * 512, 128, 256, kSwizzleNone);
+        umma_tf32(tmem, ad, bd, idesc, (step > 0 || h > 0) ? 1u : 0u);
+      }
+      umma_commit(empty(s));
+    }
+    umma_commit(done);
+  }
+  cp_async_wait<0>();
+
+  // ---------------- epilogue (warps 0-3) ----------------
+  if (warp < 4) {
+    const bool fin = mbar_wait_bounded(done, 0u);
+    tc_fence_after();
+    uint32_t r[16];
+    tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16), r);
+    tmem_wait_ld();
+    const int f = f0 + 32 * warp + lane;
+    const bool atomic = (p.tc_chunk_flags[chunk] & 1) != 0;
+    if (fin && ok && n > 0 && f < N) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int row = p.tc_out_rows[(long)item * 16 + i];
+        if (row < 0) continue;
+        float* dst = p.C + (long)row * p.ldc + f;
+        const float v = __uint_as_float(r[i]);
+        if (atomic) atomicAdd(dst, v); else *dst = v;
+      }
+    }
+    if (!fin || !ok) atomicOr(p.err_flag, 1);
+  } else if (!ok) {
+    atomicOr(p.err_flag, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, 32);
+}
+
 // ELL tiles: one CTA (8 warps) per tile.  An LPR-lane group owns 4 rows at a
 // time (4 x 4 features per lane in flight per slot), so short rows still
 // keep many B-row loads in flight.
@@ -377,61 +511,64 @@ __global__ void __launch_bounds__(kEllThreads, 4) spmm_ell_kernel(SpmmArgs p) {
 // ===========================================================================
 // value gradient: dvals[t] = <dY[row(t)], B[col(t)]>
 // ===========================================================================
-// Tensor-core k-steps: one CTA stages the step's 16 dY rows and 16 B rows in
-// shared memory, 128 features at a time, and computes only the live entries
-// (at most 2 per thread).  ELL tiles: an LPR-lane group keeps its row of dY
-// in registers and reduces one slot per iteration with shuffles.
-constexpr int kDvChunk = 128;
-constexpr int kDvPad = kDvChunk + 4;
-
+// Tensor-core tiles: one CTA per work chunk (see dvals_tc_kernel).  ELL
+// tiles: an LPR-lane group keeps its row of dY in registers and reduces one
+// slot per iteration with shuffles.
 __global__ void __launch_bounds__(128) dvals_tc_kernel(SpmmArgs p, const float* __restrict__ dY, long lddy,
                                                        float* __restrict__ dvals) {
-  __shared__ __align__(16) float ys[16 * kDvPad];
-  __shared__ __align__(16) float bs[16 * kDvPad];
-  const int ks = blockIdx.x;
-  const int tid = threadIdx.x;
+  // one CTA per tensor-core work chunk; warp w owns tile rows 4w..4w+3 and
+  // keeps their dY rows in registers; lane l owns features 4l..4l+3 of each
+  // 128-feature chunk.  A B row is loaded only when one of the warp's rows
+  // has a live entry in that column; dots reduce with shuffles.
+  const int chunk = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = p.tc_chunk_item[chunk];
+  const int kb = p.tc_chunk_kbeg[chunk], ke = p.tc_chunk_kbeg[chunk + 1];
   const int N = p.N;
-  int lo = 0, hi = p.tc_n_items;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (p.tc_item_kbeg[mid] <= ks) lo = mid; else hi = mid;
-  }
-  const int item = lo;
-  int id[2], e[2];
-  float acc[2] = {0.f, 0.f};
+  int orow[4];
 #pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    e[q] = tid + 128 * q;
-    id[q] = p.tc_nnz_id[(long)ks * 256 + e[q]];
-  }
-  if (!__syncthreads_or(id[0] >= 0 || id[1] >= 0)) return;
-  for (int fc = 0; fc < N; fc += kDvChunk) {
-    __syncthreads();
-    for (int i = tid; i < 16 * (kDvChunk / 4); i += 128) {
-      const int r = i / (kDvChunk / 4), c = (i % (kDvChunk / 4)) * 4;
-      const int orow = p.tc_out_rows[(long)item * 16 + r];
-      const int col = p.tc_cols[(long)ks * 16 + r];
-      const float4 vy = orow >= 0 ? ld_row4(dY + (long)orow * lddy, fc + c, N) : make_float4(0.f, 0.f, 0.f, 0.f);
-      const float4 vb = ld_row4(p.B + (long)col * p.ldb, fc + c, N);
-      *reinterpret_cast<float4*>(&ys[r * kDvPad + c]) = vy;
-      *reinterpret_cast<float4*>(&bs[r * kDvPad + c]) = vb;
+  for (int q = 0; q < 4; ++q) orow[q] = p.tc_out_rows[(long)item * 16 + warp * 4 + q];
+  for (int fc = 0; fc < N; fc += 128) {
+    const int f = fc + 4 * lane;
+    float4 y[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      y[q] = orow[q] >= 0 ? ld_row4(dY + (long)orow[q] * lddy, f, N) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int ks = kb; ks < ke; ++ks) {
+      // ids of this warp's 4 rows x 16 columns: lane l holds entries l and l+32
+      const int* idrow = p.tc_nnz_id + (long)ks * 256 + warp * 64;
+      const int id_a = idrow[lane], id_b = idrow[lane + 32];
+      const unsigned live_a = __ballot_sync(0xffffffffu, id_a >= 0);
+      const unsigned live_b = __ballot_sync(0xffffffffu, id_b >= 0);
+      if ((live_a | live_b) == 0u) continue;
+      const int col_l = p.tc_cols[(long)ks * 16 + (lane & 15)];
+#pragma unroll 1
+      for (int k = 0; k < 16; ++k) {
+        // entry (q, k) sits in half q/2 (a: rows 0,1; b: rows 2,3) at lane (q%2)*16 + k
+        const bool l0 = (live_a >> k) & 1u, l1 = (live_a >> (16 + k)) & 1u;
+        const bool l2 = (live_b >> k) & 1u, l3 = (live_b >> (16 + k)) & 1u;
+        if (!(l0 | l1 | l2 | l3)) continue;
+        const int col = __shfl_sync(0xffffffffu, col_l, k);
+        const float4 b = ld_row4(p.B + (long)col * p.ldb, f, N);
+        float d[4] = {l0 ? dot4(y[0], b) : 0.f, l1 ? dot4(y[1], b) : 0.f, l2 ? dot4(y[2], b) : 0.f,
+                      l3 ? dot4(y[3], b) : 0.f};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) d[q] += __shfl_xor_sync(0xffffffffu, d[q], o);
+        }
+        const int ida = __shfl_sync(0xffffffffu, id_a, k), idb = __shfl_sync(0xffffffffu, id_a, 16 + k);
+        const int idc = __shfl_sync(0xffffffffu, id_b, k), idd = __shfl_sync(0xffffffffu, id_b, 16 + k);
+        if (lane == 0) {
+          // accumulate over feature chunks (the caller zero-fills dvals)
+          if (l0) dvals[ida] += d[0];
+          if (l1) dvals[idb] += d[1];
+          if (l2) dvals[idc] += d[2];
+          if (l3) dvals[idd] += d[3];
+        }
+      }
     }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      if (id[q] < 0) continue;
-      const float* yr = &ys[(e[q] >> 4) * kDvPad];
-      const float* br = &bs[(e[q] & 15) * kDvPad];
-      float sum = 0.f;
-#pragma unroll 8
-      for (int c = 0; c < kDvChunk; c += 4)
-        sum += dot4(*reinterpret_cast<const float4*>(yr + c), *reinterpret_cast<const float4*>(br + c));
-      acc[q] += sum;
-    }
   }
-#pragma unroll
-  for (int q = 0; q < 2; ++q)
-    if (id[q] >= 0) dvals[id[q]] = acc[q];
 }
 
 template <int LPR>
@@ -505,7 +642,12 @@ __global__ void repack_values_kernel(SpmmArgs p, const float* __restrict__ vals,
     const int id = p.tc_nnz_id[i];
     const float v = id >= 0 ? vals[id] : 0.f;
     const int img = (n >> 3) * 128 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7);
-    if (p.tc_mode == STILE_TC_F16) {
+    if (p.tc_mode == STILE_TC_TF32) {
+      const int fi = (k >> 3) * 128 + (n >> 3) * 64 + ((k & 7) >> 2) * 32 + (n & 7) * 4 + (k & 3);
+      uint32_t t;
+      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
+      reinterpret_cast<uint32_t*>(tc_img)[ks * 256 + fi] = t;
+    } else if (p.tc_mode == STILE_TC_F16) {
       __half h = __float2half_rn(v);
       tc_img[ks * 256 + img] = *reinterpret_cast<uint16_t*>(&h);
     } else {
@@ -601,6 +743,15 @@ static cudaError_t launch_tc_t(const SpmmArgs& p, cudaStream_t st) {
 }
 
 cudaError_t launch_tc(const SpmmArgs& p, cudaStream_t st) {
+  if (p.tc_mode == STILE_TC_TF32) {
+    cudaError_t e = cudaFuncSetAttribute(spmm_tc_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kTfBytes);
+    if (e != cudaSuccess) return e;
+    const int grid = p.tc_n_chunks * p.n_fchunks;
+    if (grid == 0) return cudaSuccess;
+    spmm_tc_tf32_kernel<<<grid, kTfThreads, kTfBytes, st>>>(p);
+    return cudaGetLastError();
+  }
   switch (p.tc_mode) {
     case STILE_TC_F16: return launch_tc_t<STILE_TC_F16>(p, st);
     case STILE_TC_SPLIT_BF16: return launch_tc_t<STILE_TC_SPLIT_BF16>(p, st);
@@ -624,8 +775,8 @@ cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st) {
 template <int LPR>
 struct DvalsLaunch {
   static cudaError_t run(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {
-    if (p.tc_n_ksteps > 0) {
-      dvals_tc_kernel<<<p.tc_n_ksteps, 128, 0, st>>>(p, dY, lddy, dvals);
+    if (p.tc_n_chunks > 0) {
+      dvals_tc_kernel<<<p.tc_n_chunks, 128, 0, st>>>(p, dY, lddy, dvals);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }

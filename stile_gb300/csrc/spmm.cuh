@@ -79,6 +79,6 @@ struct SddmmArgs {
 cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st);
 
 cudaError_t launch_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
-                              uint32_t idesc, float* out, int* err, cudaStream_t st);
+                              uint32_t idesc, uint32_t kind, float* out, int* err, cudaStream_t st);
 
 }  // namespace stile

@@ -47,7 +47,7 @@ def run_probe(A, Bm, desc6):
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     d = (ctypes.c_uint32 * 6)(*desc6)
     idesc = (1 << 4) | (1 << 7) | (1 << 10) | (1 << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
-    rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, out.data_ptr(), err.data_ptr(),
+    rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, 0, out.data_ptr(), err.data_ptr(),
                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     _lib.check(rc, "probe")
     torch.cuda.synchronize()
@@ -69,3 +69,61 @@ def random_values(A, seed=0, dist="uniform"):
     rng = np.random.default_rng(seed)
     A.data = rng.uniform(-1, 1, size=A.nnz) if dist == "uniform" else rng.standard_normal(A.nnz)
     return A
+
+
+# tf32 path: A operand [128 (m) x 8 (k)] fp32, MN-major 128B-swizzle, atoms of
+# 32 features (LBO 1024 B); B operand [16 (n) x 8 (k)] fp32, K-major no
+# swizzle, core matrices 8 rows x 16 B, LBO 128 B (k), SBO 256 B (rows)
+TF32_DESC = (1024, 4096, 2, 128, 256, 0)
+
+
+def a_image_tf32(A, lbo=1024):
+    img = np.zeros(2048, dtype=np.uint32)
+    bits = np.ascontiguousarray(A, dtype=np.float32).view(np.uint32)
+    for m in range(128):
+        for k in range(8):
+            off = (m // 32) * lbo + k * 128 + ((((m % 32) // 4) ^ k) << 4) + (m % 4) * 4
+            img[off // 4] = bits[m, k]
+    return img
+
+
+def b_image_tf32(Bm, lbo=128, sbo=256):
+    img = np.zeros(2048, dtype=np.uint32)
+    bits = np.ascontiguousarray(Bm, dtype=np.float32).view(np.uint32)
+    for n in range(16):
+        for k in range(8):
+            off = (n // 8) * sbo + (k // 4) * lbo + (n % 8) * 16 + (k % 4) * 4
+            img[off // 4] = bits[n, k]
+    return img
+
+
+def run_probe_tf32(A, Bm, desc6=TF32_DESC):
+    import torch
+    from stile_gb300 import _lib
+    lib = _lib.load()
+    ai = torch.as_tensor(a_image_tf32(A, desc6[0]).view(np.int32).copy(), device="cuda")
+    bi = torch.as_tensor(b_image_tf32(Bm, desc6[3], desc6[4]).view(np.int32).copy(), device="cuda")
+    out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    d = (ctypes.c_uint32 * 6)(*desc6)
+    idesc = (1 << 4) | (2 << 7) | (2 << 10) | (1 << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
+    rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, 1, out.data_ptr(), err.data_ptr(),
+                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc, "probe")
+    torch.cuda.synchronize()
+    return out.cpu().numpy().reshape(128, 16), int(err.item())
+
+
+def tf32_trunc(x):
+    b = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32) & np.uint32(0xFFFFE000)
+    return b.view(np.float32)
+
+
+@functools.lru_cache(maxsize=None)
+def tf32_layout_ok():
+    rng = np.random.default_rng(6)
+    A = tf32_trunc(rng.standard_normal((128, 8)))
+    Bm = tf32_trunc(rng.standard_normal((16, 8)))
+    D, err = run_probe_tf32(A, Bm)
+    ref = A.astype(np.float64) @ Bm.astype(np.float64).T
+    return err == 0 and np.allclose(D, ref, rtol=1e-5, atol=1e-4)

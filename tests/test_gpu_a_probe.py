@@ -5,7 +5,7 @@ test runs before any fused-kernel test."""
 import numpy as np
 import pytest
 
-from gpu_util import KERNEL_DESC, bf16_round, run_probe
+from gpu_util import KERNEL_DESC, TF32_DESC, bf16_round, run_probe, run_probe_tf32, tf32_trunc
 
 pytestmark = pytest.mark.gpu
 
@@ -23,4 +23,21 @@ def test_umma_layout_matches_kernel_convention():
             report[desc] = (err, float(np.abs(D - ref).max()))
     print("probe report:", report)
     err, maxdiff = report[KERNEL_DESC]
+    assert err == 0 and maxdiff < 1e-3, report
+
+
+def test_umma_tf32_layout():
+    """kind::tf32 with fp32 operand images laid out as the tf32 tensor-core
+    path lays them out (A MN-major 128B swizzle, 32-feature atoms; B K-major
+    no swizzle).  Alternatives are reported for diagnosis."""
+    rng = np.random.default_rng(6)
+    A = tf32_trunc(rng.standard_normal((128, 8)))
+    Bm = tf32_trunc(rng.standard_normal((16, 8)))
+    ref = A.astype(np.float64) @ Bm.astype(np.float64).T
+    report = {}
+    for desc in [TF32_DESC, (1024, 4096, 2, 256, 128, 0), (2048, 1024, 2, 128, 256, 0)]:
+        D, err = run_probe_tf32(A, Bm, desc)
+        report[desc] = (err, float(np.abs(D - ref).max()))
+    print("tf32 probe report:", report)
+    err, maxdiff = report[TF32_DESC]
     assert err == 0 and maxdiff < 1e-3, report
