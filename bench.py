@@ -297,7 +297,7 @@ def _tf32_probe_ok():
     ta, tb = torch.as_tensor(ai, device="cuda"), torch.as_tensor(bi, device="cuda")
     out = torch.zeros(2048, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
-    d = (ctypes.c_uint32 * 6)(1024, 4096, 2, 128, 256, 0)
+    d = (ctypes.c_uint32 * 6)(1024, 2048, 2, 128, 256, 0)
     idesc = (1 << 4) | (2 << 7) | (2 << 10) | (1 << 15) | (2 << 17) | (8 << 24)
     rc = _lib.load().stile_debug_umma_probe(ta.data_ptr(), tb.data_ptr(), d, idesc, 1, out.data_ptr(),
                                             err.data_ptr(), None)

@@ -152,6 +152,40 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   zero.erase(std::unique(zero.begin(), zero.end()), zero.end());
   const long nck = (long)ck_item.size();
 
+  // value-gradient entry list from the tiles (needs the nonzero ids)
+  std::vector<int32_t> dv_row, dv_col, dv_id;
+  if (h->tc_nnz_id)
+    for (int i = 0; i < h->tc_n_items; ++i)
+      for (int r = 0; r < 16; ++r) {
+        const int orow = h->tc_out_rows[(long)i * 16 + r];
+        if (orow < 0) continue;
+        for (int ks = h->tc_item_kbeg[i]; ks < h->tc_item_kbeg[i + 1]; ++ks)
+          for (int k = 0; k < 16; ++k) {
+            const int id = h->tc_nnz_id[(long)ks * 256 + r * 16 + k];
+            if (id < 0) continue;
+            dv_row.push_back(orow);
+            dv_col.push_back(h->tc_cols[(long)ks * 16 + k]);
+            dv_id.push_back(id);
+          }
+      }
+  if (h->ell_nnz_id)
+    for (int i = 0; i < h->ell_n_items; ++i) {
+      const int K = h->ell_item_K[i];
+      for (int r = h->ell_item_row0[i]; r < h->ell_item_row0[i + 1]; ++r) {
+        const int orow = h->ell_out_row[r];
+        if (orow < 0) continue;
+        const long s0 = h->ell_item_slot0[i] + (long)(r - h->ell_item_row0[i]) * K;
+        for (int k = 0; k < h->ell_row_len[r]; ++k) {
+          const int id = h->ell_nnz_id[s0 + k];
+          if (id < 0) continue;
+          dv_row.push_back(orow);
+          dv_col.push_back(h->ell_kidx[s0 + k]);
+          dv_id.push_back(id);
+        }
+      }
+    }
+  const long ndv = (long)dv_id.size();
+
   Arena ar;
   const long ti = h->tc_n_items, tk = h->tc_n_ksteps;
   const long ei = h->ell_n_items, er = h->ell_n_rows, es = h->ell_n_slots;
@@ -174,6 +208,9 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   size_t i_ckb = ar.add(ck_kbeg.data(), ck_kbeg.size() * 4);
   size_t i_cki = ar.add(ck_item.data(), (size_t)nck * 4);
   size_t i_ckf = ar.add(ck_flags.data(), (size_t)nck * 4);
+  size_t i_dvr = ar.add(dv_row.data(), (size_t)ndv * 4);
+  size_t i_dvc = ar.add(dv_col.data(), (size_t)ndv * 4);
+  size_t i_dvi = ar.add(dv_id.data(), (size_t)ndv * 4);
   size_t i_err = ar.add(nullptr, 16);
 
   auto* plan = new StileSpmmPlan();
@@ -230,6 +267,10 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   plan->n_zero_rows = (int)zero.size();
   plan->zero_rows = (const int*)P(i_zero);
   a.tc_n_chunks = h->tc_n_items > 0 ? (int)nck : 0;
+  a.dv_n = ndv;
+  a.dv_row = (const int*)P(i_dvr);
+  a.dv_col = (const int*)P(i_dvc);
+  a.dv_id = (const int*)P(i_dvi);
   a.tc_chunk_kbeg = (const int*)P(i_ckb);
   a.tc_chunk_item = (const int*)P(i_cki);
   a.tc_chunk_flags = (const int*)P(i_ckf);
@@ -298,7 +339,7 @@ int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, c
   a.N = N;
   cudaError_t e = stile::launch_dvals(a, dY, lddy, dvals, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
-  g_launches += (a.tc_n_ksteps > 0) + (a.ell_n_items > 0);
+  g_launches += (a.dv_n > 0);
   return STILE_OK;
 }
 

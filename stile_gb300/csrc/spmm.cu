@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(kTcThreads) spmm_tc_kernel(SpmmArgs p) {
 // row is copied by cp.async straight into the A operand of kind::tf32
 // (features = M = 128, MN-major, 128-byte swizzle, 32-feature atoms,
 // LBO 1024 B; the two 8-row k groups of a k-step are 4096 B apart and feed
-// one MMA each).  The block values sit in the plan as the fp32 B-operand
+// one MMA each, so the descriptor's k-group stride is never used).  The block values sit in the plan as the fp32 B-operand
 // image (K-major, no swizzle, LBO 128 B, SBO 256 B; k halves 512 B apart).
 // Warps 0-3 produce (4 x 16 B copies per thread per k-step, completion
 // signalled on a full barrier by cp.async.mbarrier.arrive) and run the
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(kTfThreads) spmm_tc_tf32_kernel(SpmmArgs p) {
       const uint32_t sa = base + s * kTfStage;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const uint64_t ad = smem_desc(sa + h * 4096, 1024, 4096, kSwizzle128B);
+        const uint64_t ad = smem_desc(sa + h * 4096, 1024, 2048, kSwizzle128B);
         const uint64_t bd = smem_desc(sa + kTfA + h * 512, 128, 256, kSwizzleNone);
         umma_tf32(tmem, ad, bd, idesc, (step > 0 || h > 0) ? 1u : 0u);
       }
@@ -509,124 +509,9 @@ __global__ void __launch_bounds__(kEllThreads, 4) spmm_ell_kernel(SpmmArgs p) {
 }
 
 // ===========================================================================
-// value gradient: dvals[t] = <dY[row(t)], B[col(t)]>
+// value gradient: dvals[t] = <dY[row(t)], B[col(t)]> over the plan's entry
+// list (launch_dvals -> launch_sddmm_list)
 // ===========================================================================
-// Tensor-core tiles: one CTA per work chunk (see dvals_tc_kernel).  ELL
-// tiles: an LPR-lane group keeps its row of dY in registers and reduces one
-// slot per iteration with shuffles.
-__global__ void __launch_bounds__(128) dvals_tc_kernel(SpmmArgs p, const float* __restrict__ dY, long lddy,
-                                                       float* __restrict__ dvals) {
-  // one CTA per tensor-core work chunk; warp w owns tile rows 4w..4w+3 and
-  // keeps their dY rows in registers; lane l owns features 4l..4l+3 of each
-  // 128-feature chunk.  A B row is loaded only when one of the warp's rows
-  // has a live entry in that column; dots reduce with shuffles.
-  const int chunk = blockIdx.x;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int item = p.tc_chunk_item[chunk];
-  const int kb = p.tc_chunk_kbeg[chunk], ke = p.tc_chunk_kbeg[chunk + 1];
-  const int N = p.N;
-  int orow[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) orow[q] = p.tc_out_rows[(long)item * 16 + warp * 4 + q];
-  for (int fc = 0; fc < N; fc += 128) {
-    const int f = fc + 4 * lane;
-    float4 y[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      y[q] = orow[q] >= 0 ? ld_row4(dY + (long)orow[q] * lddy, f, N) : make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int ks = kb; ks < ke; ++ks) {
-      // ids of this warp's 4 rows x 16 columns: lane l holds entries l and l+32
-      const int* idrow = p.tc_nnz_id + (long)ks * 256 + warp * 64;
-      const int id_a = idrow[lane], id_b = idrow[lane + 32];
-      const unsigned live_a = __ballot_sync(0xffffffffu, id_a >= 0);
-      const unsigned live_b = __ballot_sync(0xffffffffu, id_b >= 0);
-      if ((live_a | live_b) == 0u) continue;
-      const int col_l = p.tc_cols[(long)ks * 16 + (lane & 15)];
-#pragma unroll 1
-      for (int k = 0; k < 16; ++k) {
-        // entry (q, k) sits in half q/2 (a: rows 0,1; b: rows 2,3) at lane (q%2)*16 + k
-        const bool l0 = (live_a >> k) & 1u, l1 = (live_a >> (16 + k)) & 1u;
-        const bool l2 = (live_b >> k) & 1u, l3 = (live_b >> (16 + k)) & 1u;
-        if (!(l0 | l1 | l2 | l3)) continue;
-        const int col = __shfl_sync(0xffffffffu, col_l, k);
-        const float4 b = ld_row4(p.B + (long)col * p.ldb, f, N);
-        float d[4] = {l0 ? dot4(y[0], b) : 0.f, l1 ? dot4(y[1], b) : 0.f, l2 ? dot4(y[2], b) : 0.f,
-                      l3 ? dot4(y[3], b) : 0.f};
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-          for (int q = 0; q < 4; ++q) d[q] += __shfl_xor_sync(0xffffffffu, d[q], o);
-        }
-        const int ida = __shfl_sync(0xffffffffu, id_a, k), idb = __shfl_sync(0xffffffffu, id_a, 16 + k);
-        const int idc = __shfl_sync(0xffffffffu, id_b, k), idd = __shfl_sync(0xffffffffu, id_b, 16 + k);
-        if (lane == 0) {
-          // accumulate over feature chunks (the caller zero-fills dvals)
-          if (l0) dvals[ida] += d[0];
-          if (l1) dvals[idb] += d[1];
-          if (l2) dvals[idc] += d[2];
-          if (l3) dvals[idd] += d[3];
-        }
-      }
-    }
-  }
-}
-
-template <int LPR>
-__global__ void __launch_bounds__(256, 4) dvals_ell_kernel(SpmmArgs p, const float* __restrict__ dY, long lddy,
-                                                           float* __restrict__ dvals) {
-  constexpr int RPW = kWarp / LPR;
-  constexpr int kGroups = 8 * RPW;
-  const int item = blockIdx.x;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int sub = lane / LPR, sl = lane % LPR;
-  const unsigned gmask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
-  const int row0 = p.ell_item_row0[item];
-  const int nrows = p.ell_item_row0[item + 1] - row0;
-  const int K = p.ell_item_K[item];
-  const long slot0 = p.ell_item_slot0[item];
-  const int N = p.N;
-  for (int r = warp * RPW + sub; r < nrows; r += kGroups) {
-    const int orow = p.ell_out_row[row0 + r];
-    const int len = orow >= 0 ? p.ell_row_len[row0 + r] : 0;
-    if (len == 0) continue;
-    const float* yrow = dY + (long)orow * lddy;
-    const long s0 = slot0 + (long)r * K;
-    if (N <= 4 * LPR) {
-      const float4 y = ld_row4(yrow, 4 * sl, N);
-      int k = 0;
-      for (; k + 2 <= len; k += 2) {
-        const float4 b0 = ld_row4(p.B + (long)__ldg(p.ell_kidx + s0 + k) * p.ldb, 4 * sl, N);
-        const float4 b1 = ld_row4(p.B + (long)__ldg(p.ell_kidx + s0 + k + 1) * p.ldb, 4 * sl, N);
-        float d0 = dot4(y, b0), d1 = dot4(y, b1);
-#pragma unroll
-        for (int o = LPR / 2; o > 0; o >>= 1) {
-          d0 += __shfl_xor_sync(gmask, d0, o);
-          d1 += __shfl_xor_sync(gmask, d1, o);
-        }
-        if (sl == 0) {
-          dvals[p.ell_nnz_id[s0 + k]] = d0;
-          dvals[p.ell_nnz_id[s0 + k + 1]] = d1;
-        }
-      }
-      if (k < len) {
-        const float4 b0 = ld_row4(p.B + (long)__ldg(p.ell_kidx + s0 + k) * p.ldb, 4 * sl, N);
-        float d0 = dot4(y, b0);
-#pragma unroll
-        for (int o = LPR / 2; o > 0; o >>= 1) d0 += __shfl_xor_sync(gmask, d0, o);
-        if (sl == 0) dvals[p.ell_nnz_id[s0 + k]] = d0;
-      }
-    } else {
-      for (int k = 0; k < len; ++k) {
-        const float* brow = p.B + (long)__ldg(p.ell_kidx + s0 + k) * p.ldb;
-        float d = 0.f;
-        for (int f = 4 * sl; f < N; f += 4 * LPR) d += dot4(ld_row4(yrow, f, N), ld_row4(brow, f, N));
-#pragma unroll
-        for (int o = LPR / 2; o > 0; o >>= 1) d += __shfl_xor_sync(gmask, d, o);
-        if (sl == 0) dvals[p.ell_nnz_id[s0 + k]] = d;
-      }
-    }
-  }
-}
 
 // ===========================================================================
 // value re-pack: refresh the plan's tile values from a CSR-ordered value
@@ -772,24 +657,8 @@ cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st) {
   return dispatch_lpr<EllLaunch>(lpr_for(p.N), p, st);
 }
 
-template <int LPR>
-struct DvalsLaunch {
-  static cudaError_t run(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {
-    if (p.tc_n_chunks > 0) {
-      dvals_tc_kernel<<<p.tc_n_chunks, 128, 0, st>>>(p, dY, lddy, dvals);
-      cudaError_t e = cudaGetLastError();
-      if (e != cudaSuccess) return e;
-    }
-    if (p.ell_n_items > 0) {
-      dvals_ell_kernel<LPR><<<p.ell_n_items, 256, 0, st>>>(p, dY, lddy, dvals);
-      return cudaGetLastError();
-    }
-    return cudaSuccess;
-  }
-};
-
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {
-  return dispatch_lpr<DvalsLaunch>(lpr_for(p.N), p, dY, lddy, dvals, st);
+  return launch_sddmm_list(p.dv_n, p.dv_row, p.dv_col, p.dv_id, dY, lddy, p.B, p.ldb, dvals, p.N, st);
 }
 
 }  // namespace stile

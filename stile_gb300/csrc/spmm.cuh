@@ -42,6 +42,12 @@ struct SpmmArgs {
   const float* ell_vals;
   const int* ell_kidx;
   const int* ell_nnz_id;
+  // value-gradient entry list enumerated from the tiles: tensor-core entries
+  // (item, row, k-step, column order) then ELL slots (row, slot order)
+  long dv_n;
+  const int* dv_row;
+  const int* dv_col;
+  const int* dv_id;
   // device error flag (bounded waits that gave up)
   int* err_flag;
 };
@@ -77,6 +83,8 @@ struct SddmmArgs {
 };
 
 cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st);
+cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const int* outs, const float* X,
+                              long ldx, const float* Y, long ldy, float* out, int F, cudaStream_t st);
 
 cudaError_t launch_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
                               uint32_t idesc, uint32_t kind, float* out, int* err, cudaStream_t st);

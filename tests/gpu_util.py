@@ -74,7 +74,7 @@ def random_values(A, seed=0, dist="uniform"):
 # tf32 path: A operand [128 (m) x 8 (k)] fp32, MN-major 128B-swizzle, atoms of
 # 32 features (LBO 1024 B); B operand [16 (n) x 8 (k)] fp32, K-major no
 # swizzle, core matrices 8 rows x 16 B, LBO 128 B (k), SBO 256 B (rows)
-TF32_DESC = (1024, 4096, 2, 128, 256, 0)
+TF32_DESC = (1024, 2048, 2, 128, 256, 0)
 
 
 def a_image_tf32(A, lbo=1024):
