@@ -443,13 +443,13 @@ __global__ void __launch_bounds__(kTfThreads) spmm_tc_tf32_kernel(SpmmArgs p) {
 }
 
 // ELL tiles: one CTA (8 warps) per tile.  An LPR-lane group owns 4 rows at a
-// time (4 x 4 features per lane in flight per slot), so short rows still
-// keep many B-row loads in flight.
+// time and loads two slots of each per iteration (8 B-row loads of 16 B in
+// flight per lane), so short rows still keep the memory system busy.
 constexpr int kEllThreads = 256;
 constexpr int kEllRows = 4;
 
 template <int LPR>
-__global__ void __launch_bounds__(kEllThreads, 4) spmm_ell_kernel(SpmmArgs p) {
+__global__ void __launch_bounds__(kEllThreads, 3) spmm_ell_kernel(SpmmArgs p) {
   constexpr int RPW = kWarp / LPR;
   constexpr int kGroups = (kEllThreads / kWarp) * RPW;
   const int item = blockIdx.x;
@@ -482,21 +482,29 @@ __global__ void __launch_bounds__(kEllThreads, 4) spmm_ell_kernel(SpmmArgs p) {
       float4 acc[kEllRows];
 #pragma unroll
       for (int q = 0; q < kEllRows; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int k = 0; k < maxlen; ++k) {
-        float4 b[kEllRows];
-        float v[kEllRows];
+      for (int k = 0; k < maxlen; k += 2) {
+        // two slots of each of the 4 rows: 8 B-row loads in flight per lane
+        float4 b[2 * kEllRows];
+        float v[2 * kEllRows];
 #pragma unroll
-        for (int q = 0; q < kEllRows; ++q) {
-          v[q] = 0.f;
-          b[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (k < len[q]) {
-            const long s = slot0 + (long)(rb + q) * K + k;
-            v[q] = __ldg(p.ell_vals + s);
-            b[q] = ld_row4(p.B + (long)__ldg(p.ell_kidx + s) * p.ldb, f, N);
+        for (int u = 0; u < 2; ++u) {
+#pragma unroll
+          for (int q = 0; q < kEllRows; ++q) {
+            const int i = u * kEllRows + q;
+            v[i] = 0.f;
+            b[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k + u < len[q]) {
+              const long s = slot0 + (long)(rb + q) * K + k + u;
+              v[i] = __ldg(p.ell_vals + s);
+              b[i] = ld_row4(p.B + (long)__ldg(p.ell_kidx + s) * p.ldb, f, N);
+            }
           }
         }
 #pragma unroll
-        for (int q = 0; q < kEllRows; ++q) fma4(acc[q], v[q], b[q]);
+        for (int u = 0; u < 2; ++u) {
+#pragma unroll
+          for (int q = 0; q < kEllRows; ++q) fma4(acc[q], v[u * kEllRows + q], b[u * kEllRows + q]);
+        }
       }
 #pragma unroll
       for (int q = 0; q < kEllRows; ++q) {
