@@ -449,7 +449,7 @@ constexpr int kEllThreads = 256;
 constexpr int kEllRows = 4;
 
 template <int LPR>
-__global__ void __launch_bounds__(kEllThreads, 3) spmm_ell_kernel(SpmmArgs p) {
+__global__ void __launch_bounds__(kEllThreads, 2) spmm_ell_kernel(SpmmArgs p) {
   constexpr int RPW = kWarp / LPR;
   constexpr int kGroups = (kEllThreads / kWarp) * RPW;
   const int item = blockIdx.x;
