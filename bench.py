@@ -277,37 +277,6 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def _tf32_probe_ok():
-    """One tcgen05.mma kind::tf32 on images laid out as the tf32 kernel lays
-    them out (the probe's shared memory covers every interpretation)."""
-    import ctypes
-    import torch
-    from stile_gb300 import _lib
-    rng = np.random.default_rng(6)
-    A = (rng.standard_normal((128, 8)).astype(np.float32).view(np.uint32) & np.uint32(0xFFFFE000)).view(np.float32)
-    Bm = (rng.standard_normal((16, 8)).astype(np.float32).view(np.uint32) & np.uint32(0xFFFFE000)).view(np.float32)
-    ai = np.zeros(2048, np.float32)
-    bi = np.zeros(2048, np.float32)
-    for m in range(128):
-        for k in range(8):
-            ai[((m // 32) * 1024 + k * 128 + ((((m % 32) // 4) ^ k) << 4) + (m % 4) * 4) // 4] = A[m, k]
-    for n_ in range(16):
-        for k in range(8):
-            bi[((n_ // 8) * 256 + (k // 4) * 128 + (n_ % 8) * 16 + (k % 4) * 4) // 4] = Bm[n_, k]
-    ta, tb = torch.as_tensor(ai, device="cuda"), torch.as_tensor(bi, device="cuda")
-    out = torch.zeros(2048, device="cuda")
-    err = torch.zeros(1, dtype=torch.int32, device="cuda")
-    d = (ctypes.c_uint32 * 6)(1024, 2048, 2, 128, 256, 0)
-    idesc = (1 << 4) | (2 << 7) | (2 << 10) | (1 << 15) | (2 << 17) | (8 << 24)
-    rc = _lib.load().stile_debug_umma_probe(ta.data_ptr(), tb.data_ptr(), d, idesc, 1, out.data_ptr(),
-                                            err.data_ptr(), None)
-    torch.cuda.synchronize()
-    if rc != 0 or int(err.item()) != 0:
-        return False
-    ref = A.astype(np.float64) @ Bm.astype(np.float64).T
-    return bool(np.allclose(out.cpu().numpy().reshape(128, 16), ref, rtol=1e-5, atol=1e-4))
-
-
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -328,9 +297,7 @@ def run_gpu(args):
     A, B_np, dC_np = make_workload()
     log(f"[bench] workload {A.shape} nnz={A.nnz} ({time.time() - t0:.1f}s)")
     t0 = time.time()
-    # tf32 tensor tiles read the fp32 B rows in place; confirm the operand
-    # layouts with the in-bounds layout probe first, else use bf16 tiles
-    tc_mode = D.TC_TF32 if _tf32_probe_ok() else D.TC_BF16
+    tc_mode = D.TC_BF16
     cfg = PlanConfig(tc_mode=tc_mode)
     op = SpmmOperator(A, N_FEAT, cfg)
     opT, perm = op.transposed
@@ -482,8 +449,7 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic",
             "config": {"workload": WORKLOAD, "M": int(A.shape[0]), "K": int(A.shape[1]), "nnz": int(nnz),
-                       "N": N_FEAT, "tc_tiles": ("tf32 operands (fp32 storage, no conversion), fp32 accumulate"
-                                                 if tc_mode == D.TC_TF32 else "bf16 operands, fp32 accumulate")
+                       "N": N_FEAT, "tc_tiles": "bf16 operands, fp32 accumulate"
                        + " (tcgen05, TMEM)",
                        "row_tiles": "fp32 (CUDA cores)", "plan": {f"{k[0]}{'/atomic' if k[1] else ''}": v
                                                                 for k, v in op.plan.summary().items()},

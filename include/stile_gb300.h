@@ -56,8 +56,7 @@ extern "C" {
 #define STILE_TC_F16 2         /* A, B rounded to fp16, fp32 accumulate */
 #define STILE_TC_SPLIT_BF16 4  /* hi+lo bf16 split of A and B, 4 products */
 #define STILE_TC_FP8 3         /* A e4m3 with per-tile scale, B e4m3, fp32 acc. */
-#define STILE_TC_TF32 5        /* A, B read as tf32 (fp32 storage), fp32 acc.; no
-                                  conversion pass: gathered B rows feed the MMA */
+
 
 /*
  * SpMM plan, device-ready host arrays (built by the emitter).
@@ -68,9 +67,7 @@ extern "C" {
  * image of one tcgen05.mma B operand (K-major, no swizzle):
  *   element (row n, col k) at byte (n/8)*256 + (k/8)*128 + (n%8)*16 + (k%8)*2
  * for 16-bit modes (bf16 / fp16); STILE_TC_SPLIT_BF16 stores the hi image
- * followed by the lo image (1024 B per k-step); STILE_TC_TF32 stores fp32
- * values (1024 B per k-step) at 4-byte index
- *   (k/8)*128 + (n/8)*64 + ((k%8)/4)*32 + (n%8)*4 + k%4.
+ * followed by the lo image (1024 B per k-step).
  *
  * ELL items: one per row-bucket tile; rows [ell_item_row0[i],
  * ell_item_row0[i+1]), every row with ell_item_K[i] slots starting at
@@ -89,7 +86,7 @@ typedef struct StileSpmmPlanHost {
   const int32_t* tc_out_rows;    /* [tc_n_items * 16] */
   const int32_t* tc_cols;        /* [tc_n_ksteps * 16] */
   const void* tc_vals;           /* [tc_n_ksteps * tc_kstep_bytes] */
-  int32_t tc_kstep_bytes;        /* 512 (bf16/fp16), 1024 (split, tf32) */
+  int32_t tc_kstep_bytes;        /* 512 (bf16/fp16), 1024 (split) */
   const float* tc_scales;        /* [tc_n_ksteps] fp8 per-tile scale, else NULL */
   const int32_t* tc_nnz_id;      /* [tc_n_ksteps * 256] row-major (n,k); -1: empty */
   int32_t ell_n_items, ell_n_rows, ell_n_slots;
@@ -156,11 +153,17 @@ int stile_sddmm_run(const StileSddmmPlan* plan, const float* X, int64_t ldx,
                     const float* Y, int64_t ldy, float* out, int32_t F,
                     void* stream);
 
-/* Plain CSR SpMM (fp32) with nonzero-balanced ranges per warp group,
- * vectorised B loads; nnz = indptr[M] (passed so no device read is needed). */
+/* Plain CSR SpMM (fp32) with nonzero-balanced ranges per warp group
+ * (stile_csr_group_nnz() nonzeros each), vectorised B loads; nnz = indptr[M]
+ * (passed so no device read is needed).  group_rows[g] (optional, may be
+ * NULL) is the row holding nonzero g * stile_csr_group_nnz(); without it
+ * every group binary-searches indptr. */
 int stile_csr_spmm_run(int32_t M, int64_t nnz, const int32_t* indptr, const int32_t* indices,
-                       const float* vals, const float* B, int64_t ldb,
+                       const float* vals, const int32_t* group_rows, const float* B, int64_t ldb,
                        float* C, int64_t ldc, int32_t N, void* stream);
+
+/* Nonzeros per warp group of the CSR kernel (for building group_rows). */
+int32_t stile_csr_group_nnz(void);
 
 /* Refresh the tile values of a plan from vals[nnz] (device, CSR order of the
  * pattern the plan was built for); the pattern and index arrays are kept.

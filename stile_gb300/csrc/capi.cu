@@ -1,8 +1,10 @@
 // C ABI: plan upload / free, entry points, error reporting.
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cstdio>
 #include <cstring>
+#include <queue>
 #include <string>
 #include <vector>
 
@@ -73,6 +75,8 @@ int stile_last_error(char* buf, size_t n) {
 
 int64_t stile_launch_count(void) { return g_launches.load(); }
 
+int32_t stile_csr_group_nnz(void) { return stile::kCsrGroupNnz; }
+
 int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   if (!h || !out) return fail(STILE_E_INVALID, "null argument");
   *out = nullptr;
@@ -82,9 +86,9 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
     return fail(STILE_E_INVALID, "negative count");
   const int mode = h->tc_mode;
   if (h->tc_n_items > 0) {
-    if (mode != STILE_TC_BF16 && mode != STILE_TC_F16 && mode != STILE_TC_SPLIT_BF16 && mode != STILE_TC_TF32)
+    if (mode != STILE_TC_BF16 && mode != STILE_TC_F16 && mode != STILE_TC_SPLIT_BF16)
       return fail(STILE_E_UNSUPPORTED, "tensor-tile mode not supported by this build");
-    const int want = (mode == STILE_TC_SPLIT_BF16 || mode == STILE_TC_TF32) ? 1024 : 512;
+    const int want = (mode == STILE_TC_SPLIT_BF16) ? 1024 : 512;
     if (h->tc_kstep_bytes != want) return fail(STILE_E_INVALID, "tc_kstep_bytes does not match mode");
     if (!h->tc_item_kbeg || !h->tc_item_flags || !h->tc_out_rows || !h->tc_cols || !h->tc_vals)
       return fail(STILE_E_INVALID, "missing tensor-tile array");
@@ -129,18 +133,27 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
 
   // tensor-core work chunks: items longer than kChunkSteps k-steps are split
   // into balanced runs that accumulate atomically; the rows of split owned
-  // items join the rows zeroed before the kernels
-  std::vector<int32_t> ck_kbeg{0}, ck_item, ck_flags;
+  // items join the rows zeroed before the kernels.  Chunks are stored longest
+  // first so that the persistent kernel's round-robin split is balanced.
+  std::vector<int32_t> ck_kbeg, ck_nk, ck_item, ck_flags;
   std::vector<int32_t> zero(h->zero_rows, h->zero_rows + h->n_zero_rows);
   for (int i = 0; i < h->tc_n_items; ++i) {
     const int kb = h->tc_item_kbeg[i], ke = h->tc_item_kbeg[i + 1];
     const int n = ke - kb;
+    if (n == 0) {  // no k-steps: an owned item's rows are zero, and no chunk is made
+      if (!(h->tc_item_flags[i] & 1))
+        for (int r = 0; r < 16; ++r)
+          if (h->tc_out_rows[(long)i * 16 + r] >= 0) zero.push_back(h->tc_out_rows[(long)i * 16 + r]);
+      continue;
+    }
     const int nch = n > stile::kChunkSteps ? (n + stile::kChunkSteps - 1) / stile::kChunkSteps : 1;
     const int per = (n + nch - 1) / nch;
     const bool split = nch > 1;
     const int atomic = (h->tc_item_flags[i] & 1) || split ? 1 : 0;
     for (int c = 0; c < nch; ++c) {
-      ck_kbeg.push_back(std::min(kb + (c + 1) * per, ke));
+      const int c0 = std::min(kb + c * per, ke), c1 = std::min(kb + (c + 1) * per, ke);
+      ck_kbeg.push_back(c0);
+      ck_nk.push_back(c1 - c0);
       ck_item.push_back(i);
       ck_flags.push_back(atomic);
     }
@@ -148,9 +161,125 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
       for (int r = 0; r < 16; ++r)
         if (h->tc_out_rows[(long)i * 16 + r] >= 0) zero.push_back(h->tc_out_rows[(long)i * 16 + r]);
   }
+  // ELL tiles as a stream of live entries in row order, cut into groups of
+  // at most `cap` entries at row boundaries.  Row code r stores into C row
+  // r; -(r + 1) adds atomically (atomic tiles; pieces of rows longer than a
+  // group, whose owned rows are zeroed first).  The capacity is the largest
+  // of 64, 32, 16 that still gives every warp the device keeps resident
+  // (48 per SM) a group.
+  std::vector<int32_t> e_col, e_rc, e_id, e_gptr{0};
+  std::vector<float> e_val;
+  {
+    long live = 0;
+    for (int i = 0; i < h->ell_n_items; ++i)
+      for (int r = h->ell_item_row0[i]; r < h->ell_item_row0[i + 1]; ++r)
+        if (h->ell_out_row[r] >= 0) live += h->ell_row_len[r];
+    int dev = 0, sms = 1;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 1;
+    const long warps = (long)sms * 48;
+    int cap = stile::kSegNnz;
+    while (cap > 16 && live / cap < warps) cap /= 2;
+    int fill = 0;
+    auto close_group = [&]() {
+      if (fill) {
+        e_gptr.push_back((int32_t)e_col.size());
+        fill = 0;
+      }
+    };
+    auto append = [&](long s0, int k0, int k1, int32_t code) {
+      for (int k = k0; k < k1; ++k) {
+        e_col.push_back(h->ell_kidx[s0 + k]);
+        e_val.push_back(h->ell_vals[s0 + k]);
+        e_rc.push_back(code);
+        if (h->ell_nnz_id) e_id.push_back(h->ell_nnz_id[s0 + k]);
+      }
+    };
+    for (int i = 0; i < h->ell_n_items; ++i) {
+      const int K = h->ell_item_K[i];
+      const bool atomic = (h->ell_item_flags[i] & 1) != 0;
+      for (int r = h->ell_item_row0[i]; r < h->ell_item_row0[i + 1]; ++r) {
+        const int orow = h->ell_out_row[r], len = h->ell_row_len[r];
+        if (orow < 0 || len <= 0) continue;
+        const long s0 = h->ell_item_slot0[i] + (long)(r - h->ell_item_row0[i]) * K;
+        if (len > cap) {
+          close_group();
+          if (!atomic) zero.push_back(orow);
+          for (int k0 = 0; k0 < len; k0 += cap) {
+            append(s0, k0, std::min(len, k0 + cap), -(orow + 1));
+            fill = 1;
+            close_group();
+          }
+        } else {
+          if (fill + len > cap) close_group();
+          append(s0, 0, len, atomic ? -(orow + 1) : orow);
+          fill += len;
+        }
+      }
+    }
+    close_group();
+  }
+  const long n_pos = (long)e_col.size();
+  if (n_pos > INT32_MAX) return fail(STILE_E_INVALID, "too many ELL entries");
   std::sort(zero.begin(), zero.end());
   zero.erase(std::unique(zero.begin(), zero.end()), zero.end());
   const long nck = (long)ck_item.size();
+
+  // persistent schedule of the tensor-core kernel: chunks, longest first,
+  // each to the least loaded of the kernel's resident CTAs; every CTA's
+  // chunks (and their k-steps) are then stored contiguously
+  int tc_grid = 0;
+  std::vector<int32_t> cta_chunk{0};
+  std::vector<int32_t> s_cols, s_nnz;
+  std::vector<uint8_t> s_vals;
+  if (nck > 0) {
+    const int resident = stile::tc_persistent_ctas();
+    if (resident <= 0) return fail(STILE_E_CUDA, "cannot size the tensor-core grid");
+    tc_grid = (int)std::min<long>(resident, nck);
+    std::vector<int32_t> by_len(nck);
+    for (long c = 0; c < nck; ++c) by_len[c] = (int32_t)c;
+    std::stable_sort(by_len.begin(), by_len.end(), [&](int32_t x, int32_t y) { return ck_nk[x] > ck_nk[y]; });
+    using Load = std::pair<long, int>;  // (k-steps so far, CTA)
+    std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
+    for (int b = 0; b < tc_grid; ++b) heap.push({0L, b});
+    std::vector<std::vector<int32_t>> owned(tc_grid);
+    for (long q = 0; q < nck; ++q) {
+      Load l = heap.top();
+      heap.pop();
+      owned[l.second].push_back(by_len[q]);
+      heap.push({l.first + ck_nk[by_len[q]], l.second});
+    }
+    std::vector<int32_t> order;
+    order.reserve(nck);
+    for (int b = 0; b < tc_grid; ++b) {
+      order.insert(order.end(), owned[b].begin(), owned[b].end());
+      cta_chunk.push_back((int32_t)order.size());
+    }
+    // k-steps in schedule order
+    const size_t kb = (size_t)h->tc_kstep_bytes;
+    s_cols.resize((size_t)h->tc_n_ksteps * 16);
+    s_vals.resize((size_t)h->tc_n_ksteps * kb);
+    if (h->tc_nnz_id) s_nnz.resize((size_t)h->tc_n_ksteps * 256);
+    std::vector<int32_t> kbeg2(nck), nk2(nck), item2(nck), flags2(nck);
+    long pos = 0;
+    for (long q = 0; q < nck; ++q) {
+      const int c = order[q];
+      const long src = ck_kbeg[c], n = ck_nk[c];
+      std::memcpy(&s_cols[pos * 16], h->tc_cols + src * 16, (size_t)n * 16 * 4);
+      std::memcpy(&s_vals[pos * kb], static_cast<const uint8_t*>(h->tc_vals) + src * kb, (size_t)n * kb);
+      if (h->tc_nnz_id) std::memcpy(&s_nnz[pos * 256], h->tc_nnz_id + src * 256, (size_t)n * 256 * 4);
+      kbeg2[q] = (int32_t)pos;
+      nk2[q] = (int32_t)n;
+      item2[q] = ck_item[c];
+      flags2[q] = ck_flags[c];
+      pos += n;
+    }
+    ck_kbeg.swap(kbeg2);
+    ck_nk.swap(nk2);
+    ck_item.swap(item2);
+    ck_flags.swap(flags2);
+    if (pos != h->tc_n_ksteps) return fail(STILE_E_INVALID, "tensor-core chunks do not cover the k-steps");
+  }
 
   // value-gradient entry list from the tiles (needs the nonzero ids)
   std::vector<int32_t> dv_row, dv_col, dv_id;
@@ -188,24 +317,22 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
 
   Arena ar;
   const long ti = h->tc_n_items, tk = h->tc_n_ksteps;
-  const long ei = h->ell_n_items, er = h->ell_n_rows, es = h->ell_n_slots;
   size_t i_kbeg = ar.add(h->tc_item_kbeg, ti ? (ti + 1) * 4 : 0);
   size_t i_flags = ar.add(h->tc_item_flags, ti * 4);
   size_t i_orows = ar.add(h->tc_out_rows, ti * 16 * 4);
-  size_t i_cols = ar.add(h->tc_cols, tk * 16 * 4);
-  size_t i_vals = ar.add(h->tc_vals, tk * (size_t)h->tc_kstep_bytes);
-  size_t i_tnid = ar.add(h->tc_nnz_id, h->tc_nnz_id ? tk * 256 * 4 : 0);
-  size_t i_erow0 = ar.add(h->ell_item_row0, ei ? (ei + 1) * 4 : 0);
-  size_t i_eK = ar.add(h->ell_item_K, ei * 4);
-  size_t i_eslot = ar.add(h->ell_item_slot0, ei * 4);
-  size_t i_eflag = ar.add(h->ell_item_flags, ei * 4);
-  size_t i_eout = ar.add(h->ell_out_row, er * 4);
-  size_t i_elen = ar.add(h->ell_row_len, er * 4);
-  size_t i_evals = ar.add(h->ell_vals, es * 4);
-  size_t i_ekidx = ar.add(h->ell_kidx, es * 4);
-  size_t i_enid = ar.add(h->ell_nnz_id, h->ell_nnz_id ? es * 4 : 0);
+  // k-step arrays in schedule order (every k-step belongs to exactly one chunk)
+  size_t i_cols = ar.add(s_cols.data(), s_cols.size() * 4);
+  size_t i_vals = ar.add(s_vals.data(), s_vals.size());
+  size_t i_tnid = ar.add(s_nnz.data(), s_nnz.size() * 4);
+  size_t i_ctac = ar.add(cta_chunk.data(), cta_chunk.size() * 4);
+  size_t i_egptr = ar.add(e_gptr.data(), e_gptr.size() * 4);
+  size_t i_ecol = ar.add(e_col.data(), (size_t)n_pos * 4);
+  size_t i_evals = ar.add(e_val.data(), (size_t)n_pos * 4);
+  size_t i_erc = ar.add(e_rc.data(), (size_t)n_pos * 4);
+  size_t i_enid = ar.add(e_id.data(), e_id.size() * 4);
   size_t i_zero = ar.add(zero.data(), zero.size() * 4);
-  size_t i_ckb = ar.add(ck_kbeg.data(), ck_kbeg.size() * 4);
+  size_t i_ckb = ar.add(ck_kbeg.data(), (size_t)nck * 4);
+  size_t i_ckn = ar.add(ck_nk.data(), (size_t)nck * 4);
   size_t i_cki = ar.add(ck_item.data(), (size_t)nck * 4);
   size_t i_ckf = ar.add(ck_flags.data(), (size_t)nck * 4);
   size_t i_dvr = ar.add(dv_row.data(), (size_t)ndv * 4);
@@ -249,21 +376,18 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   a.tc_vals = P(i_vals);
   a.tc_scales = nullptr;
   a.tc_nnz_id = h->tc_nnz_id ? (const int*)P(i_tnid) : nullptr;
-  a.ell_n_items = h->ell_n_items;
-  a.ell_item_row0 = (const int*)P(i_erow0);
-  a.ell_item_K = (const int*)P(i_eK);
-  a.ell_item_slot0 = (const int*)P(i_eslot);
-  a.ell_item_flags = (const int*)P(i_eflag);
-  a.ell_out_row = (const int*)P(i_eout);
-  a.ell_row_len = (const int*)P(i_elen);
+  a.ell_n_groups = (int)e_gptr.size() - 1;
+  a.ell_n_pos = n_pos;
+  a.ell_group_ptr = (const int*)P(i_egptr);
+  a.ell_kidx = (const int*)P(i_ecol);
   a.ell_vals = (const float*)P(i_evals);
-  a.ell_kidx = (const int*)P(i_ekidx);
+  a.ell_rowcode = (const int*)P(i_erc);
   a.ell_nnz_id = h->ell_nnz_id ? (const int*)P(i_enid) : nullptr;
   a.err_flag = plan->err_flag;
   plan->M = h->M;
   plan->K = h->K;
   plan->nnz = h->nnz;
-  plan->ell_n_slots = h->ell_n_slots;
+  plan->ell_n_slots = n_pos;
   plan->n_zero_rows = (int)zero.size();
   plan->zero_rows = (const int*)P(i_zero);
   a.tc_n_chunks = h->tc_n_items > 0 ? (int)nck : 0;
@@ -272,6 +396,9 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   a.dv_col = (const int*)P(i_dvc);
   a.dv_id = (const int*)P(i_dvi);
   a.tc_chunk_kbeg = (const int*)P(i_ckb);
+  a.tc_chunk_nk = (const int*)P(i_ckn);
+  a.tc_grid = tc_grid;
+  a.tc_cta_chunk = (const int*)P(i_ctac);
   a.tc_chunk_item = (const int*)P(i_cki);
   a.tc_chunk_flags = (const int*)P(i_ckf);
   *out = plan;
@@ -318,7 +445,7 @@ int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float
   if (a.tc_n_chunks) g_launches++;
   e = stile::launch_ell(a, st);
   if (e != cudaSuccess) return cuda_fail(e, "ELL SpMM launch");
-  if (a.ell_n_items) g_launches++;
+  if (a.ell_n_groups) g_launches++;
   return STILE_OK;
 }
 
@@ -328,7 +455,7 @@ int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, c
   if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
   if (!dvals) return fail(STILE_E_INVALID, "null dvals");
   if ((plan->args.tc_n_items && !plan->args.tc_nnz_id) ||
-      (plan->args.ell_n_items && !plan->args.ell_nnz_id))
+      (plan->args.ell_n_groups && !plan->args.ell_nnz_id))
     return fail(STILE_E_INVALID, "plan was uploaded without nonzero ids");
   int rc;
   if ((rc = check_dense(ldb, N, B, "B")) != 0) return rc;
@@ -346,7 +473,7 @@ int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, c
 int stile_spmm_plan_set_values(StileSpmmPlan* plan, const float* vals, void* stream) {
   if (!plan || !vals) return fail(STILE_E_INVALID, "null argument");
   if ((plan->args.tc_n_items && !plan->args.tc_nnz_id) ||
-      (plan->args.ell_n_items && !plan->args.ell_nnz_id))
+      (plan->args.ell_n_groups && !plan->args.ell_nnz_id))
     return fail(STILE_E_INVALID, "plan was uploaded without nonzero ids");
   cudaError_t e = stile::launch_repack(plan->args, vals, plan->ell_n_slots,
                                        static_cast<cudaStream_t>(stream));
@@ -368,7 +495,8 @@ int stile_spmm_plan_error_flag(StileSpmmPlan* plan, void* stream, int32_t* flag)
 }
 
 int stile_csr_spmm_run(int32_t M, int64_t nnz, const int32_t* indptr, const int32_t* indices, const float* vals,
-                       const float* B, int64_t ldb, float* C, int64_t ldc, int32_t N, void* stream) {
+                       const int32_t* group_rows, const float* B, int64_t ldb, float* C, int64_t ldc, int32_t N,
+                       void* stream) {
   if (M < 0 || N <= 0) return fail(STILE_E_INVALID, "bad shape");
   if (M == 0) return STILE_OK;
   if (!indptr || !indices || !vals) return fail(STILE_E_INVALID, "null CSR array");
@@ -376,7 +504,7 @@ int stile_csr_spmm_run(int32_t M, int64_t nnz, const int32_t* indptr, const int3
   if ((rc = check_dense(ldb, N, B, "B")) != 0) return rc;
   if ((rc = check_dense(ldc, N, C, "C")) != 0) return rc;
   if (nnz < 0) return fail(STILE_E_INVALID, "negative nnz");
-  cudaError_t e = stile::launch_csr_spmm(M, indptr, indices, vals, B, ldb, C, ldc, N, nnz,
+  cudaError_t e = stile::launch_csr_spmm(M, indptr, indices, vals, B, ldb, C, ldc, N, nnz, group_rows,
                                          static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "CSR SpMM launch");
   g_launches++;

@@ -96,6 +96,15 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes)
                : "memory");
 }
+// Bulk asynchronous global -> shared copy (no tensor map): both addresses
+// 16-byte aligned, bytes a multiple of 16; completion is signalled as
+// transaction bytes on the mbarrier at `bar`.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;" ::: "memory");
 }
@@ -142,11 +151,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.release.cta.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(bar)
+      : "memory");
+}
+
+// Arrive on the barrier and raise its expected transaction bytes.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 st, [%0], %1;\n\t}\n" ::"r"(bar),
+      "r"(bytes)
+      : "memory");
+}
+
 // Bounded wait: gives up after ~2^22 polls (each try_wait suspends for a
 // bounded, implementation-defined time) and reports failure to the caller.
+// After a few failed polls the thread sleeps between polls, so that waiting
+// warps leave the issue slots to the warps doing the work.
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
   for (uint32_t i = 0; i < (1u << 22); ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if (i >= 4) __nanosleep(32);
   }
   return false;
 }

@@ -2,9 +2,13 @@
 //
 //  * csr_spmm_kernel     plain CSR-row SpMM (the comparator)
 //  * zero_rows_kernel    zeroes output rows that no owned tile stores
-//  * spmm_tc_kernel      dense 16-row block tiles on the tensor cores
-//                        (tcgen05.mma, accumulator in TMEM), cp.async ring
-//  * spmm_ell_kernel     ELL row-bucket tiles on CUDA cores
+//  * spmm_tc_ws_kernel   dense 16-row block tiles on the tensor cores
+//                        (tcgen05.mma, accumulator in TMEM): warp-specialised
+//                        cp.async producers + MMA issuer (bf16 / fp16)
+//  * spmm_tc_kernel      the same with hi+lo split products and periodic
+//                        accumulator drains (split-bf16, fp32-level accuracy)
+//  * spmm_ell_seg_kernel ELL row-bucket tiles on CUDA cores, as a stream of
+//                        live entries cut into groups at row boundaries
 //                        The two launches together are the reference's
 //                        horizontally fused kernel (my_fuse_formats.py:2437):
 //                        the same tiles, split by template into two grids so
@@ -12,6 +16,8 @@
 //  * spmm_dvals_kernel   value gradient <dY[row], B[col]> for every nonzero,
 //                        walking the same tiles.
 #include "common.cuh"
+#include <algorithm>
+
 #include "spmm.cuh"
 
 namespace stile {
@@ -20,11 +26,12 @@ namespace stile {
 // plain CSR SpMM (the comparator)
 // ===========================================================================
 // Nonzero-balanced CSR: every LPR-lane group owns kCsrNnz consecutive
-// nonzeros, finds its first row by binary search in indptr and walks the
+// nonzeros, takes its first row from group_rows (or, when that is NULL,
+// from a binary search in indptr) and walks the
 // rows it touches (4 B rows in flight per lane).  A row lying wholly inside
 // the range is stored; a row that straddles a range boundary is accumulated
 // with atomics into a row that csr_prezero_kernel zeroed first.
-constexpr int kCsrNnz = 64;
+constexpr int kCsrNnz = kCsrGroupNnz;
 
 __device__ __forceinline__ int row_of_nnz(const int* __restrict__ indptr, int M, long t) {
   // largest r with indptr[r] <= t
@@ -56,7 +63,7 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int M, const int* __restr
                                                        const float* __restrict__ vals,
                                                        const float* __restrict__ B, long ldb,
                                                        float* __restrict__ C, long ldc, int N,
-                                                       int n_groups) {
+                                                       int n_groups, const int* __restrict__ group_rows) {
   const int lane = threadIdx.x & 31;
   const int sub = lane / LPR, sl = lane % LPR;
   const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
@@ -64,7 +71,7 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int M, const int* __restr
   const long nnz = indptr[M];
   const long t0 = (long)g * kCsrNnz;
   const long t1 = min(t0 + kCsrNnz, nnz);
-  int r = row_of_nnz(indptr, M, t0);
+  int r = group_rows ? __ldg(group_rows + g) : row_of_nnz(indptr, M, t0);
   long t = t0;
   while (r < M && t < t1) {
     const long rb = indptr[r], re = indptr[r + 1];
@@ -183,7 +190,7 @@ __global__ void __launch_bounds__(kTcThreads) spmm_tc_kernel(SpmmArgs p) {
   asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
 
   const int kb = p.tc_chunk_kbeg[chunk];
-  const int n = p.tc_chunk_kbeg[chunk + 1] - kb;
+  const int n = p.tc_chunk_nk[chunk];
   const int item = p.tc_chunk_item[chunk];
   const int N = p.N;
   const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
@@ -308,45 +315,72 @@ __global__ void __launch_bounds__(kTcThreads) spmm_tc_kernel(SpmmArgs p) {
   if (warp == 0) tmem_dealloc(tmem, 32);
 }
 
-// tf32 tensor-core kernel (B in fp32).  No conversion pass: each gathered B
-// row is copied by cp.async straight into the A operand of kind::tf32
-// (features = M = 128, MN-major, 128-byte swizzle, 32-feature atoms,
-// LBO 1024 B; the two 8-row k groups of a k-step are 4096 B apart and feed
-// one MMA each, so the descriptor's k-group stride is never used).  The block values sit in the plan as the fp32 B-operand
-// image (K-major, no swizzle, LBO 128 B, SBO 256 B; k halves 512 B apart).
-// Warps 0-3 produce (4 x 16 B copies per thread per k-step, completion
-// signalled on a full barrier by cp.async.mbarrier.arrive) and run the
-// epilogue; warp 4 waits on the full barrier, issues the two MMAs and
-// commits to the stage's empty barrier.
-constexpr int kTfStages = 4;
-constexpr uint32_t kTfA = 8192;                 // 16 k x 128 features x 4 B
-constexpr uint32_t kTfB = 1024;                 // 16 rows x 16 k x 4 B
-constexpr uint32_t kTfStage = kTfA + kTfB;      // 9216 = 9 x 1024
-constexpr uint32_t kTfBytes = 1024 + kTfStages * kTfStage + 128;
-constexpr int kTfThreads = 160;
+// Persistent bf16 / fp16 tensor-core kernel.
+//
+// The upload assigns chunks to the kernel's CTAs (longest first, each to the
+// least loaded CTA) and stores every CTA's k-steps contiguously, so a CTA's
+// work is the step range [s_beg, s_beg + S), walked once per 128-feature
+// slice; its units are (slice, chunk) pairs in that order.
+// Roles (warps 0-3 producers, warp 4 lane 0 MMA issuer, warps 5-8 epilogue):
+//  * Column ids: every 32 steps each producer thread loads 4 ids of the
+//    block after next with one 16-byte load and, one block later, stores
+//    them into a two-block shared ring; one producer barrier per block
+//    publishes it.  No copy ever waits on a column-id load.
+//  * Producers: per k-step thread (w, l) copies features 4l..4l+3 of the
+//    step's rows w, w+4, w+8, w+12 (and threads 0-31 the step's 512-byte
+//    value image) with cp.async into a kTcStages-deep raw ring, kTcStages-1
+//    steps ahead (commit groups, no register scoreboards).  It converts its
+//    own copies to bf16 / fp16 into operand slot g % 4 and one lane per warp
+//    arrives on the slot's full barrier; before refilling a slot lane 0
+//    waits on its empty barrier (committed by the MMA that read it).
+//  * MMA: per unit t waits until the epilogue released accumulator t % 4
+//    (TMEM columns 16 * (t % 4)), then per step waits for a full slot,
+//    issues tcgen05.mma and commits to the slot's empty barrier; a unit's
+//    last step also commits to the accumulator's full barrier.
+//  * Epilogue: per unit waits for its accumulator, reads it (warp w reads
+//    TMEM lanes 32 * (w % 4)..+31), releases it and writes C.
+// Every wait is bounded; a wait that gives up sets the error flag and ends
+// that role, and the others then end at their next (bounded) wait.
+constexpr int kTcStages = 5;                             // raw ring stages (4 steps in flight)
+constexpr int kAccBufs = 4;                              // accumulators of 16 TMEM columns
+constexpr int kColBlock = 32;                            // k-steps per column-id block
+constexpr uint32_t kWsRaw = kRawRows + kBStage;          // 8704 B: 16 fp32 rows + value image
+constexpr uint32_t kWsSlot = kAStage + 1024;             // A image + value image, 1024-aligned
+constexpr int kWsSlots = 4;                              // operand slots between producers and MMA
+constexpr uint32_t kColRing = 2 * kColBlock * 16 * 4;    // 4 KB
+constexpr uint32_t kWsBytes = 1024 + kWsSlots * kWsSlot + kTcStages * kWsRaw + kColRing + 256;
+constexpr int kWsThreads = 288;
 
-__global__ void __launch_bounds__(kTfThreads) spmm_tc_tf32_kernel(SpmmArgs p) {
+// kFull: every 128-feature slice is complete (N % 128 == 0)
+template <int MODE, bool kFull>
+__global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
   extern __shared__ uint8_t smem_raw[];
-  const int chunk = blockIdx.x / p.n_fchunks;
-  const int f0 = (blockIdx.x % p.n_fchunks) * 128;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
-  const uint32_t bars = base + kTfStages * kTfStage;  // full[S], empty[S], done
-  const uint32_t tmem_slot = bars + 8 * (2 * kTfStages + 1);
-  auto full = [&](int s) { return bars + 8 * s; };
-  auto empty = [&](int s) { return bars + 8 * (kTfStages + s); };
-  const uint32_t done = bars + 8 * (2 * kTfStages);
+  const uint32_t slots = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const uint32_t ring = slots + kWsSlots * kWsSlot;
+  const uint32_t cring = ring + kTcStages * kWsRaw;
+  const uint32_t bars = cring + kColRing;
+  // full[kWsSlots], empty[kWsSlots], acc_full[kAccBufs], acc_empty[kAccBufs], drain
+  const uint32_t full0 = bars, empty0 = bars + 8 * kWsSlots;
+  const uint32_t accf0 = bars + 16 * kWsSlots, acce0 = accf0 + 8 * kAccBufs;
+  const uint32_t drain = acce0 + 8 * kAccBufs;
+  const uint32_t tmem_slot = drain + 8;
 
   if (tid == 0) {
-    for (int s = 0; s < kTfStages; ++s) {
-      mbar_init(full(s), 128);
-      mbar_init(empty(s), 1);
+    for (int s = 0; s < kWsSlots; ++s) {
+      mbar_init(full0 + 8 * s, 4);
+      mbar_init(empty0 + 8 * s, 1);
     }
-    mbar_init(done, 1);
+    for (int b = 0; b < kAccBufs; ++b) {
+      mbar_init(accf0 + 8 * b, 1);
+      mbar_init(acce0 + 8 * b, 4);
+    }
+    mbar_init(drain, 1);
     fence_mbar_init();
   }
   if (warp == 0) {
-    tmem_alloc(tmem_slot, 32);
+    __syncwarp();
+    tmem_alloc(tmem_slot, 16 * kAccBufs);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -355,164 +389,246 @@ __global__ void __launch_bounds__(kTfThreads) spmm_tc_tf32_kernel(SpmmArgs p) {
   uint32_t tmem;
   asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
 
-  const int kb = p.tc_chunk_kbeg[chunk];
-  const int n = p.tc_chunk_kbeg[chunk + 1] - kb;
-  const int item = p.tc_chunk_item[chunk];
+  // this CTA's chunks and their contiguous k-steps
+  const int cb = __ldg(p.tc_cta_chunk + blockIdx.x);
+  const int nc = __ldg(p.tc_cta_chunk + blockIdx.x + 1) - cb;
+  const int s_beg = nc > 0 ? __ldg(p.tc_chunk_kbeg + cb) : 0;
+  const int S = nc > 0 ? __ldg(p.tc_chunk_kbeg + cb + nc - 1) + __ldg(p.tc_chunk_nk + cb + nc - 1) - s_beg : 0;
+  const int nf = p.n_fchunks;
+  const long T = (long)S * nf;  // this CTA's k-steps over all slices
+  const int n_units = nc * nf;
   const int N = p.N;
   bool ok = true;
 
   if (warp < 4) {
     // ---------------- producers ----------------
-    const int f = f0 + 4 * lane;
-    const uint32_t bytes = (f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u);
-    const int atom = lane >> 3, cic = lane & 7;
     const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
+    // column-id blocks: thread t carries ids of rows 4(t%4)..+3 of the
+    // block's step t/4
+    int4 cblk = make_int4(0, 0, 0, 0);
+    long cblk_g = 0;  // first step of the block held in cblk
+    auto col_block_load = [&](long g0b) {
+      cblk_g = g0b;
+      const long g = g0b + (tid >> 2);
+      if (g < T) {
+        int local = (int)(g % S);
+        cblk = __ldg(reinterpret_cast<const int4*>(p.tc_cols + (long)(s_beg + local) * 16) + (tid & 3));
+      }
+    };
+    auto col_block_store = [&]() {
+      const uint32_t half = (uint32_t)((cblk_g / kColBlock) & 1);
+      st_shared_v4(cring + half * (kColBlock * 64) + (uint32_t)(tid >> 2) * 64 + (uint32_t)(tid & 3) * 16,
+                   make_uint4((uint32_t)cblk.x, (uint32_t)cblk.y, (uint32_t)cblk.z, (uint32_t)cblk.w));
+    };
+    auto producer_sync = [&]() { asm volatile("bar.sync 1, 128;" ::: "memory"); };
+    // issue cursor: step gi = k-step ks of slice f0
+    long gi = 0;
+    int iks = s_beg, if0 = 0;
+    auto issue = [&]() {
+      if (gi % kColBlock == 0) {
+        // entering block gi / 32: publish it, then fetch the one after it
+        col_block_store();
+        producer_sync();
+        col_block_load(gi + kColBlock);
+      }
+      if (gi < T) {
+        const uint32_t sr = ring + (uint32_t)(gi % kTcStages) * kWsRaw;
+        const uint32_t crow = cring + (uint32_t)((gi / kColBlock) & 1) * (kColBlock * 64) +
+                              (uint32_t)(gi % kColBlock) * 64;
+        const int f = if0 + 4 * lane;
+        const uint32_t bytes = kFull ? 16u : ((f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u));
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int kk = warp + 4 * j;
+          uint32_t col;
+          asm volatile("ld.shared.u32 %0, [%1];" : "=r"(col) : "r"(crow + 4u * kk));
+          const float* row = p.B + (long)col * p.ldb;
+          cp_async16(sr + kk * 512 + lane * 16, bytes ? (const void*)(row + f) : (const void*)row, bytes);
+        }
+        if (tid < 32) cp_async16(sr + kRawRows + tid * 16, vals + (long)iks * kBStage + tid * 16, 16u);
+      }
+      ++gi;
+      if (++iks == s_beg + S) {
+        iks = s_beg;
+        if0 += 128;
+      }
+    };
+    col_block_load(0);
 #pragma unroll 1
-    for (int step = 0; step < n; ++step) {
-      const int s = step % kTfStages;
-      if (step >= kTfStages) {
-        if (!mbar_wait_bounded(empty(s), (uint32_t)((step / kTfStages) - 1) & 1u)) {
+    for (int j = 0; j < kTcStages - 1; ++j) {
+      issue();
+      cp_async_commit();
+    }
+#pragma unroll 1
+    for (long g = 0; g < T; ++g) {
+      issue();
+      cp_async_commit();
+      cp_async_wait<kTcStages - 1>();
+      const int slot = (int)(g % kWsSlots);
+      if (g >= kWsSlots) {
+        const uint32_t par = (uint32_t)((g - kWsSlots) / kWsSlots) & 1u;
+        bool got = true;
+        if (lane == 0) got = mbar_wait_bounded(empty0 + 8 * slot, par);
+        if (!__shfl_sync(0xffffffffu, got, 0)) {
           ok = false;
           break;
         }
+        if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par);  // completed: returns at once
       }
-      const uint32_t sa = base + s * kTfStage;
-      const long ks = kb + step;
+      const uint32_t sr = ring + (uint32_t)(g % kTcStages) * kWsRaw;
+      const uint32_t sa = slots + slot * kWsSlot;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int kk = warp + 4 * j;
-        const int g = kk >> 3, r = kk & 7;
-        const float* row = p.B + (long)p.tc_cols[ks * 16 + kk] * p.ldb;
-        const uint32_t dst = sa + g * 4096 + atom * 1024 + r * 128 + ((cic ^ r) << 4);
-        cp_async16(dst, bytes ? (const void*)(row + f) : (const void*)row, bytes);
+        const uint4 raw = ld_shared_v4(sr + kk * 512 + lane * 16);
+        const float4 v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y), __uint_as_float(raw.z),
+                                     __uint_as_float(raw.w));
+        const uint32_t o = a_img_off(4 * lane, kk);
+        if (MODE == STILE_TC_F16) st_shared_v2(sa + o, pack_f16x2(v.x, v.y), pack_f16x2(v.z, v.w));
+        else st_shared_v2(sa + o, pack_bf16x2(v.x, v.y), pack_bf16x2(v.z, v.w));
       }
-      if (tid < 64) cp_async16(sa + kTfA + tid * 16, vals + ks * kTfB + tid * 16, 16u);
-      cp_async_mbar_arrive_noinc(full(s));
+      if (tid < 32) st_shared_v4(sa + kAStage + tid * 16, ld_shared_v4(sr + kRawRows + tid * 16));
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(full0 + 8 * slot);
     }
-  } else if (lane == 0) {
+    cp_async_wait<0>();
+    // a producer that stopped early still arrives at every column-block
+    // barrier the others reach: issue() runs for gi in [0, T + kTcStages - 1)
+    if (!ok) {
+      for (; gi < T + kTcStages - 1; ++gi)
+        if (gi % kColBlock == 0) producer_sync();
+    }
+  } else if (warp == 4) {
     // ---------------- MMA issuer ----------------
-    const uint32_t idesc = make_idesc(2, 2, 1, 0, 128, 16);
+    if (lane == 0) {
+      const uint32_t idesc = (MODE == STILE_TC_F16) ? make_idesc(0, 0, 1, 0, 128, 16)
+                                                    : make_idesc(1, 1, 1, 0, 128, 16);
+      long g = 0;
 #pragma unroll 1
-    for (int step = 0; step < n; ++step) {
-      const int s = step % kTfStages;
-      if (!mbar_wait_bounded(full(s), (uint32_t)(step / kTfStages) & 1u)) {
+      for (int t = 0; t < n_units && ok; ++t) {
+        const int n = __ldg(p.tc_chunk_nk + cb + t % nc);
+        const int b = t % kAccBufs;
+        if (t >= kAccBufs && !mbar_wait_bounded(acce0 + 8 * b, (uint32_t)((t - kAccBufs) / kAccBufs) & 1u)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(16 * b);
+#pragma unroll 1
+        for (int s = 0; s < n; ++s, ++g) {
+          const int slot = (int)(g % kWsSlots);
+          if (!mbar_wait_bounded(full0 + 8 * slot, (uint32_t)(g / kWsSlots) & 1u)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = slots + slot * kWsSlot;
+          umma_f16(d, smem_desc(sa, kALbo, kASbo, kSwizzle128B),
+                   smem_desc(sa + kAStage, kBLbo, kBSbo, kSwizzleNone), idesc, s > 0 ? 1u : 0u);
+          umma_commit(empty0 + 8 * slot);
+        }
+        if (ok) umma_commit(accf0 + 8 * b);
+      }
+      // every MMA this thread issued has completed before TMEM is freed
+      umma_commit(drain);
+      if (!mbar_wait_bounded(drain, 0u)) ok = false;
+    }
+    __syncwarp();
+  } else {
+    // ---------------- epilogue ----------------
+    const int quarter = warp & 3;
+#pragma unroll 1
+    for (int t = 0; t < n_units; ++t) {
+      const int b = t % kAccBufs;
+      const uint32_t par = (uint32_t)(t / kAccBufs) & 1u;
+      bool got = true;
+      if (lane == 0) got = mbar_wait_bounded(accf0 + 8 * b, par);
+      if (!__shfl_sync(0xffffffffu, got, 0)) {
         ok = false;
         break;
       }
-      fence_proxy_async_smem();
+      if (lane != 0) mbar_wait_bounded(accf0 + 8 * b, par);  // completed: returns at once
       tc_fence_after();
-      const uint32_t sa = base + s * kTfStage;
+      uint32_t r[16];
+      tmem_ld16(tmem + (uint32_t)(16 * b) + ((uint32_t)(32 * quarter) << 16), r);
+      tmem_wait_ld();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acce0 + 8 * b);
+      const int c = cb + t % nc;
+      const int f = (t / nc) * 128 + 32 * quarter + lane;
+      if (kFull || f < N) {
+        const int item = __ldg(p.tc_chunk_item + c);
+        const bool atomic = (__ldg(p.tc_chunk_flags + c) & 1) != 0;
+        const int* orows = p.tc_out_rows + (long)item * 16;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const uint64_t ad = smem_desc(sa + h * 4096, 1024, 2048, kSwizzle128B);
-        const uint64_t bd = smem_desc(sa + kTfA + h * 512, 128, 256, kSwizzleNone);
-        umma_tf32(tmem, ad, bd, idesc, (step > 0 || h > 0) ? 1u : 0u);
-      }
-      umma_commit(empty(s));
-    }
-    umma_commit(done);
-  }
-  cp_async_wait<0>();
-
-  // ---------------- epilogue (warps 0-3) ----------------
-  if (warp < 4) {
-    const bool fin = mbar_wait_bounded(done, 0u);
-    tc_fence_after();
-    uint32_t r[16];
-    tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16), r);
-    tmem_wait_ld();
-    const int f = f0 + 32 * warp + lane;
-    const bool atomic = (p.tc_chunk_flags[chunk] & 1) != 0;
-    if (fin && ok && n > 0 && f < N) {
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int row = p.tc_out_rows[(long)item * 16 + i];
-        if (row < 0) continue;
-        float* dst = p.C + (long)row * p.ldc + f;
-        const float v = __uint_as_float(r[i]);
-        if (atomic) atomicAdd(dst, v); else *dst = v;
+        for (int i = 0; i < 16; ++i) {
+          const int row = __ldg(orows + i);
+          if (row < 0) continue;
+          float* dst = p.C + (long)row * p.ldc + f;
+          const float v = __uint_as_float(r[i]);
+          if (atomic) atomicAdd(dst, v); else *dst = v;
+        }
       }
     }
-    if (!fin || !ok) atomicOr(p.err_flag, 1);
-  } else if (!ok) {
-    atomicOr(p.err_flag, 1);
   }
+  if (!ok) atomicOr(p.err_flag, 1);
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, 32);
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, 16 * kAccBufs);
 }
 
-// ELL tiles: one CTA (8 warps) per tile.  An LPR-lane group owns 4 rows at a
-// time and loads two slots of each per iteration (8 B-row loads of 16 B in
-// flight per lane), so short rows still keep the memory system busy.
-constexpr int kEllThreads = 256;
-constexpr int kEllRows = 4;
+// ELL tiles as a stream of live entries (column, value, row code) in row
+// order.  An LPR-lane sub-group owns one group of <= kSegNnz entries and
+// walks it kSegBatch entries at a time: the batch's column ids, values and
+// row codes are broadcast loads, then kSegBatch B-row gathers are in flight
+// per lane; the running sum is flushed at every change of row code (store
+// for an owned row, atomic add for a row of an atomic tile or a piece of a
+// split row).  Few registers per thread, so 64 warps per SM keep enough
+// gathers in flight to approach the L2 gather rate.
+constexpr int kSegBatch = 4;
 
 template <int LPR>
-__global__ void __launch_bounds__(kEllThreads, 2) spmm_ell_kernel(SpmmArgs p) {
-  constexpr int RPW = kWarp / LPR;
-  constexpr int kGroups = (kEllThreads / kWarp) * RPW;
-  const int item = blockIdx.x;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int sub = lane / LPR, sl = lane % LPR;
-  const int row0 = p.ell_item_row0[item];
-  const int nrows = p.ell_item_row0[item + 1] - row0;
-  const int K = p.ell_item_K[item];
-  const long slot0 = p.ell_item_slot0[item];
-  const bool atomic = (p.ell_item_flags[item] & 1) != 0;
+__global__ void __launch_bounds__(256, 6) spmm_ell_seg_kernel(SpmmArgs p) {
+  const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
+  const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
+  if (g >= p.ell_n_groups) return;
+  const int p0 = __ldg(p.ell_group_ptr + g);
+  const int n = __ldg(p.ell_group_ptr + g + 1) - p0;
+  const int* __restrict__ kidx = p.ell_kidx + p0;
+  const float* __restrict__ vals = p.ell_vals + p0;
+  const int* __restrict__ rcode = p.ell_rowcode + p0;
   const int N = p.N;
-  const int g = warp * RPW + sub;
-  for (int rb = g * kEllRows; rb < nrows; rb += kGroups * kEllRows) {
-    int orow[kEllRows], len[kEllRows];
-    int maxlen = 0;
+  for (int fc = 0; fc < N; fc += 4 * LPR) {
+    const int f = fc + 4 * sl;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    int cur = __ldg(rcode);
+#pragma unroll 1
+    for (int b0 = 0; b0 < n; b0 += kSegBatch) {
+      float4 bv[kSegBatch];
 #pragma unroll
-    for (int q = 0; q < kEllRows; ++q) {
-      const int r = rb + q;
-      orow[q] = -1;
-      len[q] = 0;
-      if (r < nrows) {
-        orow[q] = p.ell_out_row[row0 + r];
-        len[q] = orow[q] >= 0 ? p.ell_row_len[row0 + r] : 0;
+      for (int u = 0; u < kSegBatch; ++u) {
+        const int i = min(b0 + u, n - 1);
+        bv[u] = b0 + u < n ? ld_row4(p.B + (long)__ldg(kidx + i) * p.ldb, f, N) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      maxlen = max(maxlen, len[q]);
-    }
-    if (maxlen == 0) continue;
-    for (int fc = 0; fc < N; fc += 4 * LPR) {
-      const int f = fc + 4 * sl;
-      float4 acc[kEllRows];
 #pragma unroll
-      for (int q = 0; q < kEllRows; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int k = 0; k < maxlen; k += 2) {
-        // two slots of each of the 4 rows: 8 B-row loads in flight per lane
-        float4 b[2 * kEllRows];
-        float v[2 * kEllRows];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-#pragma unroll
-          for (int q = 0; q < kEllRows; ++q) {
-            const int i = u * kEllRows + q;
-            v[i] = 0.f;
-            b[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (k + u < len[q]) {
-              const long s = slot0 + (long)(rb + q) * K + k + u;
-              v[i] = __ldg(p.ell_vals + s);
-              b[i] = ld_row4(p.B + (long)__ldg(p.ell_kidx + s) * p.ldb, f, N);
-            }
+      for (int u = 0; u < kSegBatch; ++u) {
+        if (b0 + u < n) {
+          const int code = __ldg(rcode + b0 + u);
+          if (code != cur) {
+            if (cur >= 0) st_row4(p.C + (long)cur * p.ldc, f, N, acc);
+            else red_row4(p.C + (long)(-cur - 1) * p.ldc, f, N, acc);
+            acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            cur = code;
           }
+          fma4(acc, __ldg(vals + b0 + u), bv[u]);
         }
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-#pragma unroll
-          for (int q = 0; q < kEllRows; ++q) fma4(acc[q], v[u * kEllRows + q], b[u * kEllRows + q]);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < kEllRows; ++q) {
-        if (orow[q] < 0) continue;
-        float* crow = p.C + (long)orow[q] * p.ldc;
-        if (atomic) red_row4(crow, f, N, acc[q]); else st_row4(crow, f, N, acc[q]);
       }
     }
+    if (cur >= 0) st_row4(p.C + (long)cur * p.ldc, f, N, acc);
+    else red_row4(p.C + (long)(-cur - 1) * p.ldc, f, N, acc);
   }
 }
 
@@ -535,12 +651,7 @@ __global__ void repack_values_kernel(SpmmArgs p, const float* __restrict__ vals,
     const int id = p.tc_nnz_id[i];
     const float v = id >= 0 ? vals[id] : 0.f;
     const int img = (n >> 3) * 128 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7);
-    if (p.tc_mode == STILE_TC_TF32) {
-      const int fi = (k >> 3) * 128 + (n >> 3) * 64 + ((k & 7) >> 2) * 32 + (n & 7) * 4 + (k & 3);
-      uint32_t t;
-      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
-      reinterpret_cast<uint32_t*>(tc_img)[ks * 256 + fi] = t;
-    } else if (p.tc_mode == STILE_TC_F16) {
+    if (p.tc_mode == STILE_TC_F16) {
       __half h = __float2half_rn(v);
       tc_img[ks * 256 + img] = *reinterpret_cast<uint16_t*>(&h);
     } else {
@@ -594,7 +705,7 @@ static cudaError_t dispatch_lpr(int lpr, Args... args) {
 template <int LPR>
 struct CsrLaunch {
   static cudaError_t run(int M, const int* indptr, const int* indices, const float* vals, const float* B,
-                         long ldb, float* C, long ldc, int N, long nnz, cudaStream_t st) {
+                         long ldb, float* C, long ldc, int N, long nnz, const int* group_rows, cudaStream_t st) {
     const int n_groups = (int)((nnz + kCsrNnz - 1) / kCsrNnz);
     csr_prezero_kernel<<<(M + 255) / 256, 256, 0, st>>>(M, indptr, C, ldc, N);
     cudaError_t e = cudaGetLastError();
@@ -602,14 +713,15 @@ struct CsrLaunch {
     constexpr int GPB = 256 / LPR;
     const int grid = (n_groups + GPB - 1) / GPB;
     if (grid == 0) return cudaSuccess;
-    csr_spmm_kernel<LPR><<<grid, 256, 0, st>>>(M, indptr, indices, vals, B, ldb, C, ldc, N, n_groups);
+    csr_spmm_kernel<LPR><<<grid, 256, 0, st>>>(M, indptr, indices, vals, B, ldb, C, ldc, N, n_groups, group_rows);
     return cudaGetLastError();
   }
 };
 
 cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const float* vals,
-                            const float* B, long ldb, float* C, long ldc, int N, long nnz, cudaStream_t st) {
-  return dispatch_lpr<CsrLaunch>(lpr_for(N), M, indptr, indices, vals, B, ldb, C, ldc, N, nnz, st);
+                            const float* B, long ldb, float* C, long ldc, int N, long nnz,
+                            const int* group_rows, cudaStream_t st) {
+  return dispatch_lpr<CsrLaunch>(lpr_for(N), M, indptr, indices, vals, B, ldb, C, ldc, N, nnz, group_rows, st);
 }
 
 cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st) {
@@ -635,28 +747,73 @@ static cudaError_t launch_tc_t(const SpmmArgs& p, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// CTAs of `kernel` resident per SM at `threads` threads and `smem` bytes of
+// dynamic shared memory, from the device's limits (shared memory with the
+// per-block reservation, registers, threads, blocks); at least 1.
+template <typename K>
+static cudaError_t resident_ctas(K kernel, int threads, size_t smem, int* sms, int* per_sm) {
+  int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0, thr_sm = 0, blk_sm = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
+    return e;
+  if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess)
+    return e;
+  if ((e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess)
+    return e;
+  if ((e = cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&blk_sm, cudaDevAttrMaxBlocksPerMultiprocessor, dev)) != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  if ((e = cudaFuncGetAttributes(&fa, kernel)) != cudaSuccess) return e;
+  const int warps = (threads + 31) / 32;
+  const int regs_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
+  const long by_smem = (long)smem_sm / (long)(smem + fa.sharedSizeBytes + reserved);
+  const long by_regs = regs_warp > 0 ? (long)(regs_sm / regs_warp) / warps : blk_sm;
+  const long by_thr = thr_sm / (warps * 32);
+  long n = std::min(std::min(by_smem, by_regs), std::min(by_thr, (long)blk_sm));
+  *per_sm = (int)std::max(1L, n);
+  return cudaSuccess;
+}
+
+template <int MODE, bool kFull>
+static cudaError_t launch_ws_t(const SpmmArgs& p, cudaStream_t st) {
+  auto k = spmm_tc_ws_kernel<MODE, kFull>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWsBytes);
+  if (e != cudaSuccess) return e;
+  // shared memory for the resident CTAs; the rest of the unified L1 /
+  // shared storage stays L1
+  e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  if (p.tc_n_chunks == 0 || p.tc_grid == 0) return cudaSuccess;
+  k<<<p.tc_grid, kWsThreads, kWsBytes, st>>>(p);
+  return cudaGetLastError();
+}
+
+int tc_persistent_ctas() {
+  int sms = 0, per_sm = 0;
+  if (resident_ctas(spmm_tc_ws_kernel<STILE_TC_BF16, true>, kWsThreads, kWsBytes, &sms, &per_sm) != cudaSuccess)
+    return 0;
+  return sms * per_sm;
+}
+
 cudaError_t launch_tc(const SpmmArgs& p, cudaStream_t st) {
-  if (p.tc_mode == STILE_TC_TF32) {
-    cudaError_t e = cudaFuncSetAttribute(spmm_tc_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kTfBytes);
-    if (e != cudaSuccess) return e;
-    const int grid = p.tc_n_chunks * p.n_fchunks;
-    if (grid == 0) return cudaSuccess;
-    spmm_tc_tf32_kernel<<<grid, kTfThreads, kTfBytes, st>>>(p);
-    return cudaGetLastError();
-  }
   switch (p.tc_mode) {
-    case STILE_TC_F16: return launch_tc_t<STILE_TC_F16>(p, st);
+    case STILE_TC_F16:
+      return p.N % 128 == 0 ? launch_ws_t<STILE_TC_F16, true>(p, st) : launch_ws_t<STILE_TC_F16, false>(p, st);
     case STILE_TC_SPLIT_BF16: return launch_tc_t<STILE_TC_SPLIT_BF16>(p, st);
-    default: return launch_tc_t<STILE_TC_BF16>(p, st);
+    default:
+      return p.N % 128 == 0 ? launch_ws_t<STILE_TC_BF16, true>(p, st) : launch_ws_t<STILE_TC_BF16, false>(p, st);
   }
 }
 
 template <int LPR>
 struct EllLaunch {
   static cudaError_t run(const SpmmArgs& p, cudaStream_t st) {
-    if (p.ell_n_items == 0) return cudaSuccess;
-    spmm_ell_kernel<LPR><<<p.ell_n_items, kEllThreads, 0, st>>>(p);
+    if (p.ell_n_groups == 0) return cudaSuccess;
+    const long groups_per_block = 256 / LPR;
+    const long grid = (p.ell_n_groups + groups_per_block - 1) / groups_per_block;
+    spmm_ell_seg_kernel<LPR><<<(unsigned)grid, 256, 0, st>>>(p);
     return cudaGetLastError();
   }
 };

@@ -19,7 +19,12 @@ struct SpmmArgs {
   int tc_mode;
   // tensor-core work chunks (items split into runs of <= kChunkSteps k-steps)
   int tc_n_chunks;
-  const int* tc_chunk_kbeg;   // [tc_n_chunks + 1]
+  const int* tc_chunk_kbeg;   // [tc_n_chunks] first k-step
+  const int* tc_chunk_nk;     // [tc_n_chunks] k-steps
+  // persistent schedule: CTA b owns chunks [tc_cta_chunk[b], tc_cta_chunk[b + 1]),
+  // whose k-steps are contiguous
+  int tc_grid;
+  const int* tc_cta_chunk;    // [tc_grid + 1]
   const int* tc_chunk_item;   // [tc_n_chunks]
   const int* tc_chunk_flags;  // [tc_n_chunks] bit0: atomic
   // tensor-core items
@@ -31,17 +36,16 @@ struct SpmmArgs {
   const void* tc_vals;
   const float* tc_scales;
   const int* tc_nnz_id;
-  // ELL items
-  int ell_n_items;
-  const int* ell_item_row0;
-  const int* ell_item_K;
-  const int* ell_item_slot0;
-  const int* ell_item_flags;
-  const int* ell_out_row;
-  const int* ell_row_len;
-  const float* ell_vals;
-  const int* ell_kidx;
-  const int* ell_nnz_id;
+  // ELL tiles, compacted at upload into a stream of live entries in row
+  // order, cut into groups of at most kSegNnz entries at row boundaries
+  // (rows longer than that are split into atomic pieces of their own)
+  int ell_n_groups;
+  long ell_n_pos;
+  const int* ell_group_ptr;  // [ell_n_groups + 1]
+  const int* ell_kidx;       // [ell_n_pos] column of B
+  const float* ell_vals;     // [ell_n_pos]
+  const int* ell_rowcode;    // [ell_n_pos] out row r (store) or -(r + 1) (atomic add)
+  const int* ell_nnz_id;     // [ell_n_pos] nonzero id (or NULL)
   // value-gradient entry list enumerated from the tiles: tensor-core entries
   // (item, row, k-step, column order) then ELL slots (row, slot order)
   long dv_n;
@@ -53,9 +57,15 @@ struct SpmmArgs {
 };
 
 cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const float* vals,
-                            const float* B, long ldb, float* C, long ldc, int N, long nnz, cudaStream_t st);
+                            const float* B, long ldb, float* C, long ldc, int N, long nnz,
+                            const int* group_rows, cudaStream_t st);
+constexpr int kCsrGroupNnz = 64;  // nonzeros per warp group of the CSR kernel
+constexpr int kSegNnz = 64;       // entries per group of the ELL stream kernel
 cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st);
 cudaError_t launch_tc(const SpmmArgs& p, cudaStream_t st);
+// CTAs of the persistent tensor-core kernel resident on the current device
+// (0 on error)
+int tc_persistent_ctas();
 cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st);
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals,
                          cudaStream_t st);

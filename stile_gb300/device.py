@@ -30,7 +30,7 @@ import scipy.sparse as sp
 from .emit import emit_sddmm_reference, emit_spmm_reference
 from .plan import ELL, ONE_D, TC, TC_SDDMM
 
-TC_BF16, TC_F16, TC_FP8, TC_SPLIT_BF16, TC_TF32 = 1, 2, 3, 4, 5
+TC_BF16, TC_F16, TC_FP8, TC_SPLIT_BF16 = 1, 2, 3, 4
 
 
 class ValueIndex:
@@ -72,24 +72,6 @@ def _to_bf16_bits(x):
 
 def _bf16_bits_to_f32(b):
     return (b.astype(np.uint32) << 16).view(np.float32)
-
-
-def _to_tf32(x):
-    """Round-to-nearest float32 -> tf32 (10 mantissa bits), kept in fp32."""
-    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
-    r = ((u + 0x1000) & 0xFFFFE000).astype(np.uint32)
-    return r.view(np.float32)
-
-
-def operand_image_tf32(vals):
-    """[n_ksteps, 16 (n), 16 (k)] fp32 -> [n_ksteps, 256] fp32 in the tf32
-    B-operand layout: k halves of 8 (128 floats each), K-major core matrices
-    of 8 rows x 4 elements: index (k//8)*128 + (n//8)*64 + ((k%8)//4)*32 +
-    (n%8)*4 + k%4."""
-    nk = vals.shape[0]
-    v = vals.reshape(nk, 2, 8, 2, 2, 4)            # (ks, n_grp, n_in, k_half, k_core, k_in)
-    v = v.transpose(0, 3, 1, 4, 2, 5)              # (ks, k_half, n_grp, k_core, n_in, k_in)
-    return np.ascontiguousarray(v.reshape(nk, 256))
 
 
 def _to_f16_bits(x):
@@ -214,9 +196,6 @@ def build_spmm_device(tiles, A, N=32, tc_mode=TC_BF16, emitted=None):
     elif tc_mode == TC_F16:
         img = operand_image_16bit(_to_f16_bits(vals_f).reshape(n_ks, 16, 16))
         tc_bytes = 512
-    elif tc_mode == TC_TF32:
-        img = operand_image_tf32(_to_tf32(vals_f).reshape(n_ks, 16, 16))
-        tc_bytes = 1024
     elif tc_mode == TC_SPLIT_BF16:
         hi = _to_bf16_bits(vals_f)
         lo = _to_bf16_bits(vals_f - _bf16_bits_to_f32(hi))

@@ -198,6 +198,11 @@ class CsrMatrix:
         self.indices = torch.as_tensor(A.indices.astype(np.int32), device=device)
         self.vals = torch.as_tensor(A.data.astype(np.float32), device=device)
         self.lib = _lib.load()
+        # first row of every nonzero-balanced group of the CSR kernel
+        gn = int(self.lib.stile_csr_group_nnz())
+        starts = np.arange(0, max(A.nnz, 1), gn, dtype=np.int64)
+        rows = np.searchsorted(A.indptr, starts, side="right") - 1
+        self.group_rows = torch.as_tensor(np.minimum(rows, max(A.shape[0] - 1, 0)).astype(np.int32), device=device)
 
     def spmm(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         B, ldb = dense_operand(B, "B")
@@ -207,8 +212,8 @@ class CsrMatrix:
         else:
             ldc = out.stride(0)
         _lib.check(self.lib.stile_csr_spmm_run(self.shape[0], self.nnz, self.indptr.data_ptr(), self.indices.data_ptr(),
-                                               self.vals.data_ptr(), B.data_ptr(), ldb, out.data_ptr(), ldc,
-                                               N, _stream()), "stile_csr_spmm_run")
+                                               self.vals.data_ptr(), self.group_rows.data_ptr(), B.data_ptr(), ldb,
+                                               out.data_ptr(), ldc, N, _stream()), "stile_csr_spmm_run")
         return out
 
 

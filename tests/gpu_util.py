@@ -71,9 +71,9 @@ def random_values(A, seed=0, dist="uniform"):
     return A
 
 
-# tf32 path: A operand [128 (m) x 8 (k)] fp32, MN-major 128B-swizzle, atoms of
-# 32 features (LBO 1024 B); B operand [16 (n) x 8 (k)] fp32, K-major no
-# swizzle, core matrices 8 rows x 16 B, LBO 128 B (k), SBO 256 B (rows)
+# kind::tf32 probe images.  MN-major variant of A [128 (m) x 8 (k)] fp32:
+# 128B-swizzle, atoms of 32 features (LBO 1024 B).  B [16 (n) x 8 (k)] fp32,
+# K-major no swizzle, core matrices 8 rows x 16 B, LBO 128 B (k), SBO 256 B.
 TF32_DESC = (1024, 2048, 2, 128, 256, 0)
 
 
@@ -97,16 +97,30 @@ def b_image_tf32(Bm, lbo=128, sbo=256):
     return img
 
 
-def run_probe_tf32(A, Bm, desc6=TF32_DESC):
+def a_image_tf32_kmajor(A, lbo=128, sbo=256):
+    """A [128 (m) x 8 (k)] fp32, K-major no swizzle: core matrices 8 rows x
+    4 elements, LBO between the two k cores, SBO between 8-row groups."""
+    img = np.zeros(2048, dtype=np.uint32)
+    bits = np.ascontiguousarray(A, dtype=np.float32).view(np.uint32)
+    for m in range(128):
+        for k in range(8):
+            off = (m // 8) * sbo + (k // 4) * lbo + (m % 8) * 16 + (k % 4) * 4
+            img[off // 4] = bits[m, k]
+    return img
+
+
+def run_probe_tf32(A, Bm, desc6=TF32_DESC, a_kmajor=False):
     import torch
     from stile_gb300 import _lib
     lib = _lib.load()
-    ai = torch.as_tensor(a_image_tf32(A, desc6[0]).view(np.int32).copy(), device="cuda")
+    aimg = a_image_tf32_kmajor(A, desc6[0], desc6[1]) if a_kmajor else a_image_tf32(A, desc6[0])
+    ai = torch.as_tensor(aimg.view(np.int32).copy(), device="cuda")
     bi = torch.as_tensor(b_image_tf32(Bm, desc6[3], desc6[4]).view(np.int32).copy(), device="cuda")
     out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     d = (ctypes.c_uint32 * 6)(*desc6)
-    idesc = (1 << 4) | (2 << 7) | (2 << 10) | (1 << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
+    a_mn = 0 if a_kmajor else 1
+    idesc = (1 << 4) | (2 << 7) | (2 << 10) | (a_mn << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
     rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, 1, out.data_ptr(), err.data_ptr(),
                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     _lib.check(rc, "probe")
@@ -117,13 +131,3 @@ def run_probe_tf32(A, Bm, desc6=TF32_DESC):
 def tf32_trunc(x):
     b = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32) & np.uint32(0xFFFFE000)
     return b.view(np.float32)
-
-
-@functools.lru_cache(maxsize=None)
-def tf32_layout_ok():
-    rng = np.random.default_rng(6)
-    A = tf32_trunc(rng.standard_normal((128, 8)))
-    Bm = tf32_trunc(rng.standard_normal((16, 8)))
-    D, err = run_probe_tf32(A, Bm)
-    ref = A.astype(np.float64) @ Bm.astype(np.float64).T
-    return err == 0 and np.allclose(D, ref, rtol=1e-5, atol=1e-4)

@@ -14,7 +14,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 def declared_functions():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|int64_t)\s+(stile_\w+)\s*\(", src, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|int32_t)\s+(stile_\w+)\s*\(", src, flags=re.M)))
 
 
 def test_header_declares_entry_points():
@@ -42,4 +42,4 @@ def test_invalid_arguments_are_reported_not_aborted():
     assert rc == -1
     assert "negative" in _lib.last_error()
     assert lib.stile_spmm_run(None, None, 0, None, 0, 4, None) == -1
-    assert lib.stile_csr_spmm_run(-1, 0, None, None, None, None, 4, None, 4, 4, None) == -1
+    assert lib.stile_csr_spmm_run(-1, 0, None, None, None, None, None, 4, None, 4, 4, None) == -1

@@ -48,18 +48,3 @@ def test_operand_image_layout():
             assert img[idx] == n * 16 + k
 
 
-def test_operand_image_tf32_layout():
-    v = np.arange(256, dtype=np.float32).reshape(1, 16, 16)  # value = n*16 + k
-    img = D.operand_image_tf32(v)[0]
-    for n in range(16):
-        for k in range(16):
-            idx = (k // 8) * 128 + (n // 8) * 64 + ((k % 8) // 4) * 32 + (n % 8) * 4 + k % 4
-            assert img[idx] == n * 16 + k
-
-
-def test_tf32_rounding():
-    x = np.array([1.0, 1.0 + 2 ** -11, 1.0 + 3 * 2 ** -11, -2.5, 0.0], dtype=np.float32)
-    r = D._to_tf32(x)
-    assert r[0] == 1.0 and r[3] == -2.5 and r[4] == 0.0
-    # 10 mantissa bits survive, the 11th rounds
-    assert np.all((r.view(np.uint32) & 0x1FFF) == 0)

@@ -27,17 +27,22 @@ def test_umma_layout_matches_kernel_convention():
 
 
 def test_umma_tf32_layout():
-    """kind::tf32 with fp32 operand images laid out as the tf32 tensor-core
-    path lays them out (A MN-major 128B swizzle, 32-feature atoms; B K-major
-    no swizzle).  Alternatives are reported for diagnosis."""
+    """kind::tf32 with both fp32 operands K-major, no swizzle (core matrices
+    of 8 rows x 16 B, LBO 128 B along k, SBO 256 B between 8-row groups)
+    equals A @ B^T.  The MN-major (feature-contiguous) A variants are only
+    reported: on this part they do not give A @ B^T, which is why no SpMM
+    tile feeds fp32 B rows to kind::tf32 in place."""
     rng = np.random.default_rng(6)
     A = tf32_trunc(rng.standard_normal((128, 8)))
     Bm = tf32_trunc(rng.standard_normal((16, 8)))
     ref = A.astype(np.float64) @ Bm.astype(np.float64).T
     report = {}
-    for desc in [TF32_DESC, (1024, 4096, 2, 256, 128, 0), (2048, 1024, 2, 128, 256, 0)]:
+    for desc in [TF32_DESC, (1024, 2048, 2, 256, 128, 0), (2048, 1024, 2, 128, 256, 0)]:
         D, err = run_probe_tf32(A, Bm, desc)
-        report[desc] = (err, float(np.abs(D - ref).max()))
+        report[("mn", desc)] = (err, float(np.abs(D - ref).max()))
+    for desc in [(128, 256, 0, 128, 256, 0), (256, 128, 0, 128, 256, 0)]:
+        D, err = run_probe_tf32(A, Bm, desc, a_kmajor=True)
+        report[("k", desc)] = (err, float(np.abs(D - ref).max()))
     print("tf32 probe report:", report)
-    err, maxdiff = report[TF32_DESC]
+    err, maxdiff = report[("k", (128, 256, 0, 128, 256, 0))]
     assert err == 0 and maxdiff < 1e-3, report

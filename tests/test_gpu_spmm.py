@@ -6,7 +6,7 @@ import torch
 
 from conftest import golden_files
 from golden_plan import plan_from_fixture
-from gpu_util import random_values, tf32_layout_ok, umma_layout_ok
+from gpu_util import random_values, umma_layout_ok
 import oracle.semantics as S
 from stile_gb300 import device as D
 from stile_gb300.ops import CsrMatrix, DeviceSpmmPlan
@@ -27,15 +27,13 @@ def _needs_tc(plan):
     return any(t.template == "TensorCore_template" for t in plan.tiles)
 
 
-@pytest.mark.parametrize("mode,tol", [(D.TC_BF16, 1e-2), (D.TC_F16, 2e-3), (D.TC_SPLIT_BF16, 1e-5),
-                                      (D.TC_TF32, 2e-3)], ids=["bf16", "f16", "split", "tf32"])
+@pytest.mark.parametrize("mode,tol", [(D.TC_BF16, 1e-2), (D.TC_F16, 2e-3), (D.TC_SPLIT_BF16, 1e-5)],
+                         ids=["bf16", "f16", "split"])
 @pytest.mark.parametrize("path", SPMM_FIXTURES, ids=lambda p: p.split("/")[-1][:-4])
 def test_fused_spmm_matches_fp64(path, mode, tol):
     meta, plan, A = _case(path)
     if _needs_tc(plan) and not umma_layout_ok():
         pytest.fail("tensor-core layout probe failed; fused kernel not run")
-    if _needs_tc(plan) and mode == D.TC_TF32 and not tf32_layout_ok():
-        pytest.fail("tf32 layout probe failed; tf32 kernel not run")
     N = meta["N"]
     dev = D.build_spmm_device(plan.tiles, A, N=N, tc_mode=mode)
     p = DeviceSpmmPlan(dev)
@@ -65,6 +63,27 @@ def test_fused_spmm_ell_only_path_is_fp32_exact(path):
     assert S.rel_fro(C, S.spmm_fp64(A, B)) <= 1e-5
 
 
+@pytest.mark.parametrize("N", [3, 41, 128, 200, 260])
+@pytest.mark.parametrize("name", ["community_1024", "powerlaw_512_ell", "hubblocks_4096"])
+def test_fused_spmm_feature_widths(name, N):
+    """A plan runs at any feature count: N % 4 != 0 takes the register
+    gather path for row tiles, N % 4 == 0 the bulk-copy path; N > 128 spans
+    several 128-feature slices."""
+    path = [p for p in SPMM_FIXTURES if name in p][0]
+    meta, plan, A = _case(path, seed=11)
+    if _needs_tc(plan) and not umma_layout_ok():
+        pytest.fail("tensor-core layout probe failed; fused kernel not run")
+    dev = D.build_spmm_device(plan.tiles, A, N=meta["N"], tc_mode=D.TC_BF16)
+    p = DeviceSpmmPlan(dev)
+    B = np.random.default_rng(N).standard_normal((A.shape[1], N)).astype(np.float32)
+    C = p.run(torch.as_tensor(B, device="cuda")).cpu().numpy()
+    tol = 1e-2 if _needs_tc(plan) else 1e-5
+    assert S.rel_fro(C, S.spmm_fp64(A, B)) <= tol
+    assert p.error_flag() == 0
+    empty = np.diff(A.indptr) == 0
+    assert np.all(C[empty] == 0)
+
+
 @pytest.mark.parametrize("path", SPMM_FIXTURES, ids=lambda p: p.split("/")[-1][:-4])
 def test_dvals_matches_fp64_sddmm(path):
     meta, plan, A = _case(path, seed=4)
@@ -79,11 +98,11 @@ def test_dvals_matches_fp64_sddmm(path):
     assert S.rel_fro(dv, ref) <= 1e-5
 
 
-@pytest.mark.parametrize("mode,tol", [(D.TC_SPLIT_BF16, 1e-5), (D.TC_TF32, 2e-3)], ids=["split", "tf32"])
+@pytest.mark.parametrize("mode,tol", [(D.TC_BF16, 1e-2), (D.TC_SPLIT_BF16, 1e-5)], ids=["bf16", "split"])
 def test_set_values_repacks_in_place(mode, tol):
     path = [p for p in SPMM_FIXTURES if "community_1024" in p][0]
     meta, plan, A = _case(path, seed=5)
-    if not umma_layout_ok() or (mode == D.TC_TF32 and not tf32_layout_ok()):
+    if not umma_layout_ok():
         pytest.fail("tensor-core layout probe failed; fused kernel not run")
     dev = D.build_spmm_device(plan.tiles, A, N=meta["N"], tc_mode=mode)
     p = DeviceSpmmPlan(dev)
