@@ -165,6 +165,26 @@ int stile_csr_spmm_run(int32_t M, int64_t nnz, const int32_t* indptr, const int3
 /* Nonzeros per warp group of the CSR kernel (for building group_rows). */
 int32_t stile_csr_group_nnz(void);
 
+/* Plain CSR SpMM that allocates nothing.  No counterpart in the reference.
+ * For callers that must not allocate device memory: their memory belongs to
+ * another allocator (a host framework's caching pool, an arena handed out up
+ * front), and a cudaMalloc / cudaFree of their own may also synchronise the
+ * device and stall other streams.  Same result as stile_csr_spmm_run with a
+ * group_rows map, but the map is built on the device into a scratch array
+ * compiled into the library: STILE_CSR_NOALLOC_MAX_GROUPS entries (1 MiB),
+ * held by every GPU that loads the library until the process exits, so
+ * nnz <= STILE_CSR_NOALLOC_MAX_GROUPS * stile_csr_group_nnz() (16,777,216);
+ * larger inputs are rejected with STILE_E_INVALID.  The first call on each
+ * device looks up the array's device address (with that device current);
+ * make that first call before any stream capture.  All calls on a device
+ * share the array: every entry a call reads it writes first, but calls that
+ * overlap on the GPU (unordered streams) race on it. */
+#define STILE_CSR_NOALLOC_MAX_GROUPS (1 << 18)
+int stile_csr_spmm_run_noalloc(int32_t M, int64_t nnz, const int32_t* indptr,
+                               const int32_t* indices, const float* vals,
+                               const float* B, int64_t ldb, float* C, int64_t ldc,
+                               int32_t N, void* stream);
+
 /* Refresh the tile values of a plan from vals[nnz] (device, CSR order of the
  * pattern the plan was built for); the pattern and index arrays are kept.
  * Used when A's values change between calls (training the values). */

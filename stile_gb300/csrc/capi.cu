@@ -634,3 +634,8 @@ int stile_debug_umma_probe(const void* a_img, const void* b_img, const uint32_t*
 }
 
 }  // extern "C"
+
+namespace stile {
+int report_error(int code, const char* msg) { return fail(code, msg); }
+void note_launches(int n) { g_launches += n; }
+}  // namespace stile

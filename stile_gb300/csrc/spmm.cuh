@@ -63,6 +63,11 @@ constexpr int kCsrGroupNnz = 64;  // nonzeros per warp group of the CSR kernel
 constexpr int kSegNnz = 64;       // entries per group of the ELL stream kernel
 cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st);
 cudaError_t launch_tc(const SpmmArgs& p, cudaStream_t st);
+// C-ABI bookkeeping shared by the entry points of every translation unit:
+// record `msg` as the calling thread's last error and return `code`; count
+// kernel launches
+int report_error(int code, const char* msg);
+void note_launches(int n);
 // CTAs of the persistent tensor-core kernel resident on the current device
 // (0 on error)
 int tc_persistent_ctas();
