@@ -4,6 +4,7 @@
 #include <climits>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <queue>
 #include <string>
 #include <vector>
@@ -56,6 +57,11 @@ struct StileSpmmPlan {
   long nnz = 0, ell_n_slots = 0;
   int n_zero_rows = 0;
   const int* zero_rows = nullptr;
+  // the ELL kernel runs on `side`, forked from and joined back into the
+  // caller's stream, concurrently with the tensor-core kernel
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  std::mutex run_mu;  // one fork / join sequence at a time
 };
 
 struct StileSddmmPlan {
@@ -221,6 +227,18 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   }
   const long n_pos = (long)e_col.size();
   if (n_pos > INT32_MAX) return fail(STILE_E_INVALID, "too many ELL entries");
+  // packed entries; an entry ends its run when the next one in its group
+  // has another row code (or there is none)
+  std::vector<int32_t> e_ent((size_t)n_pos * 4);
+  for (size_t g = 0; g + 1 < e_gptr.size(); ++g)
+    for (long q = e_gptr[g]; q < e_gptr[g + 1]; ++q) {
+      int32_t vbits;
+      std::memcpy(&vbits, &e_val[q], 4);
+      e_ent[q * 4 + 0] = e_col[q];
+      e_ent[q * 4 + 1] = vbits;
+      e_ent[q * 4 + 2] = e_rc[q];
+      e_ent[q * 4 + 3] = (q + 1 == e_gptr[g + 1] || e_rc[q + 1] != e_rc[q]) ? 1 : 0;
+    }
   std::sort(zero.begin(), zero.end());
   zero.erase(std::unique(zero.begin(), zero.end()), zero.end());
   const long nck = (long)ck_item.size();
@@ -326,9 +344,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   size_t i_tnid = ar.add(s_nnz.data(), s_nnz.size() * 4);
   size_t i_ctac = ar.add(cta_chunk.data(), cta_chunk.size() * 4);
   size_t i_egptr = ar.add(e_gptr.data(), e_gptr.size() * 4);
-  size_t i_ecol = ar.add(e_col.data(), (size_t)n_pos * 4);
-  size_t i_evals = ar.add(e_val.data(), (size_t)n_pos * 4);
-  size_t i_erc = ar.add(e_rc.data(), (size_t)n_pos * 4);
+  size_t i_eent = ar.add(e_ent.data(), e_ent.size() * 4);
   size_t i_enid = ar.add(e_id.data(), e_id.size() * 4);
   size_t i_zero = ar.add(zero.data(), zero.size() * 4);
   size_t i_ckb = ar.add(ck_kbeg.data(), (size_t)nck * 4);
@@ -357,6 +373,15 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
       }
     }
   }
+  if ((e = cudaStreamCreateWithFlags(&plan->side, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&plan->fork, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&plan->join, cudaEventDisableTiming)) != cudaSuccess) {
+    if (plan->fork) cudaEventDestroy(plan->fork);
+    if (plan->side) cudaStreamDestroy(plan->side);
+    cudaFree(plan->arena);
+    delete plan;
+    return cuda_fail(e, "plan stream / events");
+  }
   plan->err_flag = reinterpret_cast<int*>(base + ar.offs[i_err]);
   e = cudaMemset(plan->err_flag, 0, 16);
   if (e != cudaSuccess) {
@@ -379,9 +404,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   a.ell_n_groups = (int)e_gptr.size() - 1;
   a.ell_n_pos = n_pos;
   a.ell_group_ptr = (const int*)P(i_egptr);
-  a.ell_kidx = (const int*)P(i_ecol);
-  a.ell_vals = (const float*)P(i_evals);
-  a.ell_rowcode = (const int*)P(i_erc);
+  a.ell_entry = (const int4*)P(i_eent);
   a.ell_nnz_id = h->ell_nnz_id ? (const int*)P(i_enid) : nullptr;
   a.err_flag = plan->err_flag;
   plan->M = h->M;
@@ -407,6 +430,9 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
 
 int stile_spmm_plan_free(StileSpmmPlan* plan) {
   if (!plan) return STILE_OK;
+  if (plan->fork) cudaEventDestroy(plan->fork);
+  if (plan->join) cudaEventDestroy(plan->join);
+  if (plan->side) cudaStreamDestroy(plan->side);
   cudaError_t e = cudaFree(plan->arena);
   delete plan;
   if (e != cudaSuccess) return cuda_fail(e, "cudaFree(plan)");
@@ -430,9 +456,18 @@ int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float
   if ((rc = check_dense(ldb, N, B, "B")) != 0) return rc;
   if ((rc = check_dense(ldc, N, C, "C")) != 0) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  cudaError_t e = stile::launch_zero_rows(plan->zero_rows, plan->n_zero_rows, C, ldc, N, st);
-  if (e != cudaSuccess) return cuda_fail(e, "zero_rows launch");
-  if (plan->n_zero_rows) g_launches++;
+  cudaError_t e;
+  // rows without an owned writer start at zero; when they are the majority,
+  // one strided memset of C is cheaper than the row list (owned rows are
+  // overwritten by their writer anyway)
+  if (2L * plan->n_zero_rows >= plan->M) {
+    e = cudaMemset2DAsync(C, (size_t)ldc * 4, 0, (size_t)N * 4, (size_t)plan->M, st);
+    if (e != cudaSuccess) return cuda_fail(e, "zeroing C");
+  } else {
+    e = stile::launch_zero_rows(plan->zero_rows, plan->n_zero_rows, C, ldc, N, st);
+    if (e != cudaSuccess) return cuda_fail(e, "zero_rows launch");
+    if (plan->n_zero_rows) g_launches++;
+  }
   stile::SpmmArgs a = plan->args;
   a.B = B;
   a.ldb = ldb;
@@ -440,12 +475,27 @@ int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float
   a.ldc = ldc;
   a.N = N;
   a.n_fchunks = (N + 127) / 128;
+  const bool both = a.tc_n_chunks > 0 && a.ell_n_groups > 0;
+  std::unique_lock<std::mutex> lock(const_cast<StileSpmmPlan*>(plan)->run_mu, std::defer_lock);
+  cudaStream_t ell_st = st;
+  if (both) {
+    // fork: the ELL kernel on the plan's side stream, after the zeroing
+    lock.lock();
+    ell_st = plan->side;
+    if ((e = cudaEventRecord(plan->fork, st)) != cudaSuccess || (e = cudaStreamWaitEvent(ell_st, plan->fork, 0)) != cudaSuccess)
+      return cuda_fail(e, "stream fork");
+  }
+  e = stile::launch_ell(a, ell_st);
+  if (e != cudaSuccess) return cuda_fail(e, "ELL SpMM launch");
+  if (a.ell_n_groups) g_launches++;
   e = stile::launch_tc(a, st);
   if (e != cudaSuccess) return cuda_fail(e, "tensor-core SpMM launch");
   if (a.tc_n_chunks) g_launches++;
-  e = stile::launch_ell(a, st);
-  if (e != cudaSuccess) return cuda_fail(e, "ELL SpMM launch");
-  if (a.ell_n_groups) g_launches++;
+  if (both) {
+    // join: the caller's stream continues once the ELL kernel is done
+    if ((e = cudaEventRecord(plan->join, ell_st)) != cudaSuccess || (e = cudaStreamWaitEvent(st, plan->join, 0)) != cudaSuccess)
+      return cuda_fail(e, "stream join");
+  }
   return STILE_OK;
 }
 

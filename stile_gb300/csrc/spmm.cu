@@ -580,55 +580,67 @@ __global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
   if (warp == 0) tmem_dealloc(tmem, 16 * kAccBufs);
 }
 
-// ELL tiles as a stream of live entries (column, value, row code) in row
-// order.  An LPR-lane sub-group owns one group of <= kSegNnz entries and
-// walks it kSegBatch entries at a time: the batch's column ids, values and
-// row codes are broadcast loads, then kSegBatch B-row gathers are in flight
-// per lane; the running sum is flushed at every change of row code (store
-// for an owned row, atomic add for a row of an atomic tile or a piece of a
-// split row).  Few registers per thread, so 64 warps per SM keep enough
-// gathers in flight to approach the L2 gather rate.
+// ELL tiles as a stream of live entries in row order, packed as 16-byte
+// records {column, value, row code, run end}.  An LPR-lane sub-group owns
+// one group of <= kSegNnz entries.  Its lanes hold the group's records LPR
+// at a time (one per lane, the next LPR loaded while these are consumed),
+// broadcast them by shuffle, keep kSegBatch B-row gathers in flight per lane
+// and flush the running sum after every entry that ends its row's run
+// (store for an owned row, atomic add for a row of an atomic tile or a piece
+// of a split row).  No gather waits on a metadata load, and few registers
+// per thread leave room for many warps per SM.
 constexpr int kSegBatch = 4;
 
-template <int LPR>
-__global__ void __launch_bounds__(256, 6) spmm_ell_seg_kernel(SpmmArgs p) {
+// kVec: N % 4 == 0, so a lane's 4 features are all in range or all out
+template <int LPR, bool kVec>
+__global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
+  const unsigned mask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
   const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
-  if (g >= p.ell_n_groups) return;
+  if (g >= p.ell_n_groups) return;  // the whole sub-group leaves together
   const int p0 = __ldg(p.ell_group_ptr + g);
   const int n = __ldg(p.ell_group_ptr + g + 1) - p0;
-  const int* __restrict__ kidx = p.ell_kidx + p0;
-  const float* __restrict__ vals = p.ell_vals + p0;
-  const int* __restrict__ rcode = p.ell_rowcode + p0;
+  const int4* __restrict__ ent = p.ell_entry + p0;
   const int N = p.N;
+  auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, 0); };
   for (int fc = 0; fc < N; fc += 4 * LPR) {
     const int f = fc + 4 * sl;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    int cur = __ldg(rcode);
+    int4 mcur = rec(sl);
 #pragma unroll 1
-    for (int b0 = 0; b0 < n; b0 += kSegBatch) {
-      float4 bv[kSegBatch];
+    for (int c0 = 0; c0 < n; c0 += LPR) {
+      const int4 mnext = rec(c0 + LPR + sl);
+#pragma unroll 1
+      for (int b0 = c0; b0 < min(n, c0 + LPR); b0 += kSegBatch) {
+        float4 bv[kSegBatch];
 #pragma unroll
-      for (int u = 0; u < kSegBatch; ++u) {
-        const int i = min(b0 + u, n - 1);
-        bv[u] = b0 + u < n ? ld_row4(p.B + (long)__ldg(kidx + i) * p.ldb, f, N) : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
+        for (int u = 0; u < kSegBatch; ++u) {
+          const int c = __shfl_sync(mask, mcur.x, b0 - c0 + u, LPR);
+          if (kVec) bv[u] = (b0 + u < n && f < N) ? ldg4(p.B + (long)c * p.ldb + f) : make_float4(0.f, 0.f, 0.f, 0.f);
+          else bv[u] = b0 + u < n ? ld_row4(p.B + (long)c * p.ldb, f, N) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
 #pragma unroll
-      for (int u = 0; u < kSegBatch; ++u) {
-        if (b0 + u < n) {
-          const int code = __ldg(rcode + b0 + u);
-          if (code != cur) {
-            if (cur >= 0) st_row4(p.C + (long)cur * p.ldc, f, N, acc);
-            else red_row4(p.C + (long)(-cur - 1) * p.ldc, f, N, acc);
+        for (int u = 0; u < kSegBatch; ++u) {
+          const float v = __int_as_float(__shfl_sync(mask, mcur.y, b0 - c0 + u, LPR));
+          const int code = __shfl_sync(mask, mcur.z, b0 - c0 + u, LPR);
+          const int end = __shfl_sync(mask, mcur.w, b0 - c0 + u, LPR);
+          fma4(acc, v, bv[u]);  // records past n are zero: value 0, no run end
+          if (end) {
+            float* row = p.C + (long)(code >= 0 ? code : -code - 1) * p.ldc;
+            if (kVec) {
+              if (f < N) {
+                if (code >= 0) *reinterpret_cast<float4*>(row + f) = acc;
+                else atomicAdd(reinterpret_cast<float4*>(row + f), acc);
+              }
+            } else {
+              if (code >= 0) st_row4(row, f, N, acc); else red_row4(row, f, N, acc);
+            }
             acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            cur = code;
           }
-          fma4(acc, __ldg(vals + b0 + u), bv[u]);
         }
       }
+      mcur = mnext;
     }
-    if (cur >= 0) st_row4(p.C + (long)cur * p.ldc, f, N, acc);
-    else red_row4(p.C + (long)(-cur - 1) * p.ldc, f, N, acc);
   }
 }
 
@@ -641,7 +653,7 @@ __global__ void __launch_bounds__(256, 6) spmm_ell_seg_kernel(SpmmArgs p) {
 // value re-pack: refresh the plan's tile values from a CSR-ordered value
 // array (used when the matrix values change but the pattern does not)
 // ===========================================================================
-__global__ void repack_values_kernel(SpmmArgs p, const float* __restrict__ vals, float* ell_vals,
+__global__ void repack_values_kernel(SpmmArgs p, const float* __restrict__ vals, int4* ell_entry,
                                      uint16_t* tc_img, long n_ell_slots) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long n_tc = (long)p.tc_n_ksteps * 256;
@@ -667,7 +679,7 @@ __global__ void repack_values_kernel(SpmmArgs p, const float* __restrict__ vals,
   } else if (i - n_tc < n_ell_slots) {
     const long s = i - n_tc;
     const int id = p.ell_nnz_id[s];
-    ell_vals[s] = id >= 0 ? vals[id] : 0.f;
+    ell_entry[s].y = __float_as_int(id >= 0 ? vals[id] : 0.f);
   }
 }
 
@@ -676,7 +688,7 @@ cudaError_t launch_repack(const SpmmArgs& p, const float* vals, long n_ell_slots
   if (total == 0) return cudaSuccess;
   const long grid = (total + 255) / 256;
   repack_values_kernel<<<(unsigned)grid, 256, 0, st>>>(
-      p, vals, const_cast<float*>(p.ell_vals),
+      p, vals, const_cast<int4*>(p.ell_entry),
       reinterpret_cast<uint16_t*>(const_cast<void*>(p.tc_vals)), n_ell_slots);
   return cudaGetLastError();
 }
@@ -813,7 +825,8 @@ struct EllLaunch {
     if (p.ell_n_groups == 0) return cudaSuccess;
     const long groups_per_block = 256 / LPR;
     const long grid = (p.ell_n_groups + groups_per_block - 1) / groups_per_block;
-    spmm_ell_seg_kernel<LPR><<<(unsigned)grid, 256, 0, st>>>(p);
+    if (p.N % 4 == 0) spmm_ell_seg_kernel<LPR, true><<<(unsigned)grid, 256, 0, st>>>(p);
+    else spmm_ell_seg_kernel<LPR, false><<<(unsigned)grid, 256, 0, st>>>(p);
     return cudaGetLastError();
   }
 };

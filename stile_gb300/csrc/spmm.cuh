@@ -42,9 +42,9 @@ struct SpmmArgs {
   int ell_n_groups;
   long ell_n_pos;
   const int* ell_group_ptr;  // [ell_n_groups + 1]
-  const int* ell_kidx;       // [ell_n_pos] column of B
-  const float* ell_vals;     // [ell_n_pos]
-  const int* ell_rowcode;    // [ell_n_pos] out row r (store) or -(r + 1) (atomic add)
+  // [ell_n_pos] {column of B, value bits, row code, 1 if the entry ends its
+  // row's run in the group}; row code r stores into C row r, -(r + 1) adds
+  const int4* ell_entry;
   const int* ell_nnz_id;     // [ell_n_pos] nonzero id (or NULL)
   // value-gradient entry list enumerated from the tiles: tensor-core entries
   // (item, row, k-step, column order) then ELL slots (row, slot order)
