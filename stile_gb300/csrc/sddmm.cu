@@ -14,19 +14,27 @@
 namespace stile {
 
 // Entry-list SDDMM: out[outs[t]] = <X[rows[t]], Y[cols[t]]>.  An LPR-lane
-// group takes 8 consecutive entries per iteration (row loads 8 at a time,
-// 128-bit each) and reduces the 8 dot products together with a
-// transposing butterfly: after the three halving steps every lane holds one
-// entry's partial sum, so 8 dots cost 9 shuffles instead of 40.  Entries
-// sorted by row reuse the X row from L1.
-template <int LPR>
-__global__ void __launch_bounds__(256, 2) sddmm_list_kernel(long n, const int* __restrict__ rows,
-                                                            const int* __restrict__ cols,
-                                                            const int* __restrict__ outs,
-                                                            const float* __restrict__ X, long ldx,
-                                                            const float* __restrict__ Y, long ldy,
-                                                            float* __restrict__ out, int F) {
-  constexpr int V = 8;
+// group takes V consecutive entries per iteration: lanes 0..V-1 load the
+// entries' (row, column, output) and broadcast them by shuffle where used;
+// the Y rows are gathered 4 at a time (128-bit per lane) and an X row is
+// gathered only where the row changes from the previous entry (lists
+// grouped by row, as both callers' are, read each X row about once per
+// run).  The V dot products are reduced together with a transposing
+// butterfly: each halving step sends half of the partial sums across and
+// keeps the other half, so after log2(V) steps every lane holds one entry's
+// partial sum (8 dots cost 9 shuffles instead of 40).
+constexpr int kSddmmV = 8;           // entries per group iteration
+constexpr int kSddmmBlocks = 4;      // resident 256-thread blocks per SM (register budget)
+
+// kVec: F % 4 == 0, so a lane's 4 features are all in range or all out
+template <int LPR, int V, bool kVec>
+__global__ void __launch_bounds__(256, kSddmmBlocks) sddmm_list_kernel(long n, const int* __restrict__ rows,
+                                                                     const int* __restrict__ cols,
+                                                                     const int* __restrict__ outs,
+                                                                     const float* __restrict__ X, long ldx,
+                                                                     const float* __restrict__ Y, long ldy,
+                                                                     float* __restrict__ out, int F) {
+  static_assert(V % 4 == 0, "entries are gathered 4 at a time");
   constexpr int GPB = 256 / LPR;
   const int lane = threadIdx.x & 31;
   const int sub = lane / LPR, sl = lane % LPR;
@@ -35,60 +43,70 @@ __global__ void __launch_bounds__(256, 2) sddmm_list_kernel(long n, const int* _
   const long stride = (long)gridDim.x * GPB;
   for (long base = g * V; base < n; base += stride * V) {
     const int cnt = (int)min((long)V, n - base);
-    int r[V], c[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      r[v] = v < cnt ? __ldg(rows + base + v) : 0;
-      c[v] = v < cnt ? __ldg(cols + base + v) : 0;
+    // groups of >= V lanes: lanes 0..V-1 load one entry each; smaller
+    // groups load every entry
+    int rl = 0, cl = 0, ol = 0;
+    if (LPR >= V) {
+      const bool mine = sl < V && sl < cnt;
+      rl = mine ? __ldg(rows + base + sl) : 0;
+      cl = mine ? __ldg(cols + base + sl) : 0;
+      ol = mine ? __ldg(outs + base + sl) : 0;
     }
+    auto row_of = [&](int v) {
+      return LPR >= V ? __shfl_sync(gmask, rl, v, LPR) : (v < cnt ? __ldg(rows + base + v) : 0);
+    };
+    auto col_of = [&](int v) {
+      return LPR >= V ? __shfl_sync(gmask, cl, v, LPR) : (v < cnt ? __ldg(cols + base + v) : 0);
+    };
     float a[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) a[v] = 0.f;
     for (int fc = 0; fc < F; fc += 4 * LPR) {
       const int f = fc + 4 * sl;
-      // two phases of 4 entries: 8 row loads in flight, 8 float4 live
+      auto ld = [&](const float* row) {
+        if (kVec) return f < F ? ldg4(row + f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        return ld_row4(row, f, F);
+      };
+      // phases of 4 entries; xlast carries the previous phase's last X row
+      float4 xlast = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int h = 0; h < V; h += 4) {
         float4 xv[4], yv[4];
 #pragma unroll
+        for (int v = 0; v < 4; ++v) yv[v] = ld(Y + (long)col_of(h + v) * ldy);
+        // X rows: a gather only where the row changes (entry 0 always loads)
+#pragma unroll
         for (int v = 0; v < 4; ++v) {
-          xv[v] = ld_row4(X + (long)r[h + v] * ldx, f, F);
-          yv[v] = ld_row4(Y + (long)c[h + v] * ldy, f, F);
+          const int i = h + v;
+          const int ri = row_of(i);
+          const bool same = i > 0 && ri == row_of(i > 0 ? i - 1 : 0);
+          if (!same) xv[v] = ld(X + (long)ri * ldx);
+          else xv[v] = v > 0 ? xv[v > 0 ? v - 1 : 0] : xlast;
         }
 #pragma unroll
         for (int v = 0; v < 4; ++v) a[h + v] += dot4(xv[v], yv[v]);
+        xlast = xv[3];
       }
     }
-    if (LPR >= 8) {
-      constexpr int h1 = LPR / 2, h2 = LPR / 4, h3 = LPR / 8;
-      {
-        const bool up = (sl & h1) != 0;
+    if (LPR >= V) {
+      // transposing butterfly: entry e ends in the lanes whose bits at the
+      // halving strides spell e
+      int e = 0;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const float send = up ? a[i] : a[i + 4];
-          const float keep = up ? a[i + 4] : a[i];
-          a[i] = keep + __shfl_xor_sync(gmask, send, h1);
+      for (int m = V, hw = LPR / 2; m > 1; m >>= 1, hw >>= 1) {
+        const bool up = (sl & hw) != 0;
+#pragma unroll
+        for (int i = 0; i < m / 2; ++i) {
+          const float send = up ? a[i] : a[i + m / 2];
+          const float keep = up ? a[i + m / 2] : a[i];
+          a[i] = keep + __shfl_xor_sync(gmask, send, hw);
         }
-      }
-      {
-        const bool up = (sl & h2) != 0;
-#pragma unroll
-        for (int i = 0; i < 2; ++i) {
-          const float send = up ? a[i] : a[i + 2];
-          const float keep = up ? a[i + 2] : a[i];
-          a[i] = keep + __shfl_xor_sync(gmask, send, h2);
-        }
-      }
-      {
-        const bool up = (sl & h3) != 0;
-        const float send = up ? a[0] : a[1];
-        const float keep = up ? a[1] : a[0];
-        a[0] = keep + __shfl_xor_sync(gmask, send, h3);
+        if (up) e += m / 2;
       }
 #pragma unroll
-      for (int o = h3 / 2; o > 0; o >>= 1) a[0] += __shfl_xor_sync(gmask, a[0], o);
-      const int e = ((sl & h1) ? 4 : 0) + ((sl & h2) ? 2 : 0) + ((sl & h3) ? 1 : 0);
-      if ((sl & (h3 - 1)) == 0 && e < cnt) out[__ldg(outs + base + e)] = a[0];
+      for (int o = LPR / (2 * V); o > 0; o >>= 1) a[0] += __shfl_xor_sync(gmask, a[0], o);
+      const int oe = __shfl_sync(gmask, ol, e, LPR);
+      if ((sl & (LPR / V - 1)) == 0 && e < cnt) out[oe] = a[0];
     } else {
 #pragma unroll
       for (int v = 0; v < V; ++v) {
@@ -117,14 +135,18 @@ cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const in
   if (n <= 0) return cudaSuccess;
   const int lpr = lpr_for_f(F);
   const int gpb = 256 / lpr;
-  long groups = (n + 7) / 8;
+  long groups = (n + kSddmmV - 1) / kSddmmV;
   long grid = (groups + gpb - 1) / gpb;
   if (grid > 152L * 32) grid = 152L * 32;
+  const bool vec = F % 4 == 0;
+#define STILE_SDDMM_CASE(L)                                                                                   \
+  if (vec) sddmm_list_kernel<L, kSddmmV, true><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F); \
+  else sddmm_list_kernel<L, kSddmmV, false><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F);
   switch (lpr) {
-    case 4: sddmm_list_kernel<4><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F); break;
-    case 8: sddmm_list_kernel<8><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F); break;
-    case 16: sddmm_list_kernel<16><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F); break;
-    default: sddmm_list_kernel<32><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F); break;
+    case 4: STILE_SDDMM_CASE(4) break;
+    case 8: STILE_SDDMM_CASE(8) break;
+    case 16: STILE_SDDMM_CASE(16) break;
+    default: STILE_SDDMM_CASE(32) break;
   }
   return cudaGetLastError();
 }
