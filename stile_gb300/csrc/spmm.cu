@@ -321,13 +321,14 @@ __global__ void __launch_bounds__(kTcThreads) spmm_tc_kernel(SpmmArgs p) {
 // least loaded CTA) and stores every CTA's k-steps contiguously, so a CTA's
 // work is the step range [s_beg, s_beg + S), walked once per 128-feature
 // slice; its units are (slice, chunk) pairs in that order.
-// Roles (warps 0-3 producers, warp 4 lane 0 MMA issuer, warps 5-8 epilogue):
-//  * Column ids: every 32 steps each producer thread loads 4 ids of the
-//    block after next with one 16-byte load and, one block later, stores
-//    them into a two-block shared ring; one producer barrier per block
-//    publishes it.  No copy ever waits on a column-id load.
+// Roles (kProdWarps producer warps, then one warp whose lane 0 issues the
+// MMAs, then four epilogue warps):
+//  * Column ids: every 32 steps each producer thread loads kColPer ids of
+//    the block after next and, one block later, stores them into a
+//    two-block shared ring; one producer barrier per block publishes it.
+//    No copy ever waits on a column-id load.
 //  * Producers: per k-step thread (w, l) copies features 4l..4l+3 of the
-//    step's rows w, w+4, w+8, w+12 (and threads 0-31 the step's 512-byte
+//    step's rows w, w + kProdWarps, ... (and threads 0-31 the step's 512-byte
 //    value image) with cp.async into a kTcStages-deep raw ring, kTcStages-1
 //    steps ahead (commit groups, no register scoreboards).  It converts its
 //    own copies to bf16 / fp16 into operand slot g % 4 and one lane per warp
@@ -349,7 +350,11 @@ constexpr uint32_t kWsSlot = kAStage + 1024;             // A image + value imag
 constexpr int kWsSlots = 4;                              // operand slots between producers and MMA
 constexpr uint32_t kColRing = 2 * kColBlock * 16 * 4;    // 4 KB
 constexpr uint32_t kWsBytes = 1024 + kWsSlots * kWsSlot + kTcStages * kWsRaw + kColRing + 256;
-constexpr int kWsThreads = 288;
+constexpr int kProdWarps = 4;                            // producer warps: 16 / kProdWarps rows each
+constexpr int kRowsPerWarp = 16 / kProdWarps;
+constexpr int kProdThreads = kProdWarps * 32;
+constexpr int kColPer = 16 * kColBlock / kProdThreads;   // column ids per producer thread per block
+constexpr int kWsThreads = (kProdWarps + 1 + 4) * 32;   // producers, MMA warp, 4 epilogue warps
 
 // kFull: every 128-feature slice is complete (N % 128 == 0)
 template <int MODE, bool kFull>
@@ -368,7 +373,7 @@ __global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
 
   if (tid == 0) {
     for (int s = 0; s < kWsSlots; ++s) {
-      mbar_init(full0 + 8 * s, 4);
+      mbar_init(full0 + 8 * s, kProdWarps);
       mbar_init(empty0 + 8 * s, 1);
     }
     for (int b = 0; b < kAccBufs; ++b) {
@@ -400,27 +405,33 @@ __global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
   const int N = p.N;
   bool ok = true;
 
-  if (warp < 4) {
+  if (warp < kProdWarps) {
     // ---------------- producers ----------------
     const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
-    // column-id blocks: thread t carries ids of rows 4(t%4)..+3 of the
-    // block's step t/4
-    int4 cblk = make_int4(0, 0, 0, 0);
+    // column-id blocks: thread t carries kColPer ids (rows
+    // (t % (16 / kColPer)) * kColPer ..) of the block's step t / (16 / kColPer)
+    constexpr int kThrPerStep = 16 / kColPer;
+    const int cstep = tid / kThrPerStep, crow = (tid % kThrPerStep) * kColPer;
+    int cblk[kColPer];
+#pragma unroll
+    for (int i = 0; i < kColPer; ++i) cblk[i] = 0;
     long cblk_g = 0;  // first step of the block held in cblk
     auto col_block_load = [&](long g0b) {
       cblk_g = g0b;
-      const long g = g0b + (tid >> 2);
+      const long g = g0b + cstep;
       if (g < T) {
-        int local = (int)(g % S);
-        cblk = __ldg(reinterpret_cast<const int4*>(p.tc_cols + (long)(s_beg + local) * 16) + (tid & 3));
+        const int local = (int)(g % S);
+#pragma unroll
+        for (int i = 0; i < kColPer; ++i) cblk[i] = __ldg(p.tc_cols + (long)(s_beg + local) * 16 + crow + i);
       }
     };
     auto col_block_store = [&]() {
       const uint32_t half = (uint32_t)((cblk_g / kColBlock) & 1);
-      st_shared_v4(cring + half * (kColBlock * 64) + (uint32_t)(tid >> 2) * 64 + (uint32_t)(tid & 3) * 16,
-                   make_uint4((uint32_t)cblk.x, (uint32_t)cblk.y, (uint32_t)cblk.z, (uint32_t)cblk.w));
+      const uint32_t dst = cring + half * (kColBlock * 64) + (uint32_t)cstep * 64 + (uint32_t)crow * 4;
+#pragma unroll
+      for (int i = 0; i < kColPer; ++i) st_shared_u32(dst + 4 * i, (uint32_t)cblk[i]);
     };
-    auto producer_sync = [&]() { asm volatile("bar.sync 1, 128;" ::: "memory"); };
+    auto producer_sync = [&]() { asm volatile("bar.sync 1, %0;" ::"n"(kProdThreads) : "memory"); };
     // issue cursor: step gi = k-step ks of slice f0
     long gi = 0;
     int iks = s_beg, if0 = 0;
@@ -438,8 +449,8 @@ __global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
         const int f = if0 + 4 * lane;
         const uint32_t bytes = kFull ? 16u : ((f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u));
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int kk = warp + 4 * j;
+        for (int j = 0; j < kRowsPerWarp; ++j) {
+          const int kk = warp + kProdWarps * j;
           uint32_t col;
           asm volatile("ld.shared.u32 %0, [%1];" : "=r"(col) : "r"(crow + 4u * kk));
           const float* row = p.B + (long)col * p.ldb;
@@ -478,8 +489,8 @@ __global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
       const uint32_t sr = ring + (uint32_t)(g % kTcStages) * kWsRaw;
       const uint32_t sa = slots + slot * kWsSlot;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int kk = warp + 4 * j;
+      for (int j = 0; j < kRowsPerWarp; ++j) {
+        const int kk = warp + kProdWarps * j;
         const uint4 raw = ld_shared_v4(sr + kk * 512 + lane * 16);
         const float4 v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y), __uint_as_float(raw.z),
                                      __uint_as_float(raw.w));
@@ -499,7 +510,7 @@ __global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
       for (; gi < T + kTcStages - 1; ++gi)
         if (gi % kColBlock == 0) producer_sync();
     }
-  } else if (warp == 4) {
+  } else if (warp == kProdWarps) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const uint32_t idesc = (MODE == STILE_TC_F16) ? make_idesc(0, 0, 1, 0, 128, 16)
