@@ -167,8 +167,9 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
       for (int r = 0; r < 16; ++r)
         if (h->tc_out_rows[(long)i * 16 + r] >= 0) zero.push_back(h->tc_out_rows[(long)i * 16 + r]);
   }
-  // ELL tiles as a stream of live entries in row order, cut into groups of
-  // at most `cap` entries at row boundaries.  Row code r stores into C row
+  // ELL tiles as a stream of live entries ordered by output row (rows of a
+  // community then sit in neighbouring groups, which share B rows in L1),
+  // cut into groups of at most `cap` entries at row boundaries.  Row code r stores into C row
   // r; -(r + 1) adds atomically (atomic tiles; pieces of rows longer than a
   // group, whose owned rows are zeroed first).  The capacity is the largest
   // of 64, 32, 16 that still gives every warp the device keeps resident
@@ -201,13 +202,27 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
         if (h->ell_nnz_id) e_id.push_back(h->ell_nnz_id[s0 + k]);
       }
     };
+    struct EllRow {
+      int32_t orow, len;
+      long s0;
+      bool atomic;
+    };
+    std::vector<EllRow> erows;
     for (int i = 0; i < h->ell_n_items; ++i) {
       const int K = h->ell_item_K[i];
       const bool atomic = (h->ell_item_flags[i] & 1) != 0;
       for (int r = h->ell_item_row0[i]; r < h->ell_item_row0[i + 1]; ++r) {
         const int orow = h->ell_out_row[r], len = h->ell_row_len[r];
         if (orow < 0 || len <= 0) continue;
-        const long s0 = h->ell_item_slot0[i] + (long)(r - h->ell_item_row0[i]) * K;
+        erows.push_back({orow, len, h->ell_item_slot0[i] + (long)(r - h->ell_item_row0[i]) * K, atomic});
+      }
+    }
+    std::stable_sort(erows.begin(), erows.end(), [](const EllRow& x, const EllRow& y) { return x.orow < y.orow; });
+    for (const EllRow& er : erows) {
+      {
+        const int orow = er.orow, len = er.len;
+        const long s0 = er.s0;
+        const bool atomic = er.atomic;
         if (len > cap) {
           close_group();
           if (!atomic) zero.push_back(orow);
