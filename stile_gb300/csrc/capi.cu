@@ -57,11 +57,6 @@ struct StileSpmmPlan {
   long nnz = 0, ell_n_slots = 0;
   int n_zero_rows = 0;
   const int* zero_rows = nullptr;
-  // the ELL kernel runs on `side`, forked from and joined back into the
-  // caller's stream, concurrently with the tensor-core kernel
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
-  std::mutex run_mu;  // one fork / join sequence at a time
 };
 
 struct StileSddmmPlan {
@@ -242,6 +237,57 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   }
   const long n_pos = (long)e_col.size();
   if (n_pos > INT32_MAX) return fail(STILE_E_INVALID, "too many ELL entries");
+
+  // Write modes, from the actual coverage of every output row.  The ELL
+  // kernel runs first and the tensor-core kernel after it, on one stream.
+  //  * A row whose ELL entries form one run (one group) is stored by the
+  //    ELL kernel: that initialises the row, so it needs no zeroing.
+  //  * A row with several ELL runs (split across groups) is zeroed and all
+  //    its ELL runs add atomically.
+  //  * A tensor-core chunk adds atomically when one of its rows has an ELL
+  //    run or another tensor-core writer; it stores otherwise.  Rows of an
+  //    atomic chunk without an ELL run are zeroed.
+  //  * Rows nobody writes are zeroed.
+  {
+    auto row_of_code = [](int32_t c) { return c >= 0 ? c : -c - 1; };
+    std::vector<int32_t> ell_runs(h->M, 0), tc_writers(h->M, 0);
+    for (size_t g = 0; g + 1 < e_gptr.size(); ++g)
+      for (long q = e_gptr[g]; q < e_gptr[g + 1]; ++q) {
+        const int32_t r = row_of_code(e_rc[q]);
+        if (q == e_gptr[g] || row_of_code(e_rc[q - 1]) != r) ++ell_runs[r];
+      }
+    for (size_t c = 0; c < ck_item.size(); ++c)
+      for (int i = 0; i < 16; ++i) {
+        const int32_t r = h->tc_out_rows[(long)ck_item[c] * 16 + i];
+        if (r >= 0) ++tc_writers[r];
+      }
+    for (long q = 0; q < n_pos; ++q) {
+      const int32_t r = row_of_code(e_rc[q]);
+      e_rc[q] = ell_runs[r] == 1 ? r : -(r + 1);
+    }
+    std::vector<char> needs_zero(h->M, 0);
+    for (size_t c = 0; c < ck_item.size(); ++c) {
+      bool atomic = false;
+      for (int i = 0; i < 16; ++i) {
+        const int32_t r = h->tc_out_rows[(long)ck_item[c] * 16 + i];
+        if (r >= 0 && (ell_runs[r] > 0 || tc_writers[r] > 1)) atomic = true;
+      }
+      ck_flags[c] = atomic ? 1 : 0;
+      if (atomic)
+        for (int i = 0; i < 16; ++i) {
+          const int32_t r = h->tc_out_rows[(long)ck_item[c] * 16 + i];
+          if (r >= 0 && ell_runs[r] == 0) needs_zero[r] = 1;
+        }
+    }
+    for (int r = 0; r < h->M; ++r)
+      if (ell_runs[r] > 1 || (ell_runs[r] == 0 && tc_writers[r] == 0)) needs_zero[r] = 1;
+    // this list replaces the caller's zero rows and the ones noted while
+    // splitting: every row that needs zeroing is found above
+    zero.clear();
+    for (int r = 0; r < h->M; ++r)
+      if (needs_zero[r]) zero.push_back(r);
+  }
+
   // packed entries; an entry ends its run when the next one in its group
   // has another row code (or there is none)
   std::vector<int32_t> e_ent((size_t)n_pos * 4);
@@ -388,15 +434,6 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
       }
     }
   }
-  if ((e = cudaStreamCreateWithFlags(&plan->side, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&plan->fork, cudaEventDisableTiming)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&plan->join, cudaEventDisableTiming)) != cudaSuccess) {
-    if (plan->fork) cudaEventDestroy(plan->fork);
-    if (plan->side) cudaStreamDestroy(plan->side);
-    cudaFree(plan->arena);
-    delete plan;
-    return cuda_fail(e, "plan stream / events");
-  }
   plan->err_flag = reinterpret_cast<int*>(base + ar.offs[i_err]);
   e = cudaMemset(plan->err_flag, 0, 16);
   if (e != cudaSuccess) {
@@ -445,9 +482,6 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
 
 int stile_spmm_plan_free(StileSpmmPlan* plan) {
   if (!plan) return STILE_OK;
-  if (plan->fork) cudaEventDestroy(plan->fork);
-  if (plan->join) cudaEventDestroy(plan->join);
-  if (plan->side) cudaStreamDestroy(plan->side);
   cudaError_t e = cudaFree(plan->arena);
   delete plan;
   if (e != cudaSuccess) return cuda_fail(e, "cudaFree(plan)");
@@ -490,27 +524,14 @@ int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float
   a.ldc = ldc;
   a.N = N;
   a.n_fchunks = (N + 127) / 128;
-  const bool both = a.tc_n_chunks > 0 && a.ell_n_groups > 0;
-  std::unique_lock<std::mutex> lock(const_cast<StileSpmmPlan*>(plan)->run_mu, std::defer_lock);
-  cudaStream_t ell_st = st;
-  if (both) {
-    // fork: the ELL kernel on the plan's side stream, after the zeroing
-    lock.lock();
-    ell_st = plan->side;
-    if ((e = cudaEventRecord(plan->fork, st)) != cudaSuccess || (e = cudaStreamWaitEvent(ell_st, plan->fork, 0)) != cudaSuccess)
-      return cuda_fail(e, "stream fork");
-  }
-  e = stile::launch_ell(a, ell_st);
+  // the ELL kernel initialises the rows it stores; the tensor-core kernel
+  // adds to them afterwards (write modes chosen at upload)
+  e = stile::launch_ell(a, st);
   if (e != cudaSuccess) return cuda_fail(e, "ELL SpMM launch");
   if (a.ell_n_groups) g_launches++;
   e = stile::launch_tc(a, st);
   if (e != cudaSuccess) return cuda_fail(e, "tensor-core SpMM launch");
   if (a.tc_n_chunks) g_launches++;
-  if (both) {
-    // join: the caller's stream continues once the ELL kernel is done
-    if ((e = cudaEventRecord(plan->join, ell_st)) != cudaSuccess || (e = cudaStreamWaitEvent(st, plan->join, 0)) != cudaSuccess)
-      return cuda_fail(e, "stream join");
-  }
   return STILE_OK;
 }
 
