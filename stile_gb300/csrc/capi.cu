@@ -297,8 +297,9 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
       std::memcpy(&vbits, &e_val[q], 4);
       e_ent[q * 4 + 0] = e_col[q];
       e_ent[q * 4 + 1] = vbits;
-      e_ent[q * 4 + 2] = e_rc[q];
-      e_ent[q * 4 + 3] = (q + 1 == e_gptr[g + 1] || e_rc[q + 1] != e_rc[q]) ? 1 : 0;
+      const int32_t end = (q + 1 == e_gptr[g + 1] || e_rc[q + 1] != e_rc[q]) ? 1 : 0;
+      e_ent[q * 4 + 2] = e_rc[q] * 2 + end;  // row code and run end in one field
+      e_ent[q * 4 + 3] = 0;
     }
   std::sort(zero.begin(), zero.end());
   zero.erase(std::unique(zero.begin(), zero.end()), zero.end());
@@ -444,6 +445,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   auto P = [&](size_t idx) { return (const void*)(base + ar.offs[idx]); };
   stile::SpmmArgs& a = plan->args;
   a.tc_mode = mode;
+  a.K = h->K;
   a.tc_n_items = h->tc_n_items;
   a.tc_n_ksteps = h->tc_n_ksteps;
   a.tc_item_kbeg = (const int*)P(i_kbeg);

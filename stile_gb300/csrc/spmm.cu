@@ -592,21 +592,22 @@ __global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
 }
 
 // ELL tiles as a stream of live entries in row order, packed as 16-byte
-// records {column, value, row code, run end}.  An LPR-lane sub-group owns
-// one group of <= kSegNnz entries; each lane covers 4 * VEC features of a
-// row.  The sub-group holds the group's records LPR at a time (one per
-// lane, the next LPR loaded while these are consumed), broadcasts them by
-// shuffle, keeps 4 float4 B-row gathers in flight per lane and flushes the
-// running sum after every entry that ends its row's run (store for an owned
-// row, atomic add for a row of an atomic tile or a piece of a split row).
-// With VEC = 2 two sub-groups share every warp-wide shuffle and branch, so
-// the instructions per gathered byte halve; no gather waits on a metadata
-// load, and few registers leave room for many warps per SM.
-// kVec: N % 4 == 0, so a float4 of features is all in range or all out.
-template <int LPR, int VEC, bool kVec>
+// records {column, value, 2 * row code + run end, 0}.  An LPR-lane
+// sub-group owns one group of <= kSegNnz entries; each lane covers 4 * VEC
+// features of a row.  The sub-group holds the group's records LPR at a time
+// (one per lane, the next LPR loaded while these are consumed), broadcasts
+// them by shuffle, keeps 4 float4 B-row gathers in flight per lane and
+// flushes the running sum after every entry that ends its row's run (store
+// for a row the ELL kernel initialises, atomic add otherwise).  With
+// VEC = 2 two sub-groups share every warp-wide shuffle and branch, so the
+// instructions per gathered byte halve; no gather waits on a metadata load,
+// and few registers leave room for many warps per SM.
+// kFull: N % (4 * VEC * LPR) == 0, every lane's features are in range.
+// kOff32: every B row offset col * ldb fits in 32 bits.
+template <int LPR, int VEC, bool kFull, bool kOff32>
 __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   constexpr int kBatch = 4 / VEC;  // entries per batch: 4 float4 in flight per lane
-  static_assert(VEC == 1 || kVec, "wide lanes need N % 4 == 0");
+  static_assert(VEC == 1 || kFull, "wide lanes need full feature slices");
   const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
   const unsigned mask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
   const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
@@ -615,9 +616,11 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   const int n = __ldg(p.ell_group_ptr + g + 1) - p0;
   const int4* __restrict__ ent = p.ell_entry + p0;
   const int N = p.N;
+  const int ldb32 = (int)p.ldb;
   auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, 0); };
   for (int fc = 0; fc < N; fc += 4 * VEC * LPR) {
     const int f = fc + 4 * VEC * sl;
+    const float* Bf = p.B + f;
     float4 acc[VEC];
 #pragma unroll
     for (int w = 0; w < VEC; ++w) acc[w] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -631,31 +634,30 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
 #pragma unroll
         for (int u = 0; u < kBatch; ++u) {
           const int c = __shfl_sync(mask, mcur.x, b0 - c0 + u, LPR);
-          const float* row = p.B + (long)c * p.ldb;
+          // records past n hold column 0: a valid row, multiplied by 0
+          if (kFull) {
+            const float* row = kOff32 ? Bf + (unsigned)(c * ldb32) : Bf + (long)c * p.ldb;
 #pragma unroll
-          for (int w = 0; w < VEC; ++w) {
-            const int fw = f + 4 * w;
-            if (kVec) bv[u][w] = (b0 + u < n && fw < N) ? ldg4(row + fw) : make_float4(0.f, 0.f, 0.f, 0.f);
-            else bv[u][w] = b0 + u < n ? ld_row4(row, fw, N) : make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int w = 0; w < VEC; ++w) bv[u][w] = ldg4(row + 4 * w);
+          } else {
+            bv[u][0] = b0 + u < n ? ld_row4(p.B + (long)c * p.ldb, f, N) : make_float4(0.f, 0.f, 0.f, 0.f);
           }
         }
 #pragma unroll
         for (int u = 0; u < kBatch; ++u) {
           const float v = __int_as_float(__shfl_sync(mask, mcur.y, b0 - c0 + u, LPR));
-          const int code = __shfl_sync(mask, mcur.z, b0 - c0 + u, LPR);
-          const int end = __shfl_sync(mask, mcur.w, b0 - c0 + u, LPR);
+          const int ce = __shfl_sync(mask, mcur.z, b0 - c0 + u, LPR);
 #pragma unroll
           for (int w = 0; w < VEC; ++w) fma4(acc[w], v, bv[u][w]);  // records past n: value 0, no run end
-          if (end) {
+          if (ce & 1) {
+            const int code = ce >> 1;
             float* row = p.C + (long)(code >= 0 ? code : -code - 1) * p.ldc;
 #pragma unroll
             for (int w = 0; w < VEC; ++w) {
               const int fw = f + 4 * w;
-              if (kVec) {
-                if (fw < N) {
-                  if (code >= 0) *reinterpret_cast<float4*>(row + fw) = acc[w];
-                  else atomicAdd(reinterpret_cast<float4*>(row + fw), acc[w]);
-                }
+              if (kFull) {
+                if (code >= 0) *reinterpret_cast<float4*>(row + fw) = acc[w];
+                else atomicAdd(reinterpret_cast<float4*>(row + fw), acc[w]);
               } else {
                 if (code >= 0) st_row4(row, fw, N, acc[w]); else red_row4(row, fw, N, acc[w]);
               }
@@ -850,18 +852,19 @@ struct EllLaunch {
     if (p.ell_n_groups == 0) return cudaSuccess;
     const long groups_per_block = 256 / LPR;
     const long grid = (p.ell_n_groups + groups_per_block - 1) / groups_per_block;
-    if (p.N % 4 == 0) spmm_ell_seg_kernel<LPR, 1, true><<<(unsigned)grid, 256, 0, st>>>(p);
-    else spmm_ell_seg_kernel<LPR, 1, false><<<(unsigned)grid, 256, 0, st>>>(p);
+    spmm_ell_seg_kernel<LPR, 1, false, false><<<(unsigned)grid, 256, 0, st>>>(p);
     return cudaGetLastError();
   }
 };
 
 cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st) {
   if (p.ell_n_groups == 0) return cudaSuccess;
-  if (p.N % 4 == 0 && p.N >= 128) {
+  if (p.N % 128 == 0) {
     // 16-lane sub-groups of 8 features per lane (two groups per warp)
     const long grid = (p.ell_n_groups + 15) / 16;
-    spmm_ell_seg_kernel<16, 2, true><<<(unsigned)grid, 256, 0, st>>>(p);
+    const bool off32 = (long)p.K * p.ldb < (1L << 31);
+    if (off32) spmm_ell_seg_kernel<16, 2, true, true><<<(unsigned)grid, 256, 0, st>>>(p);
+    else spmm_ell_seg_kernel<16, 2, true, false><<<(unsigned)grid, 256, 0, st>>>(p);
     return cudaGetLastError();
   }
   return dispatch_lpr<EllLaunch>(lpr_for(p.N), p, st);

@@ -15,6 +15,7 @@ struct SpmmArgs {
   float* C;
   long ldc;
   int N;
+  int K;          // rows of B
   int n_fchunks;  // ceil(N / 128): tensor-core feature chunks
   int tc_mode;
   // tensor-core work chunks (items split into runs of <= kChunkSteps k-steps)
@@ -42,8 +43,9 @@ struct SpmmArgs {
   int ell_n_groups;
   long ell_n_pos;
   const int* ell_group_ptr;  // [ell_n_groups + 1]
-  // [ell_n_pos] {column of B, value bits, row code, 1 if the entry ends its
-  // row's run in the group}; row code r stores into C row r, -(r + 1) adds
+  // [ell_n_pos] {column of B, value bits, 2 * row code + run end, 0}; row
+  // code r stores into C row r, -(r + 1) adds; run end is 1 when the entry
+  // ends its row's run in the group
   const int4* ell_entry;
   const int* ell_nnz_id;     // [ell_n_pos] nonzero id (or NULL)
   // value-gradient entry list enumerated from the tiles: tensor-core entries
