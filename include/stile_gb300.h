@@ -165,6 +165,23 @@ int stile_csr_spmm_run(int32_t M, int64_t nnz, const int32_t* indptr, const int3
 /* Nonzeros per warp group of the CSR kernel (for building group_rows). */
 int32_t stile_csr_group_nnz(void);
 
+/* Learned tile cost model (replaces get_MLP_pred / PyTorchMLP,
+ * my_cost_model.py:1010-1093, and its trainer MLP_train_cost_model.py:81-204):
+ * a STILE_MLP_FEATURES -> 64 -> 32 -> 1 ReLU network over standardised tile
+ * features, STILE_MLP_PARAMS floats laid out W1[F][64], b1[64], W2[64][32],
+ * b2[32], W3[32], b3.  All pointers are device pointers.
+ * stile_mlp_forward: y[n] = net(x[n][F]), every candidate in one launch.
+ * stile_mlp_gradient: loss = sum (y - t)^2 / n and grad[STILE_MLP_PARAMS];
+ *   work holds n * 192 floats, dy n floats (scratch of the caller).
+ * stile_mlp_adam: one Adam step (bias-corrected, step >= 1). */
+#define STILE_MLP_FEATURES 12
+#define STILE_MLP_PARAMS 2945
+int stile_mlp_forward(const float* params, const float* x, int64_t n, float* y, void* stream);
+int stile_mlp_gradient(const float* params, const float* x, const float* t, int64_t n,
+                       float* work, float* dy, float* grad, float* loss, void* stream);
+int stile_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t count,
+                   float lr, float beta1, float beta2, float eps, int32_t step, void* stream);
+
 /* Plain CSR SpMM that allocates nothing.  No counterpart in the reference.
  * For callers that must not allocate device memory: their memory belongs to
  * another allocator (a host framework's caching pool, an arena handed out up

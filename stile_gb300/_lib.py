@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD, "libstile_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["spmm.cu", "sddmm.cu", "probe.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["spmm.cu", "sddmm.cu", "probe.cu", "capi.cu", "noalloc.cu", "mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -118,6 +118,14 @@ EXPORTS = {
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                           ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),
     "stile_csr_group_nnz": (ctypes.c_int32, []),
+    "stile_mlp_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                         ctypes.c_void_p]),
+    "stile_mlp_gradient": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
+    "stile_mlp_adam": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float, ctypes.c_int32, ctypes.c_void_p]),
     "stile_csr_spmm_run_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                                   ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),

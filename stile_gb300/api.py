@@ -38,9 +38,16 @@ class PlanConfig:
     tc_mode: int = D.TC_BF16
     single_level: bool = False
     max_level_num: float = float("inf")
+    # score ELL tiles with the learned model (gb300_mlp_cost_model.json)
+    # instead of the analytic fit; needs the GPU for the inference kernel
+    learned: bool = False
 
     def search_kwargs(self):
-        return dict(cost=self.cost_model, max_bucket_size=self.max_bucket_size, only_TC=self.only_TC,
+        cost = self.cost_model
+        if self.learned:
+            from .cost_model import gb300_mlp_model
+            cost = cost.with_mlp(gb300_mlp_model())
+        return dict(cost=cost, max_bucket_size=self.max_bucket_size, only_TC=self.only_TC,
                     only_ELL=self.only_ELL, max_avg_cost_diff=self.max_avg_cost_diff,
                     single_level=self.single_level, max_level_num=self.max_level_num)
 

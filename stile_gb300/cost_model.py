@@ -105,8 +105,18 @@ class CostModel:
         c = self.one_d_costs(rows, cols, F, max_bucket_size) / nnzs / F
         return float(np.min(c))
 
+    def with_mlp(self, mlp):
+        """A copy that scores ELL tiles with the learned model `mlp`
+        (stile_gb300.mlp_cost.MlpCostModel); TC and 1D tiles keep the tables
+        and fits."""
+        m = CostModel.from_json(self.to_json())
+        m.mlp = mlp
+        m.name = f"{self.name}+{mlp.name}"
+        return m
+
     def to_json(self):
         d = dict(self.__dict__)
+        d.pop("mlp", None)
         d["tc_owned"] = {str(k): v for k, v in self.tc_owned.items()}
         d["tc_atomic"] = {str(k): v for k, v in self.tc_atomic.items()}
         d["tc_sddmm"] = {f"{k[0]},{k[1]}": v for k, v in self.tc_sddmm.items()}
@@ -170,3 +180,15 @@ def gb300_model():
     m.name = "a100_fp16_reference_sm152"
     m.sm_num = 152
     return m
+
+
+GB300_MLP = os.path.join(os.path.dirname(os.path.abspath(__file__)), "gb300_mlp_cost_model.json")
+
+
+def gb300_mlp_model():
+    """The learned ELL-tile model trained on GB300 timings (calibrate_mlp.py)."""
+    from .mlp_cost import MlpCostModel
+    if not os.path.exists(GB300_MLP):
+        raise FileNotFoundError(f"no trained model at {GB300_MLP}: run python -m stile_gb300.calibrate_mlp")
+    with open(GB300_MLP) as f:
+        return MlpCostModel.from_json(f.read())

@@ -501,7 +501,16 @@ class SpmmPlanner:
                     if len(pos_is) == 0:
                         entry.append((pos_is, atomic, nn, np.array([])))
                         continue
-                    costs = self.cost.ell_costs(I, J, K, op.k_is(I, K, pos_is), atomic)
+                    k_is = op.k_is(I, K, pos_is)
+                    mlp = getattr(self.cost, "mlp", None)
+                    if mlp is not None:
+                        # learned model: every candidate of this shape in one
+                        # inference launch, from the uncovered row counts
+                        rows = I * pos_is[:, None] + np.arange(I)[None, :]
+                        rn = np.where(rows < len(upd), upd[np.minimum(rows, len(upd) - 1)], 0)
+                        costs = mlp.ell_costs(I, K, rn, k_is, self.N, atomic)
+                    else:
+                        costs = self.cost.ell_costs(I, J, K, k_is, atomic)
                     entry.append((pos_is, atomic, nn, costs))
                     with np.errstate(divide="ignore", invalid="ignore"):
                         avg = costs / nn
