@@ -441,6 +441,39 @@ def run_gpu(args):
     h2d = hB.numel() * 4 + hdC.numel() * 4
     d2h = hC.numel() * 4 + hdv.numel() * 4 + hdB.numel() * 4
 
+    # the learned cost model: its plan's measured forward time judges it
+    learned = None
+    try:
+        t0 = time.time()
+        op_l = SpmmOperator(A, N_FEAT, PlanConfig(tc_mode=tc_mode, learned=True))
+        t_l = time.time() - t0
+        Cl = torch.empty_like(C)
+
+        def fwd_learned():
+            op_l(B, out=Cl)
+
+        def fwd_analytic():
+            op(B, out=C)
+
+        for _ in range(3):
+            fwd_learned()
+            fwd_analytic()
+        tl, _ = timed(fwd_learned, max(args.steps, 5))
+        ta, _ = timed(fwd_analytic, max(args.steps, 5))
+        meta = op_l.plan.meta
+        from stile_gb300.cost_model import gb300_mlp_model
+        mm = gb300_mlp_model().meta
+        learned = {"plan_forward_ms": float(np.median(tl)), "analytic_plan_forward_ms": float(np.median(ta)),
+                   "plan": {f"{k[0]}{'/atomic' if k[1] else ''}": v for k, v in op_l.plan.summary().items()},
+                   "plan_search_s": round(t_l, 2), "cost_model": meta.get("cost_model"),
+                   "held_out_mean_abs_log_err": {k: {"mlp": v["test_mean_abs_log_err_mlp"],
+                                                     "analytic": v["test_mean_abs_log_err_analytic"]}
+                                                 for k, v in mm.items()},
+                   "C_rel_fro": S.rel_fro(Cl.cpu().numpy(), S.spmm_fp64(A, B_np))}
+        op_l.handle.close()
+    except FileNotFoundError as exc:
+        learned = {"unavailable": str(exc)}
+
     cpu = run_cpu_baseline(A, B_np, dC_np, flops) if (rank == 0 and world == 1) else None
 
     if rank == 0:
@@ -471,6 +504,7 @@ def run_gpu(args):
             "csr_baseline": {"value": plain_value, "unit": "GFLOP/s", "ms_per_step": plain_ms,
                              "speedup_hybrid_over_csr": value / plain_value},
             "accuracy": acc,
+            "learned_cost_model": learned,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
