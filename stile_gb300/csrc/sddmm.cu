@@ -26,8 +26,10 @@ namespace stile {
 constexpr int kSddmmV = 8;           // entries per group iteration
 constexpr int kSddmmBlocks = 4;      // resident 256-thread blocks per SM (register budget)
 
-// kVec: F % 4 == 0, so a lane's 4 features are all in range or all out
-template <int LPR, int V, bool kVec>
+// kVec: F % 4 == 0, so a lane's float4 of features is all in range or all
+// out.  VEC float4 per lane: with VEC = 2 (16-lane groups for F >= 128) two
+// groups share every warp-wide shuffle, halving the instructions per byte.
+template <int LPR, int V, bool kVec, int VEC = 1>
 __global__ void __launch_bounds__(256, kSddmmBlocks) sddmm_list_kernel(long n, const int* __restrict__ rows,
                                                                      const int* __restrict__ cols,
                                                                      const int* __restrict__ outs,
@@ -35,6 +37,8 @@ __global__ void __launch_bounds__(256, kSddmmBlocks) sddmm_list_kernel(long n, c
                                                                      const float* __restrict__ Y, long ldy,
                                                                      float* __restrict__ out, int F) {
   static_assert(V % 4 == 0, "entries are gathered 4 at a time");
+  static_assert(VEC == 1 || kVec, "wide lanes need F % 4 == 0");
+  constexpr int kPh = 4 / VEC;  // entries per gather phase: 8 float4 loads in flight per lane
   constexpr int GPB = 256 / LPR;
   const int lane = threadIdx.x & 31;
   const int sub = lane / LPR, sl = lane % LPR;
@@ -61,31 +65,45 @@ __global__ void __launch_bounds__(256, kSddmmBlocks) sddmm_list_kernel(long n, c
     float a[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) a[v] = 0.f;
-    for (int fc = 0; fc < F; fc += 4 * LPR) {
-      const int f = fc + 4 * sl;
-      auto ld = [&](const float* row) {
-        if (kVec) return f < F ? ldg4(row + f) : make_float4(0.f, 0.f, 0.f, 0.f);
-        return ld_row4(row, f, F);
+    for (int fc = 0; fc < F; fc += 4 * VEC * LPR) {
+      const int f = fc + 4 * VEC * sl;
+      auto ld = [&](const float* row, int w) {
+        const int fw = f + 4 * w;
+        if (kVec) return fw < F ? ldg4(row + fw) : make_float4(0.f, 0.f, 0.f, 0.f);
+        return ld_row4(row, fw, F);
       };
-      // phases of 4 entries; xlast carries the previous phase's last X row
-      float4 xlast = make_float4(0.f, 0.f, 0.f, 0.f);
+      // phases of kPh entries; xlast carries the previous phase's last X row
+      float4 xlast[VEC];
 #pragma unroll
-      for (int h = 0; h < V; h += 4) {
-        float4 xv[4], yv[4];
+      for (int w = 0; w < VEC; ++w) xlast[w] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) yv[v] = ld(Y + (long)col_of(h + v) * ldy);
+      for (int h = 0; h < V; h += kPh) {
+        float4 xv[kPh][VEC], yv[kPh][VEC];
+#pragma unroll
+        for (int v = 0; v < kPh; ++v) {
+          const float* yr = Y + (long)col_of(h + v) * ldy;
+#pragma unroll
+          for (int w = 0; w < VEC; ++w) yv[v][w] = ld(yr, w);
+        }
         // X rows: a gather only where the row changes (entry 0 always loads)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
+        for (int v = 0; v < kPh; ++v) {
           const int i = h + v;
           const int ri = row_of(i);
           const bool same = i > 0 && ri == row_of(i > 0 ? i - 1 : 0);
-          if (!same) xv[v] = ld(X + (long)ri * ldx);
-          else xv[v] = v > 0 ? xv[v > 0 ? v - 1 : 0] : xlast;
+#pragma unroll
+          for (int w = 0; w < VEC; ++w) {
+            if (!same) xv[v][w] = ld(X + (long)ri * ldx, w);
+            else xv[v][w] = v > 0 ? xv[v > 0 ? v - 1 : 0][w] : xlast[w];
+          }
         }
 #pragma unroll
-        for (int v = 0; v < 4; ++v) a[h + v] += dot4(xv[v], yv[v]);
-        xlast = xv[3];
+        for (int v = 0; v < kPh; ++v) {
+#pragma unroll
+          for (int w = 0; w < VEC; ++w) a[h + v] += dot4(xv[v][w], yv[v][w]);
+        }
+#pragma unroll
+        for (int w = 0; w < VEC; ++w) xlast[w] = xv[kPh - 1][w];
       }
     }
     if (LPR >= V) {
@@ -138,6 +156,14 @@ cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const in
   long groups = (n + kSddmmV - 1) / kSddmmV;
   long grid = (groups + gpb - 1) / gpb;
   if (grid > 152L * 32) grid = 152L * 32;
+  if (F % 128 == 0) {
+    // 16-lane groups of 8 features per lane (two groups per warp)
+    long groups2 = (n + kSddmmV - 1) / kSddmmV;
+    long grid2 = (groups2 + 15) / 16;
+    if (grid2 > 152L * 32) grid2 = 152L * 32;
+    sddmm_list_kernel<16, kSddmmV, true, 2><<<(unsigned)grid2, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F);
+    return cudaGetLastError();
+  }
   const bool vec = F % 4 == 0;
 #define STILE_SDDMM_CASE(L)                                                                                   \
   if (vec) sddmm_list_kernel<L, kSddmmV, true><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F); \

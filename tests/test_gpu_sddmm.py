@@ -12,7 +12,7 @@ from stile_gb300.ops import DeviceSddmmPlan
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("F", [32, 64, 41, 128])
+@pytest.mark.parametrize("F", [32, 64, 41, 128, 256, 200])
 @pytest.mark.parametrize("path", golden_files("sddmm"), ids=lambda p: p.split("/")[-1][:-4])
 def test_sddmm_matches_fp64(path, F):
     meta, arr = S.load_fixture(path)
