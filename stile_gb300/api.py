@@ -12,7 +12,6 @@ nonzero of A, computed by walking the forward plan's own tiles.
 """
 from __future__ import annotations
 
-import hashlib
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -23,6 +22,7 @@ from . import device as D
 from .cost_model import A100_FP16, CostModel, gb300_model
 from .ops import DeviceSddmmPlan, DeviceSpmmPlan
 from .plan import Plan
+from .plan_io import PlanCache, pattern_key  # noqa: F401  (pattern_key is public here too)
 from .planner import estimate_max_bucket_size, search_sddmm, search_spmm
 
 
@@ -41,6 +41,9 @@ class PlanConfig:
     # score ELL tiles with the learned model (gb300_mlp_cost_model.json)
     # instead of the analytic fit; needs the GPU for the inference kernel
     learned: bool = False
+    # directory of the on-disk plan cache (plan_io.PlanCache); None: search
+    # every time
+    cache_dir: str | None = None
 
     def search_kwargs(self):
         cost = self.cost_model
@@ -52,22 +55,19 @@ class PlanConfig:
                     single_level=self.single_level, max_level_num=self.max_level_num)
 
 
-def pattern_key(A) -> str:
-    """Hash of a sparsity pattern (shape + CSR structure)."""
-    A = sp.csr_matrix(A)
-    A.sort_indices()
-    h = hashlib.sha1()
-    h.update(np.asarray(A.shape, dtype=np.int64).tobytes())
-    h.update(A.indptr.astype(np.int64).tobytes())
-    h.update(A.indices.astype(np.int64).tobytes())
-    return h.hexdigest()
-
-
 def _csr(A):
     A = sp.csr_matrix(A, dtype=np.float64)
     A.sum_duplicates()
     A.sort_indices()
     return A
+
+
+def _find_plan(op_type, A, width, kw, cfg, search):
+    """(plan, "search" | "cache"): from the plan cache when the config names
+    one, else from a fresh search."""
+    if cfg.cache_dir is None:
+        return search(), "search"
+    return PlanCache(cfg.cache_dir).get_or_search(op_type, A, width, kw, search)
 
 
 class SpmmOperator:
@@ -79,8 +79,11 @@ class SpmmOperator:
         self.N = int(N)
         self.shape = self.A.shape
         self.nnz = self.A.nnz
+        self.plan_source = "given"
         if plan is None:
-            plan = search_spmm(self.A, self.N, **self.cfg.search_kwargs())
+            kw = self.cfg.search_kwargs()
+            plan, self.plan_source = _find_plan("spmm", self.A, self.N, kw, self.cfg,
+                                                lambda: search_spmm(self.A, self.N, **kw))
         self.plan = plan
         self.device_layout = D.build_spmm_device(plan.tiles, self.A, N=self.N, tc_mode=self.cfg.tc_mode)
         self.handle = DeviceSpmmPlan(self.device_layout)
@@ -128,10 +131,12 @@ class SddmmOperator:
         self.F = int(F)
         self.shape = self.A.shape
         self.nnz = self.A.nnz
+        self.plan_source = "given"
         if plan is None:
             kw = self.cfg.search_kwargs()
             kw["max_bucket_size"] = kw["max_bucket_size"] or 32
-            plan = search_sddmm(self.A, self.F, **kw)
+            plan, self.plan_source = _find_plan("sddmm", self.A, self.F, kw, self.cfg,
+                                                lambda: search_sddmm(self.A, self.F, **kw))
         self.plan = plan
         self.device_layout = D.build_sddmm_device(plan.tiles, self.shape, self.nnz)
         self.handle = DeviceSddmmPlan(self.device_layout)

@@ -114,3 +114,27 @@ def test_reference_named_facade():
     tiles = post_process_for_withdraw(op, *res[:4])
     ms = measure_latency(*measure_seleted_formats(op, "spmm", 1, tiles, 0, ["A"], 16))
     assert ms > 0
+
+
+def test_plan_cache_reuses_plans_for_operator_and_transpose(tmp_path):
+    """With a cache directory the first operator searches and stores its
+    plan (and its transpose's, on the first backward); a second operator over
+    the same pattern with other values loads both and computes the same
+    products as a fresh search."""
+    A = syn.power_law_rows(3000, 2500, min_len=2, max_len=300, seed=5)
+    N = 64
+    cfg = PlanConfig(tc_mode=D.TC_SPLIT_BF16, cache_dir=str(tmp_path))
+    op1 = plan_spmm(A, N, cfg)
+    assert op1.plan_source == "search"
+    assert op1.transposed[0].plan_source == "search"
+    A2 = sp.csr_matrix((np.random.default_rng(6).uniform(-1, 1, A.nnz), A.indices, A.indptr), shape=A.shape)
+    op2 = plan_spmm(A2, N, cfg)
+    opT, _ = op2.transposed
+    assert op2.plan_source == "cache" and opT.plan_source == "cache"
+    fresh = plan_spmm(A2, N, PlanConfig(tc_mode=D.TC_SPLIT_BF16))
+    B = torch.as_tensor(np.random.default_rng(7).standard_normal((A.shape[1], N)).astype(np.float32), device="cuda")
+    # same arrays on the device; atomic adds may land in another order
+    assert torch.allclose(op2(B), fresh(B), rtol=1e-6, atol=1e-6)
+    dC = torch.as_tensor(np.random.default_rng(8).standard_normal((A.shape[0], N)).astype(np.float32), device="cuda")
+    assert torch.allclose(opT(dC), fresh.transposed[0](dC), rtol=1e-6, atol=1e-6)
+    assert S.rel_fro(opT(dC).cpu().numpy(), S.spmm_fp64(A2.T.tocsr(), dC.cpu().numpy())) <= 1e-5
