@@ -323,17 +323,17 @@ __global__ void __launch_bounds__(kTcThreads) spmm_tc_kernel(SpmmArgs p) {
 // slice; its units are (slice, chunk) pairs in that order.
 // Roles (kProdWarps producer warps, then one warp whose lane 0 issues the
 // MMAs, then four epilogue warps):
-//  * Column ids: every 32 steps each producer thread loads kColPer ids of
-//    the block after next and, one block later, stores them into a
-//    two-block shared ring; one producer barrier per block publishes it.
-//    No copy ever waits on a column-id load.
-//  * Producers: per k-step thread (w, l) copies features 4l..4l+3 of the
-//    step's rows w, w + kProdWarps, ... (and threads 0-31 the step's 512-byte
-//    value image) with cp.async into a kTcStages-deep raw ring, kTcStages-1
-//    steps ahead (commit groups, no register scoreboards).  It converts its
-//    own copies to bf16 / fp16 into operand slot g % 4 and one lane per warp
-//    arrives on the slot's full barrier; before refilling a slot lane 0
-//    waits on its empty barrier (committed by the MMA that read it).
+//  * Producers: warp w fills the steps g = w, w + kProdWarps, ... and owns
+//    raw stage w and operand slot g % kWsSlots.  Per step each lane copies
+//    features 4l..4l+3 of the step's 16 B rows and 16 bytes of its 512-byte
+//    value image with cp.async into the stage (the rows' column ids, one per
+//    lane 0-15, were loaded one step earlier and are broadcast by shuffle),
+//    then, once the copies landed and the MMA that last read the slot has
+//    committed its empty barrier, converts its own copies to the bf16 / fp16
+//    A image in the slot, and lane 0 arrives on the slot's full barrier.
+//    The next step's copies go out right after, so every producer warp keeps
+//    one step in flight while the others convert: the steps of one CTA
+//    overlap kProdWarps ways, and no producer waits on another.
 //  * MMA: per unit t waits until the epilogue released accumulator t % 4
 //    (TMEM columns 16 * (t % 4)), then per step waits for a full slot,
 //    issues tcgen05.mma and commits to the slot's empty barrier; a unit's
@@ -342,29 +342,23 @@ __global__ void __launch_bounds__(kTcThreads) spmm_tc_kernel(SpmmArgs p) {
 //    TMEM lanes 32 * (w % 4)..+31), releases it and writes C.
 // Every wait is bounded; a wait that gives up sets the error flag and ends
 // that role, and the others then end at their next (bounded) wait.
-constexpr int kTcStages = 5;                             // raw ring stages (4 steps in flight)
+constexpr int kProdWarps = 4;                            // producer warps, one step in flight each
 constexpr int kAccBufs = 4;                              // accumulators of 16 TMEM columns
-constexpr int kColBlock = 32;                            // k-steps per column-id block
 constexpr uint32_t kWsRaw = kRawRows + kBStage;          // 8704 B: 16 fp32 rows + value image
 constexpr uint32_t kWsSlot = kAStage + 1024;             // A image + value image, 1024-aligned
-constexpr int kWsSlots = 4;                              // operand slots between producers and MMA
-constexpr uint32_t kColRing = 2 * kColBlock * 16 * 4;    // 4 KB
-constexpr uint32_t kWsBytes = 1024 + kWsSlots * kWsSlot + kTcStages * kWsRaw + kColRing + 256;
-constexpr int kProdWarps = 4;                            // producer warps: 16 / kProdWarps rows each
-constexpr int kRowsPerWarp = 16 / kProdWarps;
-constexpr int kProdThreads = kProdWarps * 32;
-constexpr int kColPer = 16 * kColBlock / kProdThreads;   // column ids per producer thread per block
+constexpr int kWsSlots = kProdWarps;                     // operand slots: warp w fills slot w
+constexpr uint32_t kWsBytes = 1024 + kWsSlots * kWsSlot + kProdWarps * kWsRaw + 256;
 constexpr int kWsThreads = (kProdWarps + 1 + 4) * 32;   // producers, MMA warp, 4 epilogue warps
+constexpr int kWsCtasPerSm = 4;
 
 // kFull: every 128-feature slice is complete (N % 128 == 0)
 template <int MODE, bool kFull>
-__global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
+__global__ void __launch_bounds__(kWsThreads, kWsCtasPerSm) spmm_tc_ws_kernel(SpmmArgs p) {
   extern __shared__ uint8_t smem_raw[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t slots = (smem_u32(smem_raw) + 1023u) & ~1023u;
   const uint32_t ring = slots + kWsSlots * kWsSlot;
-  const uint32_t cring = ring + kTcStages * kWsRaw;
-  const uint32_t bars = cring + kColRing;
+  const uint32_t bars = ring + kProdWarps * kWsRaw;
   // full[kWsSlots], empty[kWsSlots], acc_full[kAccBufs], acc_empty[kAccBufs], drain
   const uint32_t full0 = bars, empty0 = bars + 8 * kWsSlots;
   const uint32_t accf0 = bars + 16 * kWsSlots, acce0 = accf0 + 8 * kAccBufs;
@@ -373,7 +367,7 @@ __global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
 
   if (tid == 0) {
     for (int s = 0; s < kWsSlots; ++s) {
-      mbar_init(full0 + 8 * s, kProdWarps);
+      mbar_init(full0 + 8 * s, 1);
       mbar_init(empty0 + 8 * s, 1);
     }
     for (int b = 0; b < kAccBufs; ++b) {
@@ -408,73 +402,41 @@ __global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
   if (warp < kProdWarps) {
     // ---------------- producers ----------------
     const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
-    // column-id blocks: thread t carries kColPer ids (rows
-    // (t % (16 / kColPer)) * kColPer ..) of the block's step t / (16 / kColPer)
-    constexpr int kThrPerStep = 16 / kColPer;
-    const int cstep = tid / kThrPerStep, crow = (tid % kThrPerStep) * kColPer;
-    int cblk[kColPer];
-#pragma unroll
-    for (int i = 0; i < kColPer; ++i) cblk[i] = 0;
-    long cblk_g = 0;  // first step of the block held in cblk
-    auto col_block_load = [&](long g0b) {
-      cblk_g = g0b;
-      const long g = g0b + cstep;
-      if (g < T) {
-        const int local = (int)(g % S);
-#pragma unroll
-        for (int i = 0; i < kColPer; ++i) cblk[i] = __ldg(p.tc_cols + (long)(s_beg + local) * 16 + crow + i);
-      }
-    };
-    auto col_block_store = [&]() {
-      const uint32_t half = (uint32_t)((cblk_g / kColBlock) & 1);
-      const uint32_t dst = cring + half * (kColBlock * 64) + (uint32_t)cstep * 64 + (uint32_t)crow * 4;
-#pragma unroll
-      for (int i = 0; i < kColPer; ++i) st_shared_u32(dst + 4 * i, (uint32_t)cblk[i]);
-    };
-    auto producer_sync = [&]() { asm volatile("bar.sync 1, %0;" ::"n"(kProdThreads) : "memory"); };
-    // issue cursor: step gi = k-step ks of slice f0
-    long gi = 0;
-    int iks = s_beg, if0 = 0;
-    auto issue = [&]() {
-      if (gi % kColBlock == 0) {
-        // entering block gi / 32: publish it, then fetch the one after it
-        col_block_store();
-        producer_sync();
-        col_block_load(gi + kColBlock);
-      }
-      if (gi < T) {
-        const uint32_t sr = ring + (uint32_t)(gi % kTcStages) * kWsRaw;
-        const uint32_t crow = cring + (uint32_t)((gi / kColBlock) & 1) * (kColBlock * 64) +
-                              (uint32_t)(gi % kColBlock) * 64;
-        const int f = if0 + 4 * lane;
-        const uint32_t bytes = kFull ? 16u : ((f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u));
-#pragma unroll
-        for (int j = 0; j < kRowsPerWarp; ++j) {
-          const int kk = warp + kProdWarps * j;
-          uint32_t col;
-          asm volatile("ld.shared.u32 %0, [%1];" : "=r"(col) : "r"(crow + 4u * kk));
-          const float* row = p.B + (long)col * p.ldb;
-          cp_async16(sr + kk * 512 + lane * 16, bytes ? (const void*)(row + f) : (const void*)row, bytes);
-        }
-        if (tid < 32) cp_async16(sr + kRawRows + tid * 16, vals + (long)iks * kBStage + tid * 16, 16u);
-      }
-      ++gi;
-      if (++iks == s_beg + S) {
-        iks = s_beg;
-        if0 += 128;
-      }
-    };
-    col_block_load(0);
-#pragma unroll 1
-    for (int j = 0; j < kTcStages - 1; ++j) {
-      issue();
-      cp_async_commit();
+    const uint32_t stage = ring + (uint32_t)warp * kWsRaw;
+    // step g is k-step s_beg + loc of feature slice f0 / 128 (g = f0 / 128 * S + loc)
+    long g = warp;
+    int loc = 0, f0 = 0;
+    if (g < T) {
+      loc = warp % S;
+      f0 = (warp / S) * 128;
     }
-#pragma unroll 1
-    for (long g = 0; g < T; ++g) {
-      issue();
+    auto step_cols = [&](long gg, int l) {
+      return (gg < T && lane < 16) ? __ldg(p.tc_cols + (long)(s_beg + l) * 16 + lane) : 0;
+    };
+    auto issue = [&](int cols, int l, int ff) {
+      const int f = ff + 4 * lane;
+      const uint32_t bytes = kFull ? 16u : ((f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u));
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        const int col = __shfl_sync(0xffffffffu, cols, r);
+        const float* row = p.B + (long)col * p.ldb;
+        cp_async16(stage + r * 512 + lane * 16, bytes ? (const void*)(row + f) : (const void*)row, bytes);
+      }
+      cp_async16(stage + kRawRows + lane * 16, vals + (long)(s_beg + l) * kBStage + lane * 16, 16u);
       cp_async_commit();
-      cp_async_wait<kTcStages - 1>();
+    };
+    if (g < T) issue(step_cols(g, loc), loc, f0);
+#pragma unroll 1
+    for (; g < T; g += kProdWarps) {
+      // this warp's next step and its column ids (used after the convert)
+      const long gn = g + kProdWarps;
+      int locn = loc + kProdWarps, f0n = f0;
+      while (locn >= S) {
+        locn -= S;
+        f0n += 128;
+      }
+      const int coln = step_cols(gn, locn);
+      cp_async_wait<0>();
       const int slot = (int)(g % kWsSlots);
       if (g >= kWsSlots) {
         const uint32_t par = (uint32_t)((g - kWsSlots) / kWsSlots) & 1u;
@@ -486,30 +448,25 @@ __global__ void __launch_bounds__(kWsThreads, 3) spmm_tc_ws_kernel(SpmmArgs p) {
         }
         if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par);  // completed: returns at once
       }
-      const uint32_t sr = ring + (uint32_t)(g % kTcStages) * kWsRaw;
       const uint32_t sa = slots + slot * kWsSlot;
 #pragma unroll
-      for (int j = 0; j < kRowsPerWarp; ++j) {
-        const int kk = warp + kProdWarps * j;
-        const uint4 raw = ld_shared_v4(sr + kk * 512 + lane * 16);
+      for (int r = 0; r < 16; ++r) {
+        const uint4 raw = ld_shared_v4(stage + r * 512 + lane * 16);
         const float4 v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y), __uint_as_float(raw.z),
                                      __uint_as_float(raw.w));
-        const uint32_t o = a_img_off(4 * lane, kk);
+        const uint32_t o = a_img_off(4 * lane, r);
         if (MODE == STILE_TC_F16) st_shared_v2(sa + o, pack_f16x2(v.x, v.y), pack_f16x2(v.z, v.w));
         else st_shared_v2(sa + o, pack_bf16x2(v.x, v.y), pack_bf16x2(v.z, v.w));
       }
-      if (tid < 32) st_shared_v4(sa + kAStage + tid * 16, ld_shared_v4(sr + kRawRows + tid * 16));
+      st_shared_v4(sa + kAStage + lane * 16, ld_shared_v4(stage + kRawRows + lane * 16));
       fence_proxy_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(full0 + 8 * slot);
+      if (gn < T) issue(coln, locn, f0n);
+      loc = locn;
+      f0 = f0n;
     }
     cp_async_wait<0>();
-    // a producer that stopped early still arrives at every column-block
-    // barrier the others reach: issue() runs for gi in [0, T + kTcStages - 1)
-    if (!ok) {
-      for (; gi < T + kTcStages - 1; ++gi)
-        if (gi % kColBlock == 0) producer_sync();
-    }
   } else if (warp == kProdWarps) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
