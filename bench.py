@@ -37,11 +37,9 @@ def log(*a):
 
 
 def make_workload(seed=0):
-    from stile_gb300 import synthetic as syn
-    A = syn.community_graph(n=169_343, target_nnz=1_170_000, exponent=2.0, block_frac=0.30, seed=seed)
-    B = syn.dense_operand(A.shape[1], N_FEAT, seed=1)
-    dC = syn.dense_operand(A.shape[0], N_FEAT, seed=2)
-    return A, B, dC
+    from stile_gb300 import workloads as W
+    w = W.graph(seed)
+    return w.A, w.dense["B"], w.dense["dC"]
 
 
 def algorithmic_bytes_spmm(A, N, s_a=4, s_b=4, s_c=4):
@@ -515,15 +513,161 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# the other configurations (one JSON line each; the headline is "graph")
+# ---------------------------------------------------------------------------
+def run_config(args):
+    import torch
+    import oracle.semantics as S
+    from stile_gb300 import device as D
+    from stile_gb300 import workloads as W
+    from stile_gb300.api import PlanConfig, SddmmOperator, SpmmOperator
+    from stile_gb300.ops import CsrMatrix, DeviceSddmmPlan
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    t0 = time.time()
+    w = W.BY_NAME[args.workload]()
+    A = w.A
+    log(f"[bench] {w.name} {A.shape} nnz={A.nnz} ({time.time() - t0:.1f}s)")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(fn, steps):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        ts = []
+        for _ in range(steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            fn()
+            e.record()
+            e.synchronize()
+            ts.append(s.elapsed_time(e))
+        return float(np.median(ts))
+
+    def plan_summary(plan):
+        return {f"{k[0]}{'/atomic' if k[1] else ''}": v for k, v in plan.summary().items()}
+
+    peak, peak_kind = measured_peaks()
+    out = {"workload": w.name, "note": w.note, "M": int(A.shape[0]), "K": int(A.shape[1]), "nnz": int(A.nnz),
+           "width": int(w.width), "steps": args.steps, "l2": "flushed between iterations (256 MiB write)"}
+    if w.kind == "spmm":
+        N = w.width
+        tc_mode = D.TC_SPLIT_BF16 if w.fp32 else D.TC_BF16
+        t0 = time.time()
+        op = SpmmOperator(A, N, PlanConfig(tc_mode=tc_mode))
+        opT, _ = op.transposed
+        out["plan_search_s"] = round(time.time() - t0, 2)
+        out["plan"] = plan_summary(op.plan)
+        out["tc_mode"] = {D.TC_BF16: "bf16", D.TC_SPLIT_BF16: "split-bf16 (fp32 path)"}[tc_mode]
+        B_np, dC_np = w.dense["B"], w.dense["dC"]
+        B = torch.as_tensor(B_np, device=dev)
+        dC = torch.as_tensor(dC_np, device=dev)
+        C = torch.empty((A.shape[0], N), device=dev)
+        dB = torch.empty((A.shape[1], N), device=dev)
+        AT = opT.A
+
+        def step():
+            op(B, out=C)
+            op.dvals(dC, B)
+            opT(dC, out=dB)
+
+        op(B, out=C)
+        opT(dC, out=dB)
+        dv = op.dvals(dC, B)
+        torch.cuda.synchronize()
+        ids, ref = W.sddmm_fp64_sample(A, dC_np, B_np)
+        out["accuracy"] = {"C_rel_fro": S.rel_fro(C.cpu().numpy(), S.spmm_fp64(A, B_np)),
+                           "dB_rel_fro": S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(AT, dC_np)),
+                           "dvals_rel_fro_sampled": S.rel_fro(dv.cpu().numpy()[ids], ref),
+                           "dvals_sample": int(len(ids))}
+        ms_step = timed(step, args.steps)
+        ms_fwd = timed(lambda: op(B, out=C), args.steps)
+        csrA, csrAT = CsrMatrix(A), CsrMatrix(AT)
+        plain_dev = D.SddmmDevice(M=A.shape[0], K=A.shape[1], nnz=A.nnz,
+                                  mid_idx=np.repeat(np.arange(A.shape[0]), np.diff(A.indptr)).astype(np.int32),
+                                  j_idx=A.indices.astype(np.int32), remap=np.arange(A.nnz, dtype=np.int32), bm=16,
+                                  bn=16, blk_i=np.zeros(0, np.int32), blk_j=np.zeros(0, np.int32),
+                                  blk_indptr=np.zeros(1, np.int32), blk_dense_pos=np.zeros(0, np.int32),
+                                  blk_out=np.zeros(0, np.int32))
+        plain_sddmm = DeviceSddmmPlan(plain_dev)
+
+        def plain_step():
+            csrA.spmm(B, out=C)
+            plain_sddmm.run(dC, B)
+            csrAT.spmm(dC, out=dB)
+
+        ms_plain = timed(plain_step, args.steps)
+        ms_plain_fwd = timed(lambda: csrA.spmm(B, out=C), args.steps)
+        flops = 3 * 2 * A.nnz * N
+        alg = algorithmic_bytes_spmm(A, N)
+        out.update({"metric": "fwd+bwd GFLOP/s", "value": flops / (ms_step * 1e-3) / 1e9, "ms_per_step": ms_step,
+                    "forward_ms": ms_fwd, "csr_step_ms": ms_plain, "csr_forward_ms": ms_plain_fwd,
+                    "speedup_step_over_csr": ms_plain / ms_step, "speedup_forward_over_csr": ms_plain_fwd / ms_fwd,
+                    "roofline_forward": {"algorithmic_bytes": int(alg), "achieved_gbs": alg / (ms_fwd * 1e-3) / 1e9,
+                                         "peak_gbs": peak, "frac": alg / (ms_fwd * 1e-3) / 1e9 / peak,
+                                         "peak_source": peak_kind}})
+        if args.workload.startswith("pruned"):
+            # the plan chosen by the learned cost model against the analytic one
+            try:
+                t0 = time.time()
+                op_l = SpmmOperator(A, N, PlanConfig(tc_mode=tc_mode, learned=True))
+                t_l = time.time() - t0
+                Cl = torch.empty_like(C)
+                ms_l = timed(lambda: op_l(B, out=Cl), args.steps)
+                out["learned_cost_model"] = {"plan": plan_summary(op_l.plan), "plan_search_s": round(t_l, 2),
+                                             "forward_ms": ms_l, "analytic_forward_ms": ms_fwd,
+                                             "C_rel_fro": S.rel_fro(Cl.cpu().numpy(), S.spmm_fp64(A, B_np))}
+                op_l.handle.close()
+            except FileNotFoundError as exc:
+                out["learned_cost_model"] = {"unavailable": str(exc)}
+    else:
+        F = w.width
+        t0 = time.time()
+        op = SddmmOperator(A, F)
+        out["plan_search_s"] = round(time.time() - t0, 2)
+        out["plan"] = plan_summary(op.plan)
+        X_np, Y_np = w.dense["X"], w.dense["Y"]
+        X = torch.as_tensor(X_np, device=dev)
+        Y = torch.as_tensor(Y_np, device=dev)
+        res = op(X, Y)
+        torch.cuda.synchronize()
+        ids, ref = W.sddmm_fp64_sample(A, X_np, Y_np)
+        out["accuracy"] = {"rel_fro_sampled": S.rel_fro(res.cpu().numpy()[ids], ref), "sample": int(len(ids))}
+        ms = timed(lambda: op(X, Y), args.steps)
+        plain_dev = D.SddmmDevice(M=A.shape[0], K=A.shape[1], nnz=A.nnz,
+                                  mid_idx=np.repeat(np.arange(A.shape[0]), np.diff(A.indptr)).astype(np.int32),
+                                  j_idx=A.indices.astype(np.int32), remap=np.arange(A.nnz, dtype=np.int32), bm=16,
+                                  bn=16, blk_i=np.zeros(0, np.int32), blk_j=np.zeros(0, np.int32),
+                                  blk_indptr=np.zeros(1, np.int32), blk_dense_pos=np.zeros(0, np.int32),
+                                  blk_out=np.zeros(0, np.int32))
+        plain = DeviceSddmmPlan(plain_dev)
+        ms_plain = timed(lambda: plain.run(X, Y), args.steps)
+        flops = 2 * A.nnz * F
+        alg = algorithmic_bytes_sddmm(A, F)
+        out.update({"metric": "SDDMM GFLOP/s", "value": flops / (ms * 1e-3) / 1e9, "ms": ms,
+                    "plain_list_ms": ms_plain, "speedup_over_plain_list": ms_plain / ms,
+                    "roofline": {"algorithmic_bytes": int(alg), "achieved_gbs": alg / (ms * 1e-3) / 1e9,
+                                 "peak_gbs": peak, "frac": alg / (ms * 1e-3) / 1e9 / peak,
+                                 "peak_source": peak_kind}})
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="stile", choices=["stile", "reference"])
+    ap.add_argument("--workload", default="graph",
+                    help="graph (the headline line) or one of the other configurations: plain, plain_min10, "
+                         "pruned, pruned_t, sddmm, gcn, gcn_41 (one JSON line of measurements each)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "graph":
+        run_config(args)
     else:
         run_gpu(args)
 
