@@ -313,7 +313,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   std::vector<int32_t> s_cols, s_nnz;
   std::vector<uint8_t> s_vals;
   if (nck > 0) {
-    const int resident = stile::tc_persistent_ctas();
+    const int resident = stile::tc_persistent_ctas(mode);
     if (resident <= 0) return fail(STILE_E_CUDA, "cannot size the tensor-core grid");
     tc_grid = (int)std::min<long>(resident, nck);
     std::vector<int32_t> by_len(nck);

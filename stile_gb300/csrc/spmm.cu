@@ -4,9 +4,9 @@
 //  * zero_rows_kernel    zeroes output rows that no owned tile stores
 //  * spmm_tc_ws_kernel   dense 16-row block tiles on the tensor cores
 //                        (tcgen05.mma, accumulator in TMEM): warp-specialised
-//                        cp.async producers + MMA issuer (bf16 / fp16)
-//  * spmm_tc_kernel      the same with hi+lo split products and periodic
-//                        accumulator drains (split-bf16, fp32-level accuracy)
+//                        cp.async producers + MMA issuer (bf16 / fp16, and
+//                        split-bf16 hi+lo products with periodic accumulator
+//                        drains for fp32-level accuracy)
 //  * spmm_ell_seg_kernel ELL row-bucket tiles on CUDA cores, as a stream of
 //                        live entries cut into groups at row boundaries
 //                        The two launches together are the reference's
@@ -125,11 +125,11 @@ __global__ void zero_rows_kernel(const int* __restrict__ rows, int n_rows, float
 // hybrid SpMM: tensor-core kernel + ELL kernel (launched back to back)
 // ===========================================================================
 // Tensor-core chunks.  A chunk is a run of at most kChunkSteps k-steps of
-// one item (items longer than that are split; the split parts accumulate
-// with atomics into pre-zeroed rows).  Per k-step the CTA gathers the 16
-// referenced B rows (fp32, 128 features) with cp.async into a 4-stage ring
-// together with the step's 16x16 value image, converts its own copies to the
-// bf16 / fp16 A-operand image and one thread issues the tcgen05.mma.
+// one item (items longer than that are split; the parts add into rows that
+// another writer initialises).  Per k-step the kernel gathers the 16
+// referenced B rows (fp32, 128 features) and the step's 16x16 value image,
+// converts the rows to the bf16 / fp16 A-operand image and one thread
+// issues the tcgen05.mma.
 //
 // Shared-memory operand layouts (checked by the layout probe):
 //   A: [128 features (M) x 16 k (K)], MN-major, 128-byte swizzle: two
@@ -141,178 +141,12 @@ constexpr uint32_t kAStage = 4096;   // bytes of one A image (16-bit)
 constexpr uint32_t kBStage = 512;    // bytes of one B image (16-bit)
 constexpr uint32_t kALbo = 2048, kASbo = 1024;
 constexpr uint32_t kBLbo = 128, kBSbo = 256;
-constexpr int kTcThreads = 128;
-constexpr int kStages = 4;           // cp.async ring depth
 constexpr uint32_t kRawRows = 8192;  // 16 rows x 128 fp32 per stage
 
 __device__ __forceinline__ uint32_t a_img_off(int m, int k) {
   // m: feature (0..127), k: column within the k-step (0..15)
   const int atom = m >> 6, grp = k >> 3, r = k & 7, chunk = (m & 63) >> 3;
   return (uint32_t)(atom * kALbo + grp * kASbo + r * 128 + ((chunk ^ r) << 4) + (m & 7) * 2);
-}
-
-template <bool kSplit>
-struct TcLayout {
-  static constexpr uint32_t kVals = kSplit ? 2 * kBStage : kBStage;
-  static constexpr uint32_t kStage = kRawRows + kVals;
-  static constexpr uint32_t kAImg = kSplit ? 2 * kAStage : kAStage;
-  static constexpr uint32_t kRing = kStages * kStage;                 // multiple of 1024
-  static constexpr uint32_t kBytes = 1024 + kRing + 2 * kAImg + 64;  // + alignment slack
-};
-
-template <int MODE>
-__global__ void __launch_bounds__(kTcThreads) spmm_tc_kernel(SpmmArgs p) {
-  constexpr bool kSplit = (MODE == STILE_TC_SPLIT_BF16);
-  using L = TcLayout<kSplit>;
-  extern __shared__ uint8_t smem_raw[];
-  const int chunk = blockIdx.x / p.n_fchunks;
-  const int f0 = (blockIdx.x % p.n_fchunks) * 128;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-
-  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
-  const uint32_t ring = base;
-  const uint32_t aimg = base + L::kRing;
-  const uint32_t bar = aimg + 2 * L::kAImg;
-  const uint32_t tmem_slot = bar + 8;
-
-  if (tid == 0) {
-    mbar_init(bar, 1);
-    fence_mbar_init();
-  }
-  if (warp == 0) {
-    tmem_alloc(tmem_slot, 32);
-    tmem_relinquish();
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  uint32_t tmem;
-  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
-
-  const int kb = p.tc_chunk_kbeg[chunk];
-  const int n = p.tc_chunk_nk[chunk];
-  const int item = p.tc_chunk_item[chunk];
-  const int N = p.N;
-  const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
-  const uint32_t idesc = (MODE == STILE_TC_F16) ? make_idesc(0, 0, 1, 0, 128, 16)
-                                                : make_idesc(1, 1, 1, 0, 128, 16);
-
-  // this thread's 4 copies per stage: rows warp + 4j, features 4*lane..+3
-  auto issue = [&](int ks, int stg) {
-    const uint32_t sb = ring + stg * L::kStage;
-    const int f = f0 + 4 * lane;
-    const uint32_t bytes = (f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int kk = warp + 4 * j;
-      const float* row = p.B + (long)p.tc_cols[(long)ks * 16 + kk] * p.ldb;
-      cp_async16(sb + kk * 512 + lane * 16, bytes ? (const void*)(row + f) : (const void*)row, bytes);
-    }
-    if (tid < (int)(L::kVals / 16))
-      cp_async16(sb + kRawRows + tid * 16, vals + (long)ks * L::kVals + tid * 16, 16u);
-  };
-
-  // k-steps per accumulation chain before the accumulator is drained into
-  // fp32 registers (bounds the tensor core's accumulation chain)
-  constexpr int kGroup = kSplit ? 4 : 16;
-  float acc[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) acc[i] = 0.f;
-  const uint32_t my_lanes = tmem + ((uint32_t)(32 * warp) << 16);
-  bool ok = true;
-
-#pragma unroll 1
-  for (int j = 0; j < kStages - 1; ++j) {
-    if (j < n) issue(kb + j, j);
-    cp_async_commit();
-  }
-#pragma unroll 1
-  for (int step = 0; step < n; ++step) {
-    // the MMA of the previous step has read the stage the next copy overwrites
-    bool w_ok = true;
-    if (step >= 1) w_ok = mbar_wait_bounded(bar, (uint32_t)(step - 1) & 1u);
-    if (w_ok && step + kStages - 1 < n) issue(kb + step + kStages - 1, (step + kStages - 1) % kStages);
-    cp_async_commit();
-    cp_async_wait<kStages - 1>();
-    const uint32_t sb = ring + (step % kStages) * L::kStage;
-    const uint32_t ai = aimg + (step & 1) * L::kAImg;
-    if (w_ok) {
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int kk = warp + 4 * j;
-        const uint4 raw = ld_shared_v4(sb + kk * 512 + lane * 16);
-        const float4 v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y),
-                                     __uint_as_float(raw.z), __uint_as_float(raw.w));
-        const uint32_t o = a_img_off(4 * lane, kk);
-        if (MODE == STILE_TC_F16) {
-          st_shared_v2(ai + o, pack_f16x2(v.x, v.y), pack_f16x2(v.z, v.w));
-        } else {
-          const uint32_t h0 = pack_bf16x2(v.x, v.y), h1 = pack_bf16x2(v.z, v.w);
-          st_shared_v2(ai + o, h0, h1);
-          if (kSplit) {
-            const __nv_bfloat162 b0 = *reinterpret_cast<const __nv_bfloat162*>(&h0);
-            const __nv_bfloat162 b1 = *reinterpret_cast<const __nv_bfloat162*>(&h1);
-            const float2 r0 = __bfloat1622float2(b0), r1 = __bfloat1622float2(b1);
-            st_shared_v2(ai + kAStage + o, pack_bf16x2(v.x - r0.x, v.y - r0.y),
-                         pack_bf16x2(v.z - r1.x, v.w - r1.y));
-          }
-        }
-      }
-    }
-    fence_proxy_async_smem();
-    ok = __syncthreads_and(w_ok && ok) != 0;
-    if (!ok) break;
-    const bool group_start = (step % kGroup) == 0;
-    const bool group_end = ((step % kGroup) == kGroup - 1) || (step == n - 1);
-    if (tid == 0) {
-      tc_fence_after();
-      const uint64_t ad = smem_desc(ai, kALbo, kASbo, kSwizzle128B);
-      const uint64_t bd = smem_desc(sb + kRawRows, kBLbo, kBSbo, kSwizzleNone);
-      umma_f16(tmem, ad, bd, idesc, group_start ? 0u : 1u);
-      if (kSplit) {
-        const uint64_t ad_lo = smem_desc(ai + kAStage, kALbo, kASbo, kSwizzle128B);
-        const uint64_t bd_lo = smem_desc(sb + kRawRows + kBStage, kBLbo, kBSbo, kSwizzleNone);
-        umma_f16(tmem, ad, bd_lo, idesc, 1u);
-        umma_f16(tmem, ad_lo, bd, idesc, 1u);
-        umma_f16(tmem, ad_lo, bd_lo, idesc, 1u);
-      }
-      umma_commit(bar);
-    }
-    if (group_end) {
-      const bool done = __syncthreads_and(mbar_wait_bounded(bar, (uint32_t)step & 1u)) != 0;
-      if (!done) {
-        ok = false;
-        break;
-      }
-      tc_fence_after();
-      uint32_t r[16];
-      tmem_ld16(my_lanes, r);
-      tmem_wait_ld();
-#pragma unroll
-      for (int i = 0; i < 16; ++i) acc[i] += __uint_as_float(r[i]);
-      tc_fence_before();
-      __syncthreads();
-      tc_fence_after();
-    }
-  }
-  cp_async_wait<0>();
-  if (!ok && tid == 0) atomicOr(p.err_flag, 1);
-
-  // epilogue: warp w owns features f0+32w+lane, 16 tile rows in registers
-  const int f = f0 + 32 * warp + lane;
-  const bool atomic = (p.tc_chunk_flags[chunk] & 1) != 0;
-  if (f < N && n > 0 && ok) {
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const int row = p.tc_out_rows[(long)item * 16 + i];
-      if (row < 0) continue;
-      float* dst = p.C + (long)row * p.ldc + f;
-      if (atomic) atomicAdd(dst, acc[i]); else *dst = acc[i];
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, 32);
 }
 
 // Persistent bf16 / fp16 tensor-core kernel.
@@ -344,21 +178,35 @@ __global__ void __launch_bounds__(kTcThreads) spmm_tc_kernel(SpmmArgs p) {
 // that role, and the others then end at their next (bounded) wait.
 constexpr int kProdWarps = 4;                            // producer warps, one step in flight each
 constexpr int kAccBufs = 4;                              // accumulators of 16 TMEM columns
-constexpr uint32_t kWsRaw = kRawRows + kBStage;          // 8704 B: 16 fp32 rows + value image
-constexpr uint32_t kWsSlot = kAStage + 1024;             // A image + value image, 1024-aligned
 constexpr int kWsSlots = kProdWarps;                     // operand slots: warp w fills slot w
-constexpr uint32_t kWsBytes = 1024 + kWsSlots * kWsSlot + kProdWarps * kWsRaw + 256;
 constexpr int kWsThreads = (kProdWarps + 1 + 4) * 32;   // producers, MMA warp, 4 epilogue warps
-constexpr int kWsCtasPerSm = 4;
+
+// Per-mode layout.  Split-bf16 (fp32-level accuracy) keeps hi and lo images
+// of both operands: A = hi(B rows) | lo(B rows), values = hi | lo, and
+// issues three MMAs per step (hi*hi + hi*lo + lo*hi); its accumulator is
+// drained into the epilogue's fp32 registers every kGroup steps, which
+// bounds the tensor core's accumulation chain.
+template <int MODE>
+struct WsCfg {
+  static constexpr bool kSplit = MODE == STILE_TC_SPLIT_BF16;
+  static constexpr uint32_t kVals = kSplit ? 2 * kBStage : kBStage;   // value image(s) per step
+  static constexpr uint32_t kAImg = kSplit ? 2 * kAStage : kAStage;   // A image(s) per step
+  static constexpr uint32_t kSlot = kAImg + 1024;                     // + value images, 1024-aligned
+  static constexpr uint32_t kRaw = kRawRows + kVals;                  // 16 fp32 rows + value image(s)
+  static constexpr uint32_t kBytes = 1024 + kWsSlots * kSlot + kProdWarps * kRaw + 256;
+  static constexpr int kCtas = kSplit ? 3 : 4;                        // resident CTAs per SM
+  static constexpr int kGroup = kSplit ? 4 : (1 << 30);               // k-steps per accumulator drain
+};
 
 // kFull: every 128-feature slice is complete (N % 128 == 0)
 template <int MODE, bool kFull>
-__global__ void __launch_bounds__(kWsThreads, kWsCtasPerSm) spmm_tc_ws_kernel(SpmmArgs p) {
+__global__ void __launch_bounds__(kWsThreads, WsCfg<MODE>::kCtas) spmm_tc_ws_kernel(SpmmArgs p) {
+  using W = WsCfg<MODE>;
   extern __shared__ uint8_t smem_raw[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t slots = (smem_u32(smem_raw) + 1023u) & ~1023u;
-  const uint32_t ring = slots + kWsSlots * kWsSlot;
-  const uint32_t bars = ring + kProdWarps * kWsRaw;
+  const uint32_t ring = slots + kWsSlots * W::kSlot;
+  const uint32_t bars = ring + kProdWarps * W::kRaw;
   // full[kWsSlots], empty[kWsSlots], acc_full[kAccBufs], acc_empty[kAccBufs], drain
   const uint32_t full0 = bars, empty0 = bars + 8 * kWsSlots;
   const uint32_t accf0 = bars + 16 * kWsSlots, acce0 = accf0 + 8 * kAccBufs;
@@ -402,7 +250,7 @@ __global__ void __launch_bounds__(kWsThreads, kWsCtasPerSm) spmm_tc_ws_kernel(Sp
   if (warp < kProdWarps) {
     // ---------------- producers ----------------
     const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
-    const uint32_t stage = ring + (uint32_t)warp * kWsRaw;
+    const uint32_t stage = ring + (uint32_t)warp * W::kRaw;
     // step g is k-step s_beg + loc of feature slice f0 / 128 (g = f0 / 128 * S + loc)
     long g = warp;
     int loc = 0, f0 = 0;
@@ -422,7 +270,9 @@ __global__ void __launch_bounds__(kWsThreads, kWsCtasPerSm) spmm_tc_ws_kernel(Sp
         const float* row = p.B + (long)col * p.ldb;
         cp_async16(stage + r * 512 + lane * 16, bytes ? (const void*)(row + f) : (const void*)row, bytes);
       }
-      cp_async16(stage + kRawRows + lane * 16, vals + (long)(s_beg + l) * kBStage + lane * 16, 16u);
+#pragma unroll
+      for (int c = lane; c < (int)(W::kVals / 16); c += 32)
+        cp_async16(stage + kRawRows + c * 16, vals + (long)(s_beg + l) * W::kVals + c * 16, 16u);
       cp_async_commit();
     };
     if (g < T) issue(step_cols(g, loc), loc, f0);
@@ -448,17 +298,29 @@ __global__ void __launch_bounds__(kWsThreads, kWsCtasPerSm) spmm_tc_ws_kernel(Sp
         }
         if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par);  // completed: returns at once
       }
-      const uint32_t sa = slots + slot * kWsSlot;
+      const uint32_t sa = slots + slot * W::kSlot;
 #pragma unroll
       for (int r = 0; r < 16; ++r) {
         const uint4 raw = ld_shared_v4(stage + r * 512 + lane * 16);
         const float4 v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y), __uint_as_float(raw.z),
                                      __uint_as_float(raw.w));
         const uint32_t o = a_img_off(4 * lane, r);
-        if (MODE == STILE_TC_F16) st_shared_v2(sa + o, pack_f16x2(v.x, v.y), pack_f16x2(v.z, v.w));
-        else st_shared_v2(sa + o, pack_bf16x2(v.x, v.y), pack_bf16x2(v.z, v.w));
+        if (MODE == STILE_TC_F16) {
+          st_shared_v2(sa + o, pack_f16x2(v.x, v.y), pack_f16x2(v.z, v.w));
+        } else {
+          const uint32_t h01 = pack_bf16x2(v.x, v.y), h23 = pack_bf16x2(v.z, v.w);
+          st_shared_v2(sa + o, h01, h23);
+          if (W::kSplit) {
+            // lo = v - float(hi): exact in fp32, then rounded to bf16
+            const float4 hf = make_float4(__uint_as_float(h01 << 16), __uint_as_float(h01 & 0xffff0000u),
+                                          __uint_as_float(h23 << 16), __uint_as_float(h23 & 0xffff0000u));
+            st_shared_v2(sa + kAStage + o, pack_bf16x2(v.x - hf.x, v.y - hf.y), pack_bf16x2(v.z - hf.z, v.w - hf.w));
+          }
+        }
       }
-      st_shared_v4(sa + kAStage + lane * 16, ld_shared_v4(stage + kRawRows + lane * 16));
+#pragma unroll
+      for (int c = lane; c < (int)(W::kVals / 16); c += 32)
+        st_shared_v4(sa + W::kAImg + c * 16, ld_shared_v4(stage + kRawRows + c * 16));
       fence_proxy_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(full0 + 8 * slot);
@@ -473,30 +335,40 @@ __global__ void __launch_bounds__(kWsThreads, kWsCtasPerSm) spmm_tc_ws_kernel(Sp
       const uint32_t idesc = (MODE == STILE_TC_F16) ? make_idesc(0, 0, 1, 0, 128, 16)
                                                     : make_idesc(1, 1, 1, 0, 128, 16);
       long g = 0;
+      int u = 0;  // accumulation groups issued so far (accumulator u % kAccBufs)
 #pragma unroll 1
       for (int t = 0; t < n_units && ok; ++t) {
         const int n = __ldg(p.tc_chunk_nk + cb + t % nc);
-        const int b = t % kAccBufs;
-        if (t >= kAccBufs && !mbar_wait_bounded(acce0 + 8 * b, (uint32_t)((t - kAccBufs) / kAccBufs) & 1u)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t d = tmem + (uint32_t)(16 * b);
 #pragma unroll 1
-        for (int s = 0; s < n; ++s, ++g) {
-          const int slot = (int)(g % kWsSlots);
-          if (!mbar_wait_bounded(full0 + 8 * slot, (uint32_t)(g / kWsSlots) & 1u)) {
+        for (int s0 = 0; s0 < n && ok; s0 += W::kGroup, ++u) {
+          const int b = u % kAccBufs;
+          if (u >= kAccBufs && !mbar_wait_bounded(acce0 + 8 * b, (uint32_t)((u - kAccBufs) / kAccBufs) & 1u)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t sa = slots + slot * kWsSlot;
-          umma_f16(d, smem_desc(sa, kALbo, kASbo, kSwizzle128B),
-                   smem_desc(sa + kAStage, kBLbo, kBSbo, kSwizzleNone), idesc, s > 0 ? 1u : 0u);
-          umma_commit(empty0 + 8 * slot);
+          const uint32_t d = tmem + (uint32_t)(16 * b);
+          const int s1 = min(n, s0 + W::kGroup);
+#pragma unroll 1
+          for (int s = s0; s < s1; ++s, ++g) {
+            const int slot = (int)(g % kWsSlots);
+            if (!mbar_wait_bounded(full0 + 8 * slot, (uint32_t)(g / kWsSlots) & 1u)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sa = slots + slot * W::kSlot;
+            const uint64_t a_hi = smem_desc(sa, kALbo, kASbo, kSwizzle128B);
+            const uint64_t v_hi = smem_desc(sa + W::kAImg, kBLbo, kBSbo, kSwizzleNone);
+            umma_f16(d, a_hi, v_hi, idesc, s > s0 ? 1u : 0u);
+            if (W::kSplit) {
+              umma_f16(d, a_hi, smem_desc(sa + W::kAImg + kBStage, kBLbo, kBSbo, kSwizzleNone), idesc, 1u);
+              umma_f16(d, smem_desc(sa + kAStage, kALbo, kASbo, kSwizzle128B), v_hi, idesc, 1u);
+            }
+            umma_commit(empty0 + 8 * slot);
+          }
+          if (ok) umma_commit(accf0 + 8 * b);
         }
-        if (ok) umma_commit(accf0 + 8 * b);
       }
       // every MMA this thread issued has completed before TMEM is freed
       umma_commit(drain);
@@ -506,24 +378,35 @@ __global__ void __launch_bounds__(kWsThreads, kWsCtasPerSm) spmm_tc_ws_kernel(Sp
   } else {
     // ---------------- epilogue ----------------
     const int quarter = warp & 3;
+    int u = 0;  // accumulation groups consumed so far
 #pragma unroll 1
-    for (int t = 0; t < n_units; ++t) {
-      const int b = t % kAccBufs;
-      const uint32_t par = (uint32_t)(t / kAccBufs) & 1u;
-      bool got = true;
-      if (lane == 0) got = mbar_wait_bounded(accf0 + 8 * b, par);
-      if (!__shfl_sync(0xffffffffu, got, 0)) {
-        ok = false;
-        break;
+    for (int t = 0; t < n_units && ok; ++t) {
+      const int n = __ldg(p.tc_chunk_nk + cb + t % nc);
+      float acc[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) acc[i] = 0.f;
+#pragma unroll 1
+      for (int s0 = 0; s0 < n; s0 += W::kGroup, ++u) {
+        const int b = u % kAccBufs;
+        const uint32_t par = (uint32_t)(u / kAccBufs) & 1u;
+        bool got = true;
+        if (lane == 0) got = mbar_wait_bounded(accf0 + 8 * b, par);
+        if (!__shfl_sync(0xffffffffu, got, 0)) {
+          ok = false;
+          break;
+        }
+        if (lane != 0) mbar_wait_bounded(accf0 + 8 * b, par);  // completed: returns at once
+        tc_fence_after();
+        uint32_t r[16];
+        tmem_ld16(tmem + (uint32_t)(16 * b) + ((uint32_t)(32 * quarter) << 16), r);
+        tmem_wait_ld();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acce0 + 8 * b);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) acc[i] += __uint_as_float(r[i]);
       }
-      if (lane != 0) mbar_wait_bounded(accf0 + 8 * b, par);  // completed: returns at once
-      tc_fence_after();
-      uint32_t r[16];
-      tmem_ld16(tmem + (uint32_t)(16 * b) + ((uint32_t)(32 * quarter) << 16), r);
-      tmem_wait_ld();
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(acce0 + 8 * b);
+      if (!ok) break;
       const int c = cb + t % nc;
       const int f = (t / nc) * 128 + 32 * quarter + lane;
       if (kFull || f < N) {
@@ -535,8 +418,7 @@ __global__ void __launch_bounds__(kWsThreads, kWsCtasPerSm) spmm_tc_ws_kernel(Sp
           const int row = __ldg(orows + i);
           if (row < 0) continue;
           float* dst = p.C + (long)row * p.ldc + f;
-          const float v = __uint_as_float(r[i]);
-          if (atomic) atomicAdd(dst, v); else *dst = v;
+          if (atomic) atomicAdd(dst, acc[i]); else *dst = acc[i];
         }
       }
     }
@@ -727,22 +609,6 @@ cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, 
   return cudaGetLastError();
 }
 
-size_t tc_smem_bytes(int mode) {
-  return mode == STILE_TC_SPLIT_BF16 ? TcLayout<true>::kBytes : TcLayout<false>::kBytes;
-}
-
-template <int MODE>
-static cudaError_t launch_tc_t(const SpmmArgs& p, cudaStream_t st) {
-  const size_t smem = tc_smem_bytes(MODE);
-  auto k = spmm_tc_kernel<MODE>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  const int grid = p.tc_n_chunks * p.n_fchunks;
-  if (grid == 0) return cudaSuccess;
-  k<<<grid, kTcThreads, smem, st>>>(p);
-  return cudaGetLastError();
-}
-
 // CTAs of `kernel` resident per SM at `threads` threads and `smem` bytes of
 // dynamic shared memory, from the device's limits (shared memory with the
 // per-block reservation, registers, threads, blocks); at least 1.
@@ -775,6 +641,7 @@ static cudaError_t resident_ctas(K kernel, int threads, size_t smem, int* sms, i
 template <int MODE, bool kFull>
 static cudaError_t launch_ws_t(const SpmmArgs& p, cudaStream_t st) {
   auto k = spmm_tc_ws_kernel<MODE, kFull>;
+  constexpr uint32_t kWsBytes = WsCfg<MODE>::kBytes;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWsBytes);
   if (e != cudaSuccess) return e;
   // shared memory for the resident CTAs; the rest of the unified L1 /
@@ -786,10 +653,15 @@ static cudaError_t launch_ws_t(const SpmmArgs& p, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-int tc_persistent_ctas() {
+int tc_persistent_ctas(int mode) {
   int sms = 0, per_sm = 0;
-  if (resident_ctas(spmm_tc_ws_kernel<STILE_TC_BF16, true>, kWsThreads, kWsBytes, &sms, &per_sm) != cudaSuccess)
-    return 0;
+  const cudaError_t e =
+      mode == STILE_TC_SPLIT_BF16
+          ? resident_ctas(spmm_tc_ws_kernel<STILE_TC_SPLIT_BF16, true>, kWsThreads, WsCfg<STILE_TC_SPLIT_BF16>::kBytes,
+                          &sms, &per_sm)
+          : resident_ctas(spmm_tc_ws_kernel<STILE_TC_BF16, true>, kWsThreads, WsCfg<STILE_TC_BF16>::kBytes, &sms,
+                          &per_sm);
+  if (e != cudaSuccess) return 0;
   return sms * per_sm;
 }
 
@@ -797,7 +669,9 @@ cudaError_t launch_tc(const SpmmArgs& p, cudaStream_t st) {
   switch (p.tc_mode) {
     case STILE_TC_F16:
       return p.N % 128 == 0 ? launch_ws_t<STILE_TC_F16, true>(p, st) : launch_ws_t<STILE_TC_F16, false>(p, st);
-    case STILE_TC_SPLIT_BF16: return launch_tc_t<STILE_TC_SPLIT_BF16>(p, st);
+    case STILE_TC_SPLIT_BF16:
+      return p.N % 128 == 0 ? launch_ws_t<STILE_TC_SPLIT_BF16, true>(p, st)
+                            : launch_ws_t<STILE_TC_SPLIT_BF16, false>(p, st);
     default:
       return p.N % 128 == 0 ? launch_ws_t<STILE_TC_BF16, true>(p, st) : launch_ws_t<STILE_TC_BF16, false>(p, st);
   }

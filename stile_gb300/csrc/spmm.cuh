@@ -72,11 +72,10 @@ int report_error(int code, const char* msg);
 void note_launches(int n);
 // CTAs of the persistent tensor-core kernel resident on the current device
 // (0 on error)
-int tc_persistent_ctas();
+int tc_persistent_ctas(int mode);
 cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st);
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals,
                          cudaStream_t st);
-size_t tc_smem_bytes(int mode);
 constexpr int kChunkSteps = 32;
 cudaError_t launch_repack(const SpmmArgs& p, const float* vals, long n_ell_slots, cudaStream_t st);
 
