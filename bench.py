@@ -636,6 +636,14 @@ def run_config(args):
                                          "peak_gbs": peak, "frac": alg / (ms_fwd * 1e-3) / 1e9 / peak,
                                          "peak_source": peak_kind}})
         if args.workload.startswith("pruned"):
+            # activations in bf16, as the configuration has them: read as is
+            B16 = B.to(torch.bfloat16)
+            C16 = torch.empty_like(C)
+            op(B16, out=C16)
+            torch.cuda.synchronize()
+            out["bf16_B"] = {"forward_ms": timed(lambda: op(B16, out=C16), args.steps),
+                             "C_rel_fro": S.rel_fro(C16.cpu().numpy(),
+                                                    S.spmm_fp64(A, B16.float().cpu().numpy()))}
             # the plan chosen by the learned cost model against the analytic one
             try:
                 t0 = time.time()

@@ -9,9 +9,10 @@
  *       -- prepare_inputs_BSPMM / prepare_inputs_BSDDMM upload the packed
  *          format arrays with tvm.nd.array(..., device=dev)
  *          (MY_sparse/my_fuse_formats.py:3321-3332, :3544-3678)
- *   stile_spmm_run
+ *   stile_spmm_run / stile_spmm_run_bf16
  *       -- the fused SpMM PackedFunc f(*args_nd) launched by
- *          measure_latency_BSPMM (MY_sparse/my_fuse_formats.py:4152-4173)
+ *          measure_latency_BSPMM (MY_sparse/my_fuse_formats.py:4152-4173),
+ *          fp32 or bf16 dense operand
  *   stile_sddmm_run
  *       -- the fused SDDMM PackedFunc launched by measure_latency_BSDDMM
  *          (MY_sparse/my_fuse_formats.py:4292-4330) plus the host-side
@@ -141,6 +142,19 @@ int stile_sddmm_plan_free(StileSddmmPlan* plan);
  */
 int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb,
                    float* C, int64_t ldc, int32_t N, void* stream);
+
+/*
+ * The same product with B in bf16 (raw bfloat16 bits; fp32 accumulation and
+ * fp32 C): row tiles convert the gathered rows to fp32, tensor tiles feed
+ * them to the MMA unconverted.  ldb is in elements and must be a multiple
+ * of 8 (16-byte rows chunks), B 16-byte aligned; the plan's tensor tiles
+ * must be bf16 (STILE_TC_BF16), else STILE_E_UNSUPPORTED.  Counterpart: the
+ * reference's fused SpMM built for dtype "float16" / bf16 activations
+ * (SPMM/SPMMbench_our_method.py:187-222, the MydtypeIn knob).
+ */
+int stile_spmm_run_bf16(const StileSpmmPlan* plan, const uint16_t* B,
+                        int64_t ldb, float* C, int64_t ldc, int32_t N,
+                        void* stream);
 
 /* dvals[nnz] = <dY[row(t)], B[col(t)]> for every nonzero t of A (CSR order),
  * walking the forward plan's tiles. */

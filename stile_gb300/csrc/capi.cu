@@ -309,6 +309,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   // each to the least loaded of the kernel's resident CTAs; every CTA's
   // chunks (and their k-steps) are then stored contiguously
   int tc_grid = 0;
+  long max_cta_steps = 0;
   std::vector<int32_t> cta_chunk{0};
   std::vector<int32_t> s_cols, s_nnz;
   std::vector<uint8_t> s_vals;
@@ -334,6 +335,10 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
     for (int b = 0; b < tc_grid; ++b) {
       order.insert(order.end(), owned[b].begin(), owned[b].end());
       cta_chunk.push_back((int32_t)order.size());
+    }
+    while (!heap.empty()) {
+      max_cta_steps = std::max(max_cta_steps, heap.top().first);
+      heap.pop();
     }
     // k-steps in schedule order
     const size_t kb = (size_t)h->tc_kstep_bytes;
@@ -475,6 +480,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   a.tc_chunk_kbeg = (const int*)P(i_ckb);
   a.tc_chunk_nk = (const int*)P(i_ckn);
   a.tc_grid = tc_grid;
+  a.tc_max_cta_steps = (int)max_cta_steps;
   a.tc_cta_chunk = (const int*)P(i_ctac);
   a.tc_chunk_item = (const int*)P(i_cki);
   a.tc_chunk_flags = (const int*)P(i_ckf);
@@ -499,12 +505,21 @@ static int check_dense(long ld, int N, const void* ptr, const char* name) {
   return STILE_OK;
 }
 
-int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float* C, int64_t ldc,
-                   int32_t N, void* stream) {
+static int spmm_run(const StileSpmmPlan* plan, const void* B, bool b_bf16, int64_t ldb, float* C, int64_t ldc,
+                    int32_t N, void* stream) {
   if (!plan) return fail(STILE_E_INVALID, "null plan");
   if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
   int rc;
-  if ((rc = check_dense(ldb, N, B, "B")) != 0) return rc;
+  if (b_bf16) {
+    if (!B) return fail(STILE_E_INVALID, "null B");
+    if (ldb < N || (ldb % 8) != 0)
+      return fail(STILE_E_INVALID, "B (bf16): row stride must be >= N and a multiple of 8");
+    if ((reinterpret_cast<uintptr_t>(B) & 15) != 0) return fail(STILE_E_INVALID, "B: must be 16-byte aligned");
+    if (plan->args.tc_n_chunks && plan->args.tc_mode != STILE_TC_BF16)
+      return fail(STILE_E_UNSUPPORTED, "a bf16 B needs a plan with bf16 tensor tiles");
+  } else if ((rc = check_dense(ldb, N, B, "B")) != 0) {
+    return rc;
+  }
   if ((rc = check_dense(ldc, N, C, "C")) != 0) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e;
@@ -520,7 +535,8 @@ int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float
     if (plan->n_zero_rows) g_launches++;
   }
   stile::SpmmArgs a = plan->args;
-  a.B = B;
+  a.B = static_cast<const float*>(B);
+  a.b_bf16 = b_bf16 ? 1 : 0;
   a.ldb = ldb;
   a.C = C;
   a.ldc = ldc;
@@ -535,6 +551,16 @@ int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float
   if (e != cudaSuccess) return cuda_fail(e, "tensor-core SpMM launch");
   if (a.tc_n_chunks) g_launches++;
   return STILE_OK;
+}
+
+int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float* C, int64_t ldc, int32_t N,
+                   void* stream) {
+  return spmm_run(plan, B, false, ldb, C, ldc, N, stream);
+}
+
+int stile_spmm_run_bf16(const StileSpmmPlan* plan, const uint16_t* B, int64_t ldb, float* C, int64_t ldc,
+                        int32_t N, void* stream) {
+  return spmm_run(plan, B, true, ldb, C, ldc, N, stream);
 }
 
 int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, const float* B,

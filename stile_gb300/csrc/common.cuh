@@ -52,6 +52,39 @@ __device__ __forceinline__ void red_row4(float* row, int f, int N, float4 v) {
   }
 }
 
+// bf16 rows: 16-byte vectors of 8 features
+__device__ __forceinline__ uint4 ldg_u4(const void* p) {
+  return __ldg(reinterpret_cast<const uint4*>(p));
+}
+
+// features [f, f+8) of a bf16 row, masked by N (the row stride is a multiple
+// of 8 elements, so the 16-byte vector is in bounds whenever f < N)
+__device__ __forceinline__ uint4 ld_row8_bf16(const uint16_t* row, int f, int N) {
+  if (f + 7 < N) return ldg_u4(row + f);
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (f < N) {
+    const uint4 t = ldg_u4(row + f);
+    const int live = N - f;  // 1..7 features
+    const uint32_t w[4] = {t.x, t.y, t.z, t.w};
+    uint32_t o[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const uint32_t keep = (2 * i + 1 < live) ? 0xffffffffu : (2 * i < live ? 0x0000ffffu : 0u);
+      o[i] = w[i] & keep;
+    }
+    v = make_uint4(o[0], o[1], o[2], o[3]);
+  }
+  return v;
+}
+
+// 8 bf16 values (feature order: low half of word 0 first) as two float4
+__device__ __forceinline__ void bf16x8_to_f32(uint4 u, float4& lo, float4& hi) {
+  lo = make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
+                   __uint_as_float(u.y & 0xffff0000u));
+  hi = make_float4(__uint_as_float(u.z << 16), __uint_as_float(u.z & 0xffff0000u), __uint_as_float(u.w << 16),
+                   __uint_as_float(u.w & 0xffff0000u));
+}
+
 __device__ __forceinline__ void fma4(float4& acc, float a, float4 b) {
   acc.x = fmaf(a, b.x, acc.x);
   acc.y = fmaf(a, b.y, acc.y);

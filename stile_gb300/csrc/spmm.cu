@@ -17,6 +17,8 @@
 //                        walking the same tiles.
 #include "common.cuh"
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 #include "spmm.cuh"
 
@@ -178,7 +180,6 @@ __device__ __forceinline__ uint32_t a_img_off(int m, int k) {
 // that role, and the others then end at their next (bounded) wait.
 constexpr int kProdWarps = 4;                            // producer warps, one step in flight each
 constexpr int kAccBufs = 4;                              // accumulators of 16 TMEM columns
-constexpr int kWsSlots = kProdWarps;                     // operand slots: warp w fills slot w
 constexpr int kWsThreads = (kProdWarps + 1 + 4) * 32;   // producers, MMA warp, 4 epilogue warps
 
 // Per-mode layout.  Split-bf16 (fp32-level accuracy) keeps hi and lo images
@@ -186,22 +187,30 @@ constexpr int kWsThreads = (kProdWarps + 1 + 4) * 32;   // producers, MMA warp, 
 // issues three MMAs per step (hi*hi + hi*lo + lo*hi); its accumulator is
 // drained into the epilogue's fp32 registers every kGroup steps, which
 // bounds the tensor core's accumulation chain.
-template <int MODE>
+//
+// A bf16 B (kIn16) needs no conversion: the producers copy its rows with
+// cp.async straight into the swizzled A image of the slot (each 16-byte
+// chunk of a row is 8 features, one chunk of the layout), so there is no raw
+// stage and every producer warp keeps two steps in flight in its two slots.
+template <int MODE, bool kIn16 = false>
 struct WsCfg {
   static constexpr bool kSplit = MODE == STILE_TC_SPLIT_BF16;
+  static constexpr int kSlots = kIn16 ? 2 * kProdWarps : kProdWarps;  // warp w fills slots w (+ kProdWarps)
   static constexpr uint32_t kVals = kSplit ? 2 * kBStage : kBStage;   // value image(s) per step
   static constexpr uint32_t kAImg = kSplit ? 2 * kAStage : kAStage;   // A image(s) per step
   static constexpr uint32_t kSlot = kAImg + 1024;                     // + value images, 1024-aligned
-  static constexpr uint32_t kRaw = kRawRows + kVals;                  // 16 fp32 rows + value image(s)
-  static constexpr uint32_t kBytes = 1024 + kWsSlots * kSlot + kProdWarps * kRaw + 256;
+  static constexpr uint32_t kRaw = kIn16 ? 0 : kRawRows + kVals;      // 16 fp32 rows + value image(s)
+  static constexpr uint32_t kBytes = 1024 + kSlots * kSlot + kProdWarps * kRaw + 256;
   static constexpr int kCtas = kSplit ? 3 : 4;                        // resident CTAs per SM
   static constexpr int kGroup = kSplit ? 4 : (1 << 30);               // k-steps per accumulator drain
+  static_assert(!(kIn16 && MODE != STILE_TC_BF16), "a bf16 B feeds bf16 MMAs");
 };
 
 // kFull: every 128-feature slice is complete (N % 128 == 0)
-template <int MODE, bool kFull>
-__global__ void __launch_bounds__(kWsThreads, WsCfg<MODE>::kCtas) spmm_tc_ws_kernel(SpmmArgs p) {
-  using W = WsCfg<MODE>;
+template <int MODE, bool kFull, bool kIn16>
+__global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc_ws_kernel(SpmmArgs p) {
+  using W = WsCfg<MODE, kIn16>;
+  constexpr int kWsSlots = W::kSlots;
   extern __shared__ uint8_t smem_raw[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t slots = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -241,8 +250,11 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE>::kCtas) spmm_tc_ws_ker
   const int nc = __ldg(p.tc_cta_chunk + blockIdx.x + 1) - cb;
   const int s_beg = nc > 0 ? __ldg(p.tc_chunk_kbeg + cb) : 0;
   const int S = nc > 0 ? __ldg(p.tc_chunk_kbeg + cb + nc - 1) + __ldg(p.tc_chunk_nk + cb + nc - 1) - s_beg : 0;
-  const int nf = p.n_fchunks;
-  const long T = (long)S * nf;  // this CTA's k-steps over all slices
+  // feature slices of this CTA: blockIdx.y takes [sl0, sl0 + nf) (a wide B
+  // spreads its slices over more CTAs than the chunk schedule has)
+  const int sl0 = blockIdx.y * p.tc_slice_per;
+  const int nf = min(p.tc_slice_per, p.n_fchunks - sl0);
+  const long T = (long)S * nf;  // this CTA's k-steps over its slices
   const int n_units = nc * nf;
   const int N = p.N;
   bool ok = true;
@@ -256,11 +268,72 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE>::kCtas) spmm_tc_ws_ker
     int loc = 0, f0 = 0;
     if (g < T) {
       loc = warp % S;
-      f0 = (warp / S) * 128;
+      f0 = (sl0 + warp / S) * 128;
     }
     auto step_cols = [&](long gg, int l) {
       return (gg < T && lane < 16) ? __ldg(p.tc_cols + (long)(s_beg + l) * 16 + lane) : 0;
     };
+    // (loc, f0) of this warp's step after the one at (l, ff)
+    auto next_of = [&](int l, int ff, int& ln, int& fn) {
+      ln = l + kProdWarps;
+      fn = ff;
+      while (ln >= S) {
+        ln -= S;
+        fn += 128;
+      }
+    };
+    if constexpr (kIn16) {
+      const uint16_t* B16 = reinterpret_cast<const uint16_t*>(p.B);
+      const int ch = lane & 15, rh = lane >> 4;  // this lane's 16-byte chunk (8 features) and row parity
+      // the step at (l, ff) into `slot`: rows 2j + rh, features ff + 8 ch ..
+      auto issue16 = [&](int cols, int l, int ff, int slot) {
+        const uint32_t sa = slots + slot * W::kSlot;
+        const int f = ff + 8 * ch;
+        const uint32_t bytes = kFull ? 16u : ((f + 8 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 2u : 0u));
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int r = 2 * j + rh;
+          const int col = __shfl_sync(0xffffffffu, cols, r);
+          const uint16_t* row = B16 + (long)col * p.ldb;
+          cp_async16(sa + a_img_off(8 * ch, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
+        }
+        cp_async16(sa + kAStage + lane * 16, vals + (long)(s_beg + l) * kBStage + lane * 16, 16u);
+        cp_async_commit();
+      };
+      // steps g and g + kProdWarps in flight; once g has landed and the MMA
+      // that read its slot last time is done, step g + 2 kProdWarps refills it
+      int l1 = 0, f1 = 0;  // the step after g
+      next_of(loc, f0, l1, f1);
+      if (g < T) issue16(step_cols(g, loc), loc, f0, (int)(g % kWsSlots));
+      if (g + kProdWarps < T) issue16(step_cols(g + kProdWarps, l1), l1, f1, (int)((g + kProdWarps) % kWsSlots));
+#pragma unroll 1
+      for (; g < T; g += kProdWarps) {
+        int l2, f2;
+        next_of(l1, f1, l2, f2);
+        const long g2 = g + 2 * kProdWarps;
+        const int cols2 = step_cols(g2, l2);
+        if (g + kProdWarps < T) cp_async_wait<1>();
+        else cp_async_wait<0>();
+        fence_proxy_async_smem();
+        __syncwarp();
+        const int slot = (int)(g % kWsSlots);
+        if (lane == 0) mbar_arrive(full0 + 8 * slot);
+        if (g2 < T) {
+          const uint32_t par = (uint32_t)(g / kWsSlots) & 1u;
+          bool got = true;
+          if (lane == 0) got = mbar_wait_bounded(empty0 + 8 * slot, par);
+          if (!__shfl_sync(0xffffffffu, got, 0)) {
+            ok = false;
+            break;
+          }
+          if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par);  // completed: returns at once
+          issue16(cols2, l2, f2, slot);
+        }
+        l1 = l2;
+        f1 = f2;
+      }
+      cp_async_wait<0>();
+    } else {
     auto issue = [&](int cols, int l, int ff) {
       const int f = ff + 4 * lane;
       const uint32_t bytes = kFull ? 16u : ((f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u));
@@ -280,11 +353,8 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE>::kCtas) spmm_tc_ws_ker
     for (; g < T; g += kProdWarps) {
       // this warp's next step and its column ids (used after the convert)
       const long gn = g + kProdWarps;
-      int locn = loc + kProdWarps, f0n = f0;
-      while (locn >= S) {
-        locn -= S;
-        f0n += 128;
-      }
+      int locn, f0n;
+      next_of(loc, f0, locn, f0n);
       const int coln = step_cols(gn, locn);
       cp_async_wait<0>();
       const int slot = (int)(g % kWsSlots);
@@ -329,6 +399,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE>::kCtas) spmm_tc_ws_ker
       f0 = f0n;
     }
     cp_async_wait<0>();
+    }
   } else if (warp == kProdWarps) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
@@ -408,7 +479,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE>::kCtas) spmm_tc_ws_ker
       }
       if (!ok) break;
       const int c = cb + t % nc;
-      const int f = (t / nc) * 128 + 32 * quarter + lane;
+      const int f = (sl0 + t / nc) * 128 + 32 * quarter + lane;
       if (kFull || f < N) {
         const int item = __ldg(p.tc_chunk_item + c);
         const bool atomic = (__ldg(p.tc_chunk_flags + c) & 1) != 0;
@@ -443,7 +514,9 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE>::kCtas) spmm_tc_ws_ker
 // and few registers leave room for many warps per SM.
 // kFull: N % (4 * VEC * LPR) == 0, every lane's features are in range.
 // kOff32: every B row offset col * ldb fits in 32 bits.
-template <int LPR, int VEC, bool kFull, bool kOff32>
+// kSpanY: blockIdx.y takes features [y span, (y + 1) span) (a wide B over
+// few groups; span = p.ell_fc_span, a multiple of the pass width).
+template <int LPR, int VEC, bool kFull, bool kOff32, bool kSpanY = false>
 __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   constexpr int kBatch = 4 / VEC;  // entries per batch: 4 float4 in flight per lane
   static_assert(VEC == 1 || kFull, "wide lanes need full feature slices");
@@ -457,7 +530,8 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   const int N = p.N;
   const int ldb32 = (int)p.ldb;
   auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, 0); };
-  for (int fc = 0; fc < N; fc += 4 * VEC * LPR) {
+  for (int fc = kSpanY ? blockIdx.y * p.ell_fc_span : 0;
+       fc < (kSpanY ? min(N, (int)(blockIdx.y + 1) * p.ell_fc_span) : N); fc += 4 * VEC * LPR) {
     const int f = fc + 4 * VEC * sl;
     const float* Bf = p.B + f;
     float4 acc[VEC];
@@ -502,6 +576,78 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
               }
               acc[w] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
+          }
+        }
+      }
+      mcur = mnext;
+    }
+  }
+}
+
+// The same entry stream over a bf16 B: each lane covers 8 features with one
+// 16-byte load (half the gathered bytes of fp32 rows), converts them to
+// fp32 and accumulates in fp32; 4 entries' rows in flight per lane.
+template <int LPR, bool kFull, bool kOff32, bool kSpanY = false>
+__global__ void __launch_bounds__(256, 4) spmm_ell_seg_bf16_kernel(SpmmArgs p) {
+  constexpr int kBatch = 4;
+  static_assert(LPR % kBatch == 0, "batches stay inside one record block");
+  const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
+  const unsigned mask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
+  const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
+  if (g >= p.ell_n_groups) return;  // the whole sub-group leaves together
+  const int p0 = __ldg(p.ell_group_ptr + g);
+  const int n = __ldg(p.ell_group_ptr + g + 1) - p0;
+  const int4* __restrict__ ent = p.ell_entry + p0;
+  const uint16_t* __restrict__ B16 = reinterpret_cast<const uint16_t*>(p.B);
+  const int N = p.N;
+  const int ldb32 = (int)p.ldb;
+  auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, 0); };
+  for (int fc = kSpanY ? blockIdx.y * p.ell_fc_span : 0;
+       fc < (kSpanY ? min(N, (int)(blockIdx.y + 1) * p.ell_fc_span) : N); fc += 8 * LPR) {
+    const int f = fc + 8 * sl;
+    float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
+    int4 mcur = rec(sl);
+#pragma unroll 1
+    for (int c0 = 0; c0 < n; c0 += LPR) {
+      const int4 mnext = rec(c0 + LPR + sl);
+#pragma unroll 1
+      for (int b0 = c0; b0 < min(n, c0 + LPR); b0 += kBatch) {
+        uint4 bv[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+          const int c = __shfl_sync(mask, mcur.x, b0 - c0 + u, LPR);
+          // records past n hold column 0: a valid row, multiplied by 0
+          const uint16_t* row = kOff32 ? B16 + (unsigned)(c * ldb32) : B16 + (long)c * p.ldb;
+          bv[u] = kFull ? ldg_u4(row + f) : ld_row8_bf16(row, f, N);
+        }
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+          const float v = __int_as_float(__shfl_sync(mask, mcur.y, b0 - c0 + u, LPR));
+          const int ce = __shfl_sync(mask, mcur.z, b0 - c0 + u, LPR);
+          float4 lo, hi;
+          bf16x8_to_f32(bv[u], lo, hi);
+          fma4(acc0, v, lo);
+          fma4(acc1, v, hi);
+          if (ce & 1) {
+            const int code = ce >> 1;
+            float* row = p.C + (long)(code >= 0 ? code : -code - 1) * p.ldc;
+            if (kFull) {
+              if (code >= 0) {
+                *reinterpret_cast<float4*>(row + f) = acc0;
+                *reinterpret_cast<float4*>(row + f + 4) = acc1;
+              } else {
+                atomicAdd(reinterpret_cast<float4*>(row + f), acc0);
+                atomicAdd(reinterpret_cast<float4*>(row + f + 4), acc1);
+              }
+            } else if (code >= 0) {
+              st_row4(row, f, N, acc0);
+              st_row4(row, f + 4, N, acc1);
+            } else {
+              red_row4(row, f, N, acc0);
+              red_row4(row, f + 4, N, acc1);
+            }
+            acc0 = make_float4(0.f, 0.f, 0.f, 0.f);
+            acc1 = acc0;
           }
         }
       }
@@ -638,10 +784,10 @@ static cudaError_t resident_ctas(K kernel, int threads, size_t smem, int* sms, i
   return cudaSuccess;
 }
 
-template <int MODE, bool kFull>
+template <int MODE, bool kFull, bool kIn16 = false>
 static cudaError_t launch_ws_t(const SpmmArgs& p, cudaStream_t st) {
-  auto k = spmm_tc_ws_kernel<MODE, kFull>;
-  constexpr uint32_t kWsBytes = WsCfg<MODE>::kBytes;
+  auto k = spmm_tc_ws_kernel<MODE, kFull, kIn16>;
+  constexpr uint32_t kWsBytes = WsCfg<MODE, kIn16>::kBytes;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWsBytes);
   if (e != cudaSuccess) return e;
   // shared memory for the resident CTAs; the rest of the unified L1 /
@@ -649,23 +795,59 @@ static cudaError_t launch_ws_t(const SpmmArgs& p, cudaStream_t st) {
   e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
   if (p.tc_n_chunks == 0 || p.tc_grid == 0) return cudaSuccess;
-  k<<<p.tc_grid, kWsThreads, kWsBytes, st>>>(p);
+  k<<<dim3(p.tc_grid, (p.n_fchunks + p.tc_slice_per - 1) / p.tc_slice_per), kWsThreads, kWsBytes, st>>>(p);
   return cudaGetLastError();
 }
 
+// resident CTAs of the tensor-core kernel on the current device, computed
+// once per (device, split mode)
 int tc_persistent_ctas(int mode) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  const std::pair<int, int> key{dev, mode == STILE_TC_SPLIT_BF16 ? 1 : 0};
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
   int sms = 0, per_sm = 0;
   const cudaError_t e =
       mode == STILE_TC_SPLIT_BF16
-          ? resident_ctas(spmm_tc_ws_kernel<STILE_TC_SPLIT_BF16, true>, kWsThreads, WsCfg<STILE_TC_SPLIT_BF16>::kBytes,
-                          &sms, &per_sm)
-          : resident_ctas(spmm_tc_ws_kernel<STILE_TC_BF16, true>, kWsThreads, WsCfg<STILE_TC_BF16>::kBytes, &sms,
-                          &per_sm);
+          ? resident_ctas(spmm_tc_ws_kernel<STILE_TC_SPLIT_BF16, true, false>, kWsThreads,
+                          WsCfg<STILE_TC_SPLIT_BF16>::kBytes, &sms, &per_sm)
+          : resident_ctas(spmm_tc_ws_kernel<STILE_TC_BF16, true, false>, kWsThreads, WsCfg<STILE_TC_BF16>::kBytes,
+                          &sms, &per_sm);
   if (e != cudaSuccess) return 0;
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = sms * per_sm;
   return sms * per_sm;
 }
 
-cudaError_t launch_tc(const SpmmArgs& p, cudaStream_t st) {
+// Feature slices per CTA of the tensor-core grid.  The chunk schedule
+// balances k-steps over tc_grid CTAs; with nf slices a CTA's work is its
+// k-steps times nf.  When that makes the longest CTA much longer than the
+// average over all resident CTAs (a wide B over few chunks), the slices are
+// split over grid.y so that no CTA holds more than about the average.
+static int tc_slices_per_cta(const SpmmArgs& p) {
+  const int nf = p.n_fchunks;
+  if (nf <= 1 || p.tc_max_cta_steps <= 0) return nf;
+  const int resident = tc_persistent_ctas(p.tc_mode);
+  if (resident <= 0) return nf;
+  const long avg = ((long)p.tc_n_ksteps * nf + resident - 1) / resident;  // step-slices per CTA
+  const long per = avg / p.tc_max_cta_steps;
+  return (int)std::max(1L, std::min<long>(per, nf));
+}
+
+cudaError_t launch_tc(const SpmmArgs& args, cudaStream_t st) {
+  SpmmArgs p = args;
+  p.tc_slice_per = tc_slices_per_cta(p);
+  if (p.b_bf16) {
+    if (p.tc_mode != STILE_TC_BF16) return cudaErrorNotSupported;
+    return p.N % 128 == 0 ? launch_ws_t<STILE_TC_BF16, true, true>(p, st)
+                          : launch_ws_t<STILE_TC_BF16, false, true>(p, st);
+  }
   switch (p.tc_mode) {
     case STILE_TC_F16:
       return p.N % 128 == 0 ? launch_ws_t<STILE_TC_F16, true>(p, st) : launch_ws_t<STILE_TC_F16, false>(p, st);
@@ -677,25 +859,72 @@ cudaError_t launch_tc(const SpmmArgs& p, cudaStream_t st) {
   }
 }
 
+// Blocks of the ELL kernels: x over groups; when that leaves the GPU short
+// of blocks (a wide B over few groups), y splits the feature passes, up to
+// about ten blocks per SM in all.
+// (sets p.ell_fc_span to the features of one block row)
+static dim3 ell_grid(SpmmArgs& p, int groups_per_block, int pass) {
+  const long gx = (p.ell_n_groups + groups_per_block - 1) / groups_per_block;
+  const int n_pass = (p.N + pass - 1) / pass;
+  const long want = 152L * 10;
+  long gy = gx >= want ? 1 : (want + gx - 1) / gx;
+  gy = std::max(1L, std::min<long>(gy, n_pass));
+  const int per = (int)((n_pass + gy - 1) / gy);
+  gy = (n_pass + per - 1) / per;
+  p.ell_fc_span = per * pass;
+  return dim3((unsigned)gx, (unsigned)gy, 1);
+}
+
 template <int LPR>
 struct EllLaunch {
-  static cudaError_t run(const SpmmArgs& p, cudaStream_t st) {
+  static cudaError_t run(SpmmArgs p, cudaStream_t st) {
     if (p.ell_n_groups == 0) return cudaSuccess;
-    const long groups_per_block = 256 / LPR;
-    const long grid = (p.ell_n_groups + groups_per_block - 1) / groups_per_block;
-    spmm_ell_seg_kernel<LPR, 1, false, false><<<(unsigned)grid, 256, 0, st>>>(p);
+    const dim3 grid = ell_grid(p, 256 / LPR, 4 * LPR);
+    if (grid.y > 1) spmm_ell_seg_kernel<LPR, 1, false, false, true><<<grid, 256, 0, st>>>(p);
+    else spmm_ell_seg_kernel<LPR, 1, false, false><<<grid, 256, 0, st>>>(p);
     return cudaGetLastError();
   }
 };
 
-cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st) {
-  if (p.ell_n_groups == 0) return cudaSuccess;
+template <int LPR>
+struct EllBf16Launch {
+  static cudaError_t run(SpmmArgs p, cudaStream_t st) {
+    const dim3 grid = ell_grid(p, 256 / LPR, 8 * LPR);
+    if (grid.y > 1) spmm_ell_seg_bf16_kernel<LPR, false, false, true><<<grid, 256, 0, st>>>(p);
+    else spmm_ell_seg_bf16_kernel<LPR, false, false><<<grid, 256, 0, st>>>(p);
+    return cudaGetLastError();
+  }
+};
+
+static int lpr_for_bf16(int N) {
+  const int lanes = (N + 7) / 8;
+  if (lanes >= 32) return 32;
+  int l = 4;
+  while (l < lanes) l <<= 1;
+  return l;
+}
+
+cudaError_t launch_ell(const SpmmArgs& args, cudaStream_t st) {
+  if (args.ell_n_groups == 0) return cudaSuccess;
+  SpmmArgs p = args;
+  const bool off32 = (long)p.K * p.ldb < (1L << 31);
+  if (p.b_bf16) {
+    if (p.N % 128 == 0) {
+      // 16-lane sub-groups of 8 features per lane (two groups per warp)
+      const dim3 grid = ell_grid(p, 16, 128);
+      if (grid.y > 1) spmm_ell_seg_bf16_kernel<16, true, false, true><<<grid, 256, 0, st>>>(p);
+      else if (off32) spmm_ell_seg_bf16_kernel<16, true, true><<<grid, 256, 0, st>>>(p);
+      else spmm_ell_seg_bf16_kernel<16, true, false><<<grid, 256, 0, st>>>(p);
+      return cudaGetLastError();
+    }
+    return dispatch_lpr<EllBf16Launch>(lpr_for_bf16(p.N), p, st);
+  }
   if (p.N % 128 == 0) {
     // 16-lane sub-groups of 8 features per lane (two groups per warp)
-    const long grid = (p.ell_n_groups + 15) / 16;
-    const bool off32 = (long)p.K * p.ldb < (1L << 31);
-    if (off32) spmm_ell_seg_kernel<16, 2, true, true><<<(unsigned)grid, 256, 0, st>>>(p);
-    else spmm_ell_seg_kernel<16, 2, true, false><<<(unsigned)grid, 256, 0, st>>>(p);
+    const dim3 grid = ell_grid(p, 16, 128);
+    if (grid.y > 1) spmm_ell_seg_kernel<16, 2, true, false, true><<<grid, 256, 0, st>>>(p);
+    else if (off32) spmm_ell_seg_kernel<16, 2, true, true><<<grid, 256, 0, st>>>(p);
+    else spmm_ell_seg_kernel<16, 2, true, false><<<grid, 256, 0, st>>>(p);
     return cudaGetLastError();
   }
   return dispatch_lpr<EllLaunch>(lpr_for(p.N), p, st);

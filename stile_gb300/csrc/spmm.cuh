@@ -10,8 +10,12 @@ namespace stile {
 
 struct SpmmArgs {
   // dense operands
-  const float* B;
+  const float* B;  // fp32, or bf16 bits when b_bf16 (ldb in elements either way)
   long ldb;
+  int b_bf16;
+  int ell_fc_span;  // features per ELL block row (blockIdx.y); set by the launcher
+  int tc_slice_per;      // 128-feature slices per tensor-core CTA (blockIdx.y); set by the launcher
+  int tc_max_cta_steps;  // most k-steps the chunk schedule gives one CTA
   float* C;
   long ldc;
   int N;

@@ -44,6 +44,26 @@ def dense_operand(x: torch.Tensor, name="B"):
     return x, ld
 
 
+def dense_operand_bf16(x: torch.Tensor, name="B"):
+    """bf16, CUDA, row-major with a row stride that is a multiple of 8 and a
+    16-byte aligned base; copies only when needed."""
+    _require_cuda(x, name)
+    if x.dtype != torch.bfloat16:
+        raise TypeError(f"{name} must be bfloat16")
+    if x.dim() != 2:
+        raise ValueError(f"{name} must be 2-D")
+    rows, cols = x.shape
+    ld = x.stride(0)
+    ok = x.stride(1) == 1 and ld >= cols and ld % 8 == 0 and x.data_ptr() % 16 == 0
+    if not ok:
+        ldp = (cols + 7) // 8 * 8
+        buf = torch.zeros((rows, ldp), dtype=torch.bfloat16, device=x.device)
+        buf[:, :cols] = x
+        x = buf[:, :cols]
+        ld = ldp
+    return x, ld
+
+
 def new_output(rows, cols, device):
     ldp = (cols + 3) // 4 * 4
     buf = torch.empty((rows, ldp), dtype=torch.float32, device=device)
@@ -94,7 +114,10 @@ class DeviceSpmmPlan:
         self.handle = handle
 
     def run(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
-        B, ldb = dense_operand(B, "B")
+        """C = A @ B in fp32; B is fp32 or bf16 (a bf16 B is read as is:
+        half the gathered bytes, fp32 accumulation)."""
+        bf16 = B.dtype == torch.bfloat16
+        B, ldb = dense_operand_bf16(B, "B") if bf16 else dense_operand(B, "B")
         if B.shape[0] != self.K:
             raise ValueError(f"B has {B.shape[0]} rows, the plan has K={self.K}")
         N = B.shape[1]
@@ -102,8 +125,9 @@ class DeviceSpmmPlan:
             out, ldc = new_output(self.M, N, B.device)
         else:
             ldc = out.stride(0)
-        _lib.check(self.lib.stile_spmm_run(self.handle, B.data_ptr(), ldb, out.data_ptr(), ldc, N, _stream()),
-                   "stile_spmm_run")
+        fn = self.lib.stile_spmm_run_bf16 if bf16 else self.lib.stile_spmm_run
+        _lib.check(fn(self.handle, B.data_ptr(), ldb, out.data_ptr(), ldc, N, _stream()),
+                   "stile_spmm_run_bf16" if bf16 else "stile_spmm_run")
         return out
 
     def dvals(self, dY: torch.Tensor, B: torch.Tensor) -> torch.Tensor:

@@ -9,6 +9,7 @@ from golden_plan import plan_from_fixture
 from gpu_util import random_values, umma_layout_ok
 import oracle.semantics as S
 from stile_gb300 import device as D
+from stile_gb300 import synthetic as syn
 from stile_gb300.ops import CsrMatrix, DeviceSpmmPlan
 
 pytestmark = pytest.mark.gpu
@@ -131,3 +132,40 @@ def test_csr_kernel_empty_rows_and_empty_matrix():
     assert np.array_equal(out, np.asarray(A @ B, dtype=np.float32))
     Z = sp.csr_matrix((0, 8))
     assert CsrMatrix(Z).spmm(torch.as_tensor(B, device="cuda")).shape == (0, 4)
+
+
+@pytest.mark.parametrize("N", [128, 41, 4096])
+def test_bf16_dense_operand(N):
+    """A bf16 B is read as is (row tiles convert it to fp32, tensor tiles
+    feed it to the MMA): against the fp64 product with the same bf16 values,
+    the row-tile-only plan is fp32-exact and the hybrid plan is within the
+    bf16 tensor-tile tolerance."""
+    from stile_gb300 import workloads as W
+    from stile_gb300.api import PlanConfig, SpmmOperator
+    import torch
+    if N == 4096:
+        A = W.pruned(False).A
+    else:
+        A = syn.community_graph(n=8192, target_nnz=90_000, seed=3)
+    B = torch.randn((A.shape[1], N), device="cuda").to(torch.bfloat16)
+    Bf = B.float().cpu().numpy()
+    ref = S.spmm_fp64(A, Bf)
+    hyb = SpmmOperator(A, N, PlanConfig(tc_mode=D.TC_BF16))
+    assert hyb.device_layout.stats()["tc_ksteps"] > 0
+    C = hyb(B).cpu().numpy()
+    assert S.rel_fro(C, ref) <= 1e-2
+    assert S.rel_fro(C, hyb(B.float()).cpu().numpy()) <= 1e-5   # same products as the fp32 B path
+    ell = SpmmOperator(A, N, PlanConfig(tc_mode=D.TC_BF16, only_ELL=True))
+    assert S.rel_fro(ell(B).cpu().numpy(), ref) <= 1e-5
+    assert hyb.handle.error_flag() == 0 and ell.handle.error_flag() == 0
+
+
+def test_bf16_dense_operand_needs_bf16_tensor_tiles():
+    from stile_gb300.api import PlanConfig, SpmmOperator
+    import torch
+    A = syn.community_graph(n=4096, target_nnz=40_000, seed=4)
+    op = SpmmOperator(A, 64, PlanConfig(tc_mode=D.TC_SPLIT_BF16))
+    assert op.device_layout.stats()["tc_ksteps"] > 0
+    B = torch.randn((A.shape[1], 64), device="cuda").to(torch.bfloat16)
+    with pytest.raises(RuntimeError, match="bf16 tensor tiles"):
+        op(B)
