@@ -192,15 +192,21 @@ constexpr int kWsThreads = (kProdWarps + 1 + 4) * 32;   // producers, MMA warp, 
 // cp.async straight into the swizzled A image of the slot (each 16-byte
 // chunk of a row is 8 features, one chunk of the layout), so there is no raw
 // stage and every producer warp keeps two steps in flight in its two slots.
+// Slot s holds the A image(s) at a_off(s) (1024-aligned) and the value
+// image(s) at v_off(s): A images first, then all value images.
 template <int MODE, bool kIn16 = false>
 struct WsCfg {
   static constexpr bool kSplit = MODE == STILE_TC_SPLIT_BF16;
-  static constexpr int kSlots = kIn16 ? 2 * kProdWarps : kProdWarps;  // warp w fills slots w (+ kProdWarps)
+  static constexpr int kSlots = kIn16 ? 3 * kProdWarps : kProdWarps;  // warp w fills slots w, w + 4, ..
   static constexpr uint32_t kVals = kSplit ? 2 * kBStage : kBStage;   // value image(s) per step
   static constexpr uint32_t kAImg = kSplit ? 2 * kAStage : kAStage;   // A image(s) per step
-  static constexpr uint32_t kSlot = kAImg + 1024;                     // + value images, 1024-aligned
+  static constexpr uint32_t kSlotBytes = kSlots * (kAImg + kVals);
   static constexpr uint32_t kRaw = kIn16 ? 0 : kRawRows + kVals;      // 16 fp32 rows + value image(s)
-  static constexpr uint32_t kBytes = 1024 + kSlots * kSlot + kProdWarps * kRaw + 256;
+  // full / empty barrier per slot, full / empty per accumulator, drain, TMEM address
+  static constexpr uint32_t kBarBytes = (16 * kSlots + 16 * kAccBufs + 16 + 63) / 64 * 64;
+  static constexpr uint32_t kBytes = 1024 + kSlotBytes + kProdWarps * kRaw + kBarBytes;
+  static __device__ __forceinline__ uint32_t a_off(int s) { return (uint32_t)s * kAImg; }
+  static __device__ __forceinline__ uint32_t v_off(int s) { return kSlots * kAImg + (uint32_t)s * kVals; }
   static constexpr int kCtas = kSplit ? 3 : 4;                        // resident CTAs per SM
   static constexpr int kGroup = kSplit ? 4 : (1 << 30);               // k-steps per accumulator drain
   static_assert(!(kIn16 && MODE != STILE_TC_BF16), "a bf16 B feeds bf16 MMAs");
@@ -214,7 +220,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
   extern __shared__ uint8_t smem_raw[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t slots = (smem_u32(smem_raw) + 1023u) & ~1023u;
-  const uint32_t ring = slots + kWsSlots * W::kSlot;
+  const uint32_t ring = slots + W::kSlotBytes;
   const uint32_t bars = ring + kProdWarps * W::kRaw;
   // full[kWsSlots], empty[kWsSlots], acc_full[kAccBufs], acc_empty[kAccBufs], drain
   const uint32_t full0 = bars, empty0 = bars + 8 * kWsSlots;
@@ -287,7 +293,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
       const int ch = lane & 15, rh = lane >> 4;  // this lane's 16-byte chunk (8 features) and row parity
       // the step at (l, ff) into `slot`: rows 2j + rh, features ff + 8 ch ..
       auto issue16 = [&](int cols, int l, int ff, int slot) {
-        const uint32_t sa = slots + slot * W::kSlot;
+        const uint32_t sa = slots + W::a_off(slot);
         const int f = ff + 8 * ch;
         const uint32_t bytes = kFull ? 16u : ((f + 8 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 2u : 0u));
 #pragma unroll
@@ -297,28 +303,33 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
           const uint16_t* row = B16 + (long)col * p.ldb;
           cp_async16(sa + a_img_off(8 * ch, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
         }
-        cp_async16(sa + kAStage + lane * 16, vals + (long)(s_beg + l) * kBStage + lane * 16, 16u);
+        cp_async16(slots + W::v_off(slot) + lane * 16, vals + (long)(s_beg + l) * kBStage + lane * 16, 16u);
         cp_async_commit();
       };
-      // steps g and g + kProdWarps in flight; once g has landed and the MMA
-      // that read its slot last time is done, step g + 2 kProdWarps refills it
-      int l1 = 0, f1 = 0;  // the step after g
-      next_of(loc, f0, l1, f1);
-      if (g < T) issue16(step_cols(g, loc), loc, f0, (int)(g % kWsSlots));
-      if (g + kProdWarps < T) issue16(step_cols(g + kProdWarps, l1), l1, f1, (int)((g + kProdWarps) % kWsSlots));
+      // kD steps of this warp in flight; once the oldest (g) has landed and
+      // the MMA that read its slot last time is done, step g + kD kProdWarps
+      // refills that slot
+      constexpr int kD = kWsSlots / kProdWarps;
+      static_assert(kD >= 1 && kD <= 3, "one to three steps in flight per warp");
+      long gi = g;  // the next step to issue, at (li, fi)
+      int li = loc, fi = f0;
+      for (int d = 0; d < kD && gi < T; ++d) {
+        issue16(step_cols(gi, li), li, fi, (int)(gi % kWsSlots));
+        gi += kProdWarps;
+        next_of(li, fi, li, fi);
+      }
 #pragma unroll 1
       for (; g < T; g += kProdWarps) {
-        int l2, f2;
-        next_of(l1, f1, l2, f2);
-        const long g2 = g + 2 * kProdWarps;
-        const int cols2 = step_cols(g2, l2);
-        if (g + kProdWarps < T) cp_async_wait<1>();
+        const int cols_i = step_cols(gi, li);
+        const long pend = (gi - g) / kProdWarps;  // this warp's steps in flight, g the oldest
+        if (pend >= 3) cp_async_wait<2>();
+        else if (pend == 2) cp_async_wait<1>();
         else cp_async_wait<0>();
         fence_proxy_async_smem();
         __syncwarp();
         const int slot = (int)(g % kWsSlots);
         if (lane == 0) mbar_arrive(full0 + 8 * slot);
-        if (g2 < T) {
+        if (gi < T) {
           const uint32_t par = (uint32_t)(g / kWsSlots) & 1u;
           bool got = true;
           if (lane == 0) got = mbar_wait_bounded(empty0 + 8 * slot, par);
@@ -327,10 +338,10 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
             break;
           }
           if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par);  // completed: returns at once
-          issue16(cols2, l2, f2, slot);
+          issue16(cols_i, li, fi, slot);
+          gi += kProdWarps;
+          next_of(li, fi, li, fi);
         }
-        l1 = l2;
-        f1 = f2;
       }
       cp_async_wait<0>();
     } else {
@@ -368,7 +379,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
         }
         if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par);  // completed: returns at once
       }
-      const uint32_t sa = slots + slot * W::kSlot;
+      const uint32_t sa = slots + W::a_off(slot);
 #pragma unroll
       for (int r = 0; r < 16; ++r) {
         const uint4 raw = ld_shared_v4(stage + r * 512 + lane * 16);
@@ -390,7 +401,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
       }
 #pragma unroll
       for (int c = lane; c < (int)(W::kVals / 16); c += 32)
-        st_shared_v4(sa + W::kAImg + c * 16, ld_shared_v4(stage + kRawRows + c * 16));
+        st_shared_v4(slots + W::v_off(slot) + c * 16, ld_shared_v4(stage + kRawRows + c * 16));
       fence_proxy_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(full0 + 8 * slot);
@@ -428,12 +439,12 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
               break;
             }
             tc_fence_after();
-            const uint32_t sa = slots + slot * W::kSlot;
+            const uint32_t sa = slots + W::a_off(slot), sv = slots + W::v_off(slot);
             const uint64_t a_hi = smem_desc(sa, kALbo, kASbo, kSwizzle128B);
-            const uint64_t v_hi = smem_desc(sa + W::kAImg, kBLbo, kBSbo, kSwizzleNone);
+            const uint64_t v_hi = smem_desc(sv, kBLbo, kBSbo, kSwizzleNone);
             umma_f16(d, a_hi, v_hi, idesc, s > s0 ? 1u : 0u);
             if (W::kSplit) {
-              umma_f16(d, a_hi, smem_desc(sa + W::kAImg + kBStage, kBLbo, kBSbo, kSwizzleNone), idesc, 1u);
+              umma_f16(d, a_hi, smem_desc(sv + kBStage, kBLbo, kBSbo, kSwizzleNone), idesc, 1u);
               umma_f16(d, smem_desc(sa + kAStage, kALbo, kASbo, kSwizzle128B), v_hi, idesc, 1u);
             }
             umma_commit(empty0 + 8 * slot);
