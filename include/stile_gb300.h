@@ -162,10 +162,24 @@ int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy,
                      const float* B, int64_t ldb, float* dvals, int32_t N,
                      void* stream);
 
+/* dvals with B in bf16 (the operand of stile_spmm_run_bf16; dY fp32).  No
+ * counterpart in the reference, like stile_spmm_dvals. */
+int stile_spmm_dvals_bf16(const StileSpmmPlan* plan, const float* dY,
+                          int64_t lddy, const uint16_t* B, int64_t ldb,
+                          float* dvals, int32_t N, void* stream);
+
 /* out[nnz] = <X[row(t)], Y[col(t)]> (fp32), CSR order of the mask. */
 int stile_sddmm_run(const StileSddmmPlan* plan, const float* X, int64_t ldx,
                     const float* Y, int64_t ldy, float* out, int32_t F,
                     void* stream);
+
+/* The same with X and Y in bf16 (raw bfloat16 bits, row strides multiples
+ * of 8, 16-byte aligned; products and sums in fp32).  Counterpart: the
+ * fused SDDMM built for 16-bit inputs (measure_latency_BSDDMM with
+ * dtype "float16", MY_sparse/my_fuse_formats.py:4292-4330). */
+int stile_sddmm_run_bf16(const StileSddmmPlan* plan, const uint16_t* X,
+                         int64_t ldx, const uint16_t* Y, int64_t ldy,
+                         float* out, int32_t F, void* stream);
 
 /* Plain CSR SpMM (fp32) with nonzero-balanced ranges per warp group
  * (stile_csr_group_nnz() nonzeros each), vectorised B loads; nnz = indptr[M]

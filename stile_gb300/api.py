@@ -162,7 +162,8 @@ def sddmm(op: SddmmOperator, X: torch.Tensor, Y: torch.Tensor) -> torch.Tensor:
 
 
 class HybridSpMMFunction(torch.autograd.Function):
-    """C = A(vals) @ B with A's pattern fixed by ``op``.
+    """C = A(vals) @ B with A's pattern fixed by ``op`` (B fp32 or bf16; C,
+    dvals fp32; dB in B's dtype).
 
     forward : the fused hybrid kernel (values refreshed on device when
               ``vals`` changed since the last call)
@@ -191,7 +192,7 @@ class HybridSpMMFunction(torch.autograd.Function):
             dvals = op.dvals(dC, B)
         if ctx.needs_input_grad[1]:
             opT, _ = op.transposed
-            dB = opT(dC)
+            dB = opT(dC).to(B.dtype)
         return dvals, dB, None
 
 

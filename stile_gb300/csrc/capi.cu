@@ -496,6 +496,15 @@ int stile_spmm_plan_free(StileSpmmPlan* plan) {
   return STILE_OK;
 }
 
+static int check_dense_bf16(long ld, int N, const void* ptr, const char* name) {
+  if (!ptr) return fail(STILE_E_INVALID, std::string("null ") + name);
+  if (ld < N || (ld % 8) != 0)
+    return fail(STILE_E_INVALID, std::string(name) + " (bf16): row stride must be >= N and a multiple of 8");
+  if ((reinterpret_cast<uintptr_t>(ptr) & 15) != 0)
+    return fail(STILE_E_INVALID, std::string(name) + ": must be 16-byte aligned");
+  return STILE_OK;
+}
+
 static int check_dense(long ld, int N, const void* ptr, const char* name) {
   if (!ptr) return fail(STILE_E_INVALID, std::string("null ") + name);
   if (ld < N || (ld % 4) != 0)
@@ -563,8 +572,8 @@ int stile_spmm_run_bf16(const StileSpmmPlan* plan, const uint16_t* B, int64_t ld
   return spmm_run(plan, B, true, ldb, C, ldc, N, stream);
 }
 
-int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, const float* B,
-                     int64_t ldb, float* dvals, int32_t N, void* stream) {
+static int spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, const void* B, bool b_bf16,
+                      int64_t ldb, float* dvals, int32_t N, void* stream) {
   if (!plan) return fail(STILE_E_INVALID, "null plan");
   if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
   if (!dvals) return fail(STILE_E_INVALID, "null dvals");
@@ -572,16 +581,27 @@ int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, c
       (plan->args.ell_n_groups && !plan->args.ell_nnz_id))
     return fail(STILE_E_INVALID, "plan was uploaded without nonzero ids");
   int rc;
-  if ((rc = check_dense(ldb, N, B, "B")) != 0) return rc;
+  if ((rc = b_bf16 ? check_dense_bf16(ldb, N, B, "B") : check_dense(ldb, N, B, "B")) != 0) return rc;
   if ((rc = check_dense(lddy, N, dY, "dY")) != 0) return rc;
   stile::SpmmArgs a = plan->args;
-  a.B = B;
+  a.B = static_cast<const float*>(B);
+  a.b_bf16 = b_bf16 ? 1 : 0;
   a.ldb = ldb;
   a.N = N;
   cudaError_t e = stile::launch_dvals(a, dY, lddy, dvals, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
   g_launches += (a.dv_n > 0);
   return STILE_OK;
+}
+
+int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, const float* B, int64_t ldb,
+                     float* dvals, int32_t N, void* stream) {
+  return spmm_dvals(plan, dY, lddy, B, false, ldb, dvals, N, stream);
+}
+
+int stile_spmm_dvals_bf16(const StileSpmmPlan* plan, const float* dY, int64_t lddy, const uint16_t* B, int64_t ldb,
+                          float* dvals, int32_t N, void* stream) {
+  return spmm_dvals(plan, dY, lddy, B, true, ldb, dvals, N, stream);
 }
 
 int stile_spmm_plan_set_values(StileSpmmPlan* plan, const float* vals, void* stream) {
@@ -707,18 +727,19 @@ int stile_sddmm_plan_free(StileSddmmPlan* plan) {
   return STILE_OK;
 }
 
-int stile_sddmm_run(const StileSddmmPlan* plan, const float* X, int64_t ldx, const float* Y,
-                    int64_t ldy, float* out, int32_t F, void* stream) {
+static int sddmm_run(const StileSddmmPlan* plan, const void* X, int64_t ldx, const void* Y, int64_t ldy, bool bf16,
+                     float* out, int32_t F, void* stream) {
   if (!plan) return fail(STILE_E_INVALID, "null plan");
   if (F <= 0) return fail(STILE_E_INVALID, "F must be positive");
   if (!out) return fail(STILE_E_INVALID, "null out");
   int rc;
-  if ((rc = check_dense(ldx, F, X, "X")) != 0) return rc;
-  if ((rc = check_dense(ldy, F, Y, "Y")) != 0) return rc;
+  if ((rc = bf16 ? check_dense_bf16(ldx, F, X, "X") : check_dense(ldx, F, X, "X")) != 0) return rc;
+  if ((rc = bf16 ? check_dense_bf16(ldy, F, Y, "Y") : check_dense(ldy, F, Y, "Y")) != 0) return rc;
   stile::SddmmArgs a = plan->args;
-  a.X = X;
+  a.X = static_cast<const float*>(X);
+  a.xy_bf16 = bf16 ? 1 : 0;
   a.ldx = ldx;
-  a.Y = Y;
+  a.Y = static_cast<const float*>(Y);
   a.ldy = ldy;
   a.out = out;
   a.F = F;
@@ -726,6 +747,16 @@ int stile_sddmm_run(const StileSddmmPlan* plan, const float* X, int64_t ldx, con
   if (e != cudaSuccess) return cuda_fail(e, "SDDMM launch");
   g_launches += (a.n_blk > 0) + (a.n_1d > 0);
   return STILE_OK;
+}
+
+int stile_sddmm_run(const StileSddmmPlan* plan, const float* X, int64_t ldx, const float* Y, int64_t ldy, float* out,
+                    int32_t F, void* stream) {
+  return sddmm_run(plan, X, ldx, Y, ldy, false, out, F, stream);
+}
+
+int stile_sddmm_run_bf16(const StileSddmmPlan* plan, const uint16_t* X, int64_t ldx, const uint16_t* Y, int64_t ldy,
+                         float* out, int32_t F, void* stream) {
+  return sddmm_run(plan, X, ldx, Y, ldy, true, out, F, stream);
 }
 
 int stile_debug_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,

@@ -8,6 +8,8 @@
 //    bm x bn block; the X / Y rows of the block are staged in shared memory
 //    one 128-feature chunk at a time and only the live entries of the block
 //    (indicesDense) are computed.
+#include <type_traits>
+
 #include "common.cuh"
 #include "spmm.cuh"
 
@@ -29,15 +31,38 @@ constexpr int kSddmmBlocks = 4;      // resident 256-thread blocks per SM (regis
 // kVec: F % 4 == 0, so a lane's float4 of features is all in range or all
 // out.  VEC float4 per lane: with VEC = 2 (16-lane groups for F >= 128) two
 // groups share every warp-wide shuffle, halving the instructions per byte.
-template <int LPR, int V, bool kVec, int VEC = 1>
+//
+// kXb / kYb: X / Y hold bf16 (8 features per 16-byte load, converted to
+// fp32; VEC = 2 so that a lane covers the 8 features of one load).
+template <int VEC, bool kVec, bool kB16>
+__device__ __forceinline__ void load_feats(const void* row, int f, int F, float4 (&o)[VEC]) {
+  if constexpr (kB16) {
+    static_assert(VEC == 2, "a bf16 load covers 8 features");
+    bf16x8_to_f32(ld_row8_bf16(static_cast<const uint16_t*>(row), f, F), o[0], o[1]);
+  } else {
+    const float* r = static_cast<const float*>(row);
+#pragma unroll
+    for (int w = 0; w < VEC; ++w) {
+      const int fw = f + 4 * w;
+      if (kVec) o[w] = fw < F ? ldg4(r + fw) : make_float4(0.f, 0.f, 0.f, 0.f);
+      else o[w] = ld_row4(r, fw, F);
+    }
+  }
+}
+
+template <int LPR, int V, bool kVec, int VEC = 1, bool kXb = false, bool kYb = false>
 __global__ void __launch_bounds__(256, kSddmmBlocks) sddmm_list_kernel(long n, const int* __restrict__ rows,
                                                                      const int* __restrict__ cols,
                                                                      const int* __restrict__ outs,
-                                                                     const float* __restrict__ X, long ldx,
-                                                                     const float* __restrict__ Y, long ldy,
+                                                                     const void* __restrict__ Xv, long ldx,
+                                                                     const void* __restrict__ Yv, long ldy,
                                                                      float* __restrict__ out, int F) {
   static_assert(V % 4 == 0, "entries are gathered 4 at a time");
-  static_assert(VEC == 1 || kVec, "wide lanes need F % 4 == 0");
+  static_assert(VEC == 1 || kVec || kXb || kYb, "wide fp32 lanes need F % 4 == 0");
+  using TX = typename std::conditional<kXb, uint16_t, float>::type;
+  using TY = typename std::conditional<kYb, uint16_t, float>::type;
+  const TX* __restrict__ X = static_cast<const TX*>(Xv);
+  const TY* __restrict__ Y = static_cast<const TY*>(Yv);
   constexpr int kPh = 4 / VEC;  // entries per gather phase: 8 float4 loads in flight per lane
   constexpr int GPB = 256 / LPR;
   const int lane = threadIdx.x & 31;
@@ -67,11 +92,6 @@ __global__ void __launch_bounds__(256, kSddmmBlocks) sddmm_list_kernel(long n, c
     for (int v = 0; v < V; ++v) a[v] = 0.f;
     for (int fc = 0; fc < F; fc += 4 * VEC * LPR) {
       const int f = fc + 4 * VEC * sl;
-      auto ld = [&](const float* row, int w) {
-        const int fw = f + 4 * w;
-        if (kVec) return fw < F ? ldg4(row + fw) : make_float4(0.f, 0.f, 0.f, 0.f);
-        return ld_row4(row, fw, F);
-      };
       // phases of kPh entries; xlast carries the previous phase's last X row
       float4 xlast[VEC];
 #pragma unroll
@@ -80,21 +100,19 @@ __global__ void __launch_bounds__(256, kSddmmBlocks) sddmm_list_kernel(long n, c
       for (int h = 0; h < V; h += kPh) {
         float4 xv[kPh][VEC], yv[kPh][VEC];
 #pragma unroll
-        for (int v = 0; v < kPh; ++v) {
-          const float* yr = Y + (long)col_of(h + v) * ldy;
-#pragma unroll
-          for (int w = 0; w < VEC; ++w) yv[v][w] = ld(yr, w);
-        }
+        for (int v = 0; v < kPh; ++v)
+          load_feats<VEC, kVec, kYb>(Y + (long)col_of(h + v) * ldy, f, F, yv[v]);
         // X rows: a gather only where the row changes (entry 0 always loads)
 #pragma unroll
         for (int v = 0; v < kPh; ++v) {
           const int i = h + v;
           const int ri = row_of(i);
           const bool same = i > 0 && ri == row_of(i > 0 ? i - 1 : 0);
+          if (!same) {
+            load_feats<VEC, kVec, kXb>(X + (long)ri * ldx, f, F, xv[v]);
+          } else {
 #pragma unroll
-          for (int w = 0; w < VEC; ++w) {
-            if (!same) xv[v][w] = ld(X + (long)ri * ldx, w);
-            else xv[v][w] = v > 0 ? xv[v > 0 ? v - 1 : 0][w] : xlast[w];
+            for (int w = 0; w < VEC; ++w) xv[v][w] = v > 0 ? xv[v > 0 ? v - 1 : 0][w] : xlast[w];
           }
         }
 #pragma unroll
@@ -148,9 +166,41 @@ static int lpr_for_f(int F) {
   return l < 4 ? 4 : l;
 }
 
-cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const int* outs, const float* X,
-                              long ldx, const float* Y, long ldy, float* out, int F, cudaStream_t st) {
+static int lpr_for_f8(int F) {
+  const int lanes = (F + 7) / 8;
+  if (lanes >= 32) return 32;
+  int l = 4;
+  while (l < lanes) l <<= 1;
+  return l;
+}
+
+template <bool kXb, bool kYb>
+static cudaError_t launch_list_b16(long n, const int* rows, const int* cols, const int* outs, const void* X,
+                                   long ldx, const void* Y, long ldy, float* out, int F, cudaStream_t st) {
+  // 8 features per lane (one bf16 load, two float4 of an fp32 operand)
+  const int lpr = F % 128 == 0 ? 16 : lpr_for_f8(F);
+  const long groups = (n + kSddmmV - 1) / kSddmmV;
+  long grid = (groups + (256 / lpr) - 1) / (256 / lpr);
+  if (grid > 152L * 32) grid = 152L * 32;
+#define STILE_SDDMM_B16(L)                                                                                      \
+  sddmm_list_kernel<L, kSddmmV, false, 2, kXb, kYb><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, \
+                                                                                  Y, ldy, out, F)
+  switch (lpr) {
+    case 4: STILE_SDDMM_B16(4); break;
+    case 8: STILE_SDDMM_B16(8); break;
+    case 16: STILE_SDDMM_B16(16); break;
+    default: STILE_SDDMM_B16(32); break;
+  }
+#undef STILE_SDDMM_B16
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const int* outs, const void* X, bool x_bf16,
+                              long ldx, const void* Y, bool y_bf16, long ldy, float* out, int F, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  if (x_bf16 && y_bf16) return launch_list_b16<true, true>(n, rows, cols, outs, X, ldx, Y, ldy, out, F, st);
+  if (y_bf16) return launch_list_b16<false, true>(n, rows, cols, outs, X, ldx, Y, ldy, out, F, st);
+  if (x_bf16) return cudaErrorNotSupported;  // no caller has a bf16 X with an fp32 Y
   const int lpr = lpr_for_f(F);
   const int gpb = 256 / lpr;
   long groups = (n + kSddmmV - 1) / kSddmmV;
@@ -174,12 +224,29 @@ cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const in
     case 16: STILE_SDDMM_CASE(16) break;
     default: STILE_SDDMM_CASE(32) break;
   }
+#undef STILE_SDDMM_CASE
   return cudaGetLastError();
 }
 
 constexpr int kChunk = 128;
 constexpr int kPadRow = kChunk + 4;
 
+// features [f, f+4) of a bf16 row as fp32, masked by F (rows are 16-byte
+// aligned with a stride that is a multiple of 8 elements)
+__device__ __forceinline__ float4 ld_row4_bf16(const uint16_t* row, int f, int F) {
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (f < F) {
+    const uint2 u = __ldg(reinterpret_cast<const uint2*>(row + f));
+    v = make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
+                    __uint_as_float(u.y & 0xffff0000u));
+    if (f + 1 >= F) v.y = 0.f;
+    if (f + 2 >= F) v.z = 0.f;
+    if (f + 3 >= F) v.w = 0.f;
+  }
+  return v;
+}
+
+template <bool kB16>
 __global__ void __launch_bounds__(128) sddmm_block_kernel(SddmmArgs p) {
   __shared__ __align__(16) float xs[16 * kPadRow];
   __shared__ __align__(16) float ys[16 * kPadRow];
@@ -200,8 +267,15 @@ __global__ void __launch_bounds__(128) sddmm_block_kernel(SddmmArgs p) {
     for (int i = tid; i < 16 * (kChunk / 4); i += 128) {
       const int r = i / (kChunk / 4), c = (i % (kChunk / 4)) * 4;
       float4 vx = make_float4(0.f, 0.f, 0.f, 0.f), vy = vx;
-      if (r < p.bm) vx = ld_row4(p.X + (long)p.blk_i[(long)b * p.bm + r] * p.ldx, fc + c, p.F);
-      if (r < p.bn) vy = ld_row4(p.Y + (long)p.blk_j[(long)b * p.bn + r] * p.ldy, fc + c, p.F);
+      if (kB16) {
+        const uint16_t* X16 = reinterpret_cast<const uint16_t*>(p.X);
+        const uint16_t* Y16 = reinterpret_cast<const uint16_t*>(p.Y);
+        if (r < p.bm) vx = ld_row4_bf16(X16 + (long)p.blk_i[(long)b * p.bm + r] * p.ldx, fc + c, p.F);
+        if (r < p.bn) vy = ld_row4_bf16(Y16 + (long)p.blk_j[(long)b * p.bn + r] * p.ldy, fc + c, p.F);
+      } else {
+        if (r < p.bm) vx = ld_row4(p.X + (long)p.blk_i[(long)b * p.bm + r] * p.ldx, fc + c, p.F);
+        if (r < p.bn) vy = ld_row4(p.Y + (long)p.blk_j[(long)b * p.bn + r] * p.ldy, fc + c, p.F);
+      }
       *reinterpret_cast<float4*>(&xs[r * kPadRow + c]) = vx;
       *reinterpret_cast<float4*>(&ys[r * kPadRow + c]) = vy;
     }
@@ -236,11 +310,13 @@ cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st) {
   // result is the one kept, as in the reference's host reorder
   // (order_output_BSDDMM writes the TC results first, then the 1D ones)
   if (p.n_blk > 0) {
-    sddmm_block_kernel<<<p.n_blk, 128, 0, st>>>(p);
+    if (p.xy_bf16) sddmm_block_kernel<true><<<p.n_blk, 128, 0, st>>>(p);
+    else sddmm_block_kernel<false><<<p.n_blk, 128, 0, st>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  return launch_sddmm_list(p.n_1d, p.mid_idx, p.j_idx, p.remap, p.X, p.ldx, p.Y, p.ldy, p.out, p.F, st);
+  return launch_sddmm_list(p.n_1d, p.mid_idx, p.j_idx, p.remap, p.X, p.xy_bf16, p.ldx, p.Y, p.xy_bf16, p.ldy, p.out,
+                           p.F, st);
 }
 
 }  // namespace stile

@@ -942,7 +942,8 @@ cudaError_t launch_ell(const SpmmArgs& args, cudaStream_t st) {
 }
 
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {
-  return launch_sddmm_list(p.dv_n, p.dv_row, p.dv_col, p.dv_id, dY, lddy, p.B, p.ldb, dvals, p.N, st);
+  return launch_sddmm_list(p.dv_n, p.dv_row, p.dv_col, p.dv_id, dY, false, lddy, p.B, p.b_bf16 != 0, p.ldb, dvals,
+                           p.N, st);
 }
 
 }  // namespace stile

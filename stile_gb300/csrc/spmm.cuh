@@ -78,16 +78,16 @@ void note_launches(int n);
 // (0 on error)
 int tc_persistent_ctas(int mode);
 cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st);
-cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals,
-                         cudaStream_t st);
+cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st);
 constexpr int kChunkSteps = 32;
 cudaError_t launch_repack(const SpmmArgs& p, const float* vals, long n_ell_slots, cudaStream_t st);
 
 struct SddmmArgs {
-  const float* X;
+  const float* X;  // fp32, or bf16 bits when xy_bf16 (X and Y alike)
   long ldx;
   const float* Y;
   long ldy;
+  int xy_bf16;
   float* out;
   int F;
   int n_1d;
@@ -103,8 +103,8 @@ struct SddmmArgs {
 };
 
 cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st);
-cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const int* outs, const float* X,
-                              long ldx, const float* Y, long ldy, float* out, int F, cudaStream_t st);
+cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const int* outs, const void* X, bool x_bf16,
+                              long ldx, const void* Y, bool y_bf16, long ldy, float* out, int F, cudaStream_t st);
 
 cudaError_t launch_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
                               uint32_t idesc, uint32_t kind, float* out, int* err, cudaStream_t st);

@@ -131,11 +131,14 @@ class DeviceSpmmPlan:
         return out
 
     def dvals(self, dY: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+        """dvals[t] = <dY[row(t)], B[col(t)]> (fp32); B fp32 or bf16."""
         dY, lddy = dense_operand(dY, "dY")
-        B, ldb = dense_operand(B, "B")
+        bf16 = B.dtype == torch.bfloat16
+        B, ldb = dense_operand_bf16(B, "B") if bf16 else dense_operand(B, "B")
         out = torch.zeros(self.nnz, dtype=torch.float32, device=B.device)
-        _lib.check(self.lib.stile_spmm_dvals(self.handle, dY.data_ptr(), lddy, B.data_ptr(), ldb,
-                                             out.data_ptr(), B.shape[1], _stream()), "stile_spmm_dvals")
+        fn = self.lib.stile_spmm_dvals_bf16 if bf16 else self.lib.stile_spmm_dvals
+        _lib.check(fn(self.handle, dY.data_ptr(), lddy, B.data_ptr(), ldb, out.data_ptr(), B.shape[1], _stream()),
+                   "stile_spmm_dvals_bf16" if bf16 else "stile_spmm_dvals")
         return out
 
     def set_values(self, vals: torch.Tensor):
@@ -187,14 +190,22 @@ class DeviceSddmmPlan:
         self.handle = handle
 
     def run(self, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
-        X, ldx = dense_operand(X, "X")
-        Y, ldy = dense_operand(Y, "Y")
+        """out[t] = <X[row(t)], Y[col(t)]> in fp32; X and Y both bf16 are read
+        as is, any other mix is computed from fp32 copies."""
+        bf16 = X.dtype == torch.bfloat16 and Y.dtype == torch.bfloat16
+        if bf16:
+            X, ldx = dense_operand_bf16(X, "X")
+            Y, ldy = dense_operand_bf16(Y, "Y")
+        else:
+            X, ldx = dense_operand(X, "X")
+            Y, ldy = dense_operand(Y, "Y")
         if X.shape[1] != Y.shape[1]:
             raise ValueError("X and Y must have the same feature count")
         if out is None:
             out = torch.zeros(self.nnz, dtype=torch.float32, device=X.device)
-        _lib.check(self.lib.stile_sddmm_run(self.handle, X.data_ptr(), ldx, Y.data_ptr(), ldy,
-                                            out.data_ptr(), X.shape[1], _stream()), "stile_sddmm_run")
+        fn = self.lib.stile_sddmm_run_bf16 if bf16 else self.lib.stile_sddmm_run
+        _lib.check(fn(self.handle, X.data_ptr(), ldx, Y.data_ptr(), ldy, out.data_ptr(), X.shape[1], _stream()),
+                   "stile_sddmm_run_bf16" if bf16 else "stile_sddmm_run")
         return out
 
     def close(self):

@@ -138,3 +138,25 @@ def test_plan_cache_reuses_plans_for_operator_and_transpose(tmp_path):
     dC = torch.as_tensor(np.random.default_rng(8).standard_normal((A.shape[0], N)).astype(np.float32), device="cuda")
     assert torch.allclose(opT(dC), fresh.transposed[0](dC), rtol=1e-6, atol=1e-6)
     assert S.rel_fro(opT(dC).cpu().numpy(), S.spmm_fp64(A2.T.tocsr(), dC.cpu().numpy())) <= 1e-5
+
+
+def test_autograd_with_bf16_operand():
+    """B in bf16: the forward reads it as is, dvals = <dC, B> runs on the bf16
+    rows, dB = A^T dC comes back in bf16; all against fp64 products of the
+    same bf16 values."""
+    A = _graph(seed=9)
+    N = 128
+    op = plan_spmm(A, N, PlanConfig(tc_mode=D.TC_BF16))
+    rng = np.random.default_rng(3)
+    B = torch.as_tensor(rng.standard_normal((A.shape[1], N)).astype(np.float32), device="cuda").to(torch.bfloat16)
+    dC = rng.standard_normal((A.shape[0], N)).astype(np.float32)
+    vals = torch.as_tensor(A.data.astype(np.float32), device="cuda").requires_grad_(True)
+    Bt = B.clone().requires_grad_(True)
+    C = HybridSpMMFunction.apply(vals, Bt, op)
+    assert C.dtype == torch.float32
+    gv, gB = torch.autograd.grad(C, [vals, Bt], grad_outputs=torch.as_tensor(dC, device="cuda"))
+    assert gB.dtype == torch.bfloat16 and gv.dtype == torch.float32
+    Bf = B.float().cpu().numpy()
+    assert S.rel_fro(C.detach().cpu().numpy(), S.spmm_fp64(A, Bf)) <= 1e-2
+    assert S.rel_fro(gv.cpu().numpy(), S.sddmm_fp64(A, dC, Bf)) <= 1e-5
+    assert S.rel_fro(gB.float().cpu().numpy(), S.spmm_fp64(A.T.tocsr(), dC)) <= 1e-2

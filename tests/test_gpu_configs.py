@@ -58,14 +58,31 @@ def test_config3_pruned_weight_fp32_path():
     _check_spmm(w, D.TC_SPLIT_BF16, 1e-5)
 
 
-def test_config4_sddmm_mask():
+@pytest.fixture(scope="module")
+def sddmm_config():
     w = W.sddmm()
-    op = SddmmOperator(w.A, w.width)
+    return w, SddmmOperator(w.A, w.width)
+
+
+def test_config4_sddmm_mask(sddmm_config):
+    w, op = sddmm_config
     X = torch.as_tensor(w.dense["X"], device="cuda")
     Y = torch.as_tensor(w.dense["Y"], device="cuda")
     out = op(X, Y).cpu().numpy()
     ids, ref = W.sddmm_fp64_sample(w.A, w.dense["X"], w.dense["Y"], n_sample=w.A.nnz)
     assert len(ids) == w.A.nnz
+    assert S.rel_fro(out, ref) <= 1e-5
+
+
+def test_config4_sddmm_mask_bf16(sddmm_config):
+    """X and Y in bf16 (the configuration's second precision): read as is,
+    products and sums in fp32, so against the fp64 product of the same bf16
+    values the result is fp32-exact."""
+    w, op = sddmm_config
+    X = torch.as_tensor(w.dense["X"], device="cuda").to(torch.bfloat16)
+    Y = torch.as_tensor(w.dense["Y"], device="cuda").to(torch.bfloat16)
+    out = op(X, Y).cpu().numpy()
+    ids, ref = W.sddmm_fp64_sample(w.A, X.float().cpu().numpy(), Y.float().cpu().numpy(), n_sample=w.A.nnz)
     assert S.rel_fro(out, ref) <= 1e-5
 
 
