@@ -1218,16 +1218,21 @@ class SddmmPlanner:
             t.pred_avg = t.pred_cost / np.float32(t.nnz_unc)
         return t
 
-    def _one_d_tile(self, op, p):
-        nn = op.chunk_uncovered(self.uncovered)
+    def _one_d_tile(self, op, p, nn=None):
+        """Selection record of chunk p of ``op``; ``nn`` is the operator's
+        per-chunk uncovered counts when the caller already has them (they do
+        not change until the selected tiles are finalised)."""
+        if nn is None:
+            nn = op.chunk_uncovered(self.uncovered)
         return _Sel(op=op, kind=ONE_D, ts=(self.mbs,), pos=(int(p),), atomic=False, j_num=self.F,
                     nnz_unc=self.F * int(nn[p]), best_ts=(self.mbs,), params=dict(ONE_D_PARAMS))
 
     def _local_1d(self, sel, target):
         op, avg = self._avg_cache[sel.op.op_id]
         good = []
+        nn = op.chunk_uncovered(self.uncovered)
         for p in np.nonzero(avg <= target)[0]:
-            t = self._one_d_tile(op, int(p))
+            t = self._one_d_tile(op, int(p), nn)
             t.pred_cost = avg[p] * t.nnz_unc
             good.append(t)
         return good
