@@ -275,6 +275,18 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def max_over_ranks(x, dev=None):
+    """The largest of every rank's x (replicas: the slowest rank's time is the
+    job's); x itself without a process group or with one rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -387,11 +399,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     launches = launch_count() - launches0
-    ms = float(np.sum(times)) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(float(np.sum(times)) / args.steps, dev)
     value = world * flops / (ms * 1e-3) / 1e9
 
     plain_times, _ = timed(plain_step, args.steps)
@@ -456,11 +464,7 @@ def run_gpu(args):
         e2e_step()
     torch.cuda.synchronize()
     e2e_times, _ = timed(e2e_step, args.steps)
-    e2e_ms = float(np.sum(e2e_times)) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(float(np.sum(e2e_times)) / args.steps, dev)
     e2e_val = world * flops / (e2e_ms * 1e-3) / 1e9
     h2d = hB.numel() * 4 + hdC.numel() * 4
     d2h = hC.numel() * 4 + hdv.numel() * 4 + hdB.numel() * 4
