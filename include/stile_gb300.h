@@ -193,6 +193,20 @@ int stile_csr_spmm_run(int32_t M, int64_t nnz, const int32_t* indptr, const int3
 /* Nonzeros per warp group of the CSR kernel (for building group_rows). */
 int32_t stile_csr_group_nnz(void);
 
+/*
+ * Row softmax over a CSR pattern, for `batch` value sets (heads) of nnz
+ * entries each, stored one after another:
+ *   out[h][t] = exp(scale * x[h][t] - max_r) / sum over row r's entries,
+ * the entries outside the pattern taken as -inf (x and out may alias).
+ * Counterpart: the sparse-transformer softmax the reference's attention
+ * benchmarks use (my_3rdparty/Magicube/Magicube1/end2end_eval/
+ * sparse_transformer_magicube/src/cuda/softmax_kernel.cu, checked against
+ * torch.softmax(dense * scaler) in verify/bsoftmax.py).
+ */
+int stile_csr_row_softmax(int32_t M, const int32_t* indptr, int64_t nnz,
+                          const float* x, float* out, float scale,
+                          int32_t batch, void* stream);
+
 /* Learned tile cost model (replaces get_MLP_pred / PyTorchMLP,
  * my_cost_model.py:1010-1093, and its trainer MLP_train_cost_model.py:81-204):
  * a STILE_MLP_FEATURES -> 64 -> 32 -> 1 ReLU network over standardised tile

@@ -145,6 +145,56 @@ class SddmmOperator:
         return self.handle.run(X, Y, out)
 
 
+class SparseAttention:
+    """softmax(scale * Q K^T on a sparse pattern) @ V for every head: the
+    SDDMM of the scores over the pattern, a row softmax over each row's
+    entries (``stile_csr_row_softmax``, all heads in one launch), then the
+    hybrid SpMM with the probabilities as its values.  The sparse-attention
+    pipeline the reference's LogSparse / Strided operators come from
+    (MY_sparse/gen_formats_v2.py:2926-3003); both plans are searched once
+    per pattern (and cached with ``cfg.cache_dir``).
+
+    Q, K: [H, n, F] (or [n, F]); V: [H, n, Fv]; the result is fp32
+    [H, n, Fv].
+    """
+
+    def __init__(self, pattern, F, Fv=None, cfg: PlanConfig | None = None, scale=None):
+        from . import _lib
+        A = _csr(pattern)
+        A.data[:] = 1.0
+        self.A = A
+        self.n = A.shape[0]
+        self.F = int(F)
+        self.Fv = int(Fv or F)
+        self.scale = float(scale if scale is not None else 1.0 / np.sqrt(self.F))
+        cfg = cfg or PlanConfig()
+        kw = dict(cfg.__dict__)
+        kw["max_bucket_size"] = kw["max_bucket_size"] or 32
+        self.scores = SddmmOperator(A, self.F, PlanConfig(**kw))
+        self.product = SpmmOperator(A, self.Fv, cfg)
+        self.indptr = torch.as_tensor(A.indptr.astype(np.int32), device="cuda")
+        self.lib = _lib.load()
+
+    def __call__(self, Q, K, V):
+        from . import _lib
+        from .ops import _stream
+        single = Q.dim() == 2
+        if single:
+            Q, K, V = Q[None], K[None], V[None]
+        H = Q.shape[0]
+        nnz = self.A.nnz
+        S = torch.empty((H, nnz), dtype=torch.float32, device=Q.device)
+        for h in range(H):
+            self.scores(Q[h], K[h], out=S[h])
+        _lib.check(self.lib.stile_csr_row_softmax(self.n, self.indptr.data_ptr(), nnz, S.data_ptr(), S.data_ptr(),
+                                                  self.scale, H, _stream()), "stile_csr_row_softmax")
+        out = torch.empty((H, self.n, V.shape[2]), dtype=torch.float32, device=Q.device)
+        for h in range(H):
+            self.product.set_values(S[h])
+            self.product(V[h], out=out[h])
+        return out[0] if single else out
+
+
 def plan_spmm(A, N, cfg: PlanConfig | None = None) -> SpmmOperator:
     return SpmmOperator(A, N, cfg)
 

@@ -628,6 +628,18 @@ int stile_spmm_plan_error_flag(StileSpmmPlan* plan, void* stream, int32_t* flag)
   return STILE_OK;
 }
 
+int stile_csr_row_softmax(int32_t M, const int32_t* indptr, int64_t nnz, const float* x, float* out, float scale,
+                          int32_t batch, void* stream) {
+  if (M < 0 || nnz < 0 || batch < 0) return fail(STILE_E_INVALID, "bad shape");
+  if (M > 0 && !indptr) return fail(STILE_E_INVALID, "null indptr");
+  if (nnz > 0 && batch > 0 && (!x || !out)) return fail(STILE_E_INVALID, "null values");
+  cudaError_t e = stile::launch_csr_row_softmax(M, indptr, (long)nnz, x, out, scale, batch,
+                                                static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "row softmax launch");
+  g_launches += (M > 0 && batch > 0);
+  return STILE_OK;
+}
+
 int stile_csr_spmm_run(int32_t M, int64_t nnz, const int32_t* indptr, const int32_t* indices, const float* vals,
                        const int32_t* group_rows, const float* B, int64_t ldb, float* C, int64_t ldc, int32_t N,
                        void* stream) {

@@ -319,4 +319,38 @@ cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st) {
                            p.F, st);
 }
 
+// Row softmax over a CSR pattern (the sparse-attention step between the
+// SDDMM of the scores and the SpMM with the values, as in the reference's
+// sparse-transformer softmax, my_3rdparty/Magicube/Magicube1/end2end_eval/
+// sparse_transformer_magicube/verify/bsoftmax.py: softmax over each row's
+// stored entries of scale * x, the others being -inf).  One warp per row,
+// blockIdx.y = head (x and out hold `batch` value sets of nnz entries).
+__global__ void __launch_bounds__(256) csr_row_softmax_kernel(int M, const int* __restrict__ indptr, long nnz,
+                                                               const float* __restrict__ x, float* __restrict__ out,
+                                                               float scale) {
+  const int row = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= M) return;
+  const long off = (long)blockIdx.y * nnz;
+  const int b = __ldg(indptr + row), e = __ldg(indptr + row + 1);
+  float m = -INFINITY;
+  for (int t = b + lane; t < e; t += 32) m = fmaxf(m, scale * __ldg(x + off + t));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  float sum = 0.f;
+  for (int t = b + lane; t < e; t += 32) sum += expf(scale * __ldg(x + off + t) - m);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  const float inv = 1.f / sum;
+  for (int t = b + lane; t < e; t += 32) out[off + t] = expf(scale * __ldg(x + off + t) - m) * inv;
+}
+
+cudaError_t launch_csr_row_softmax(int M, const int* indptr, long nnz, const float* x, float* out, float scale,
+                                   int batch, cudaStream_t st) {
+  if (M == 0 || batch == 0) return cudaSuccess;
+  const dim3 grid((unsigned)((M + 7) / 8), (unsigned)batch);
+  csr_row_softmax_kernel<<<grid, 256, 0, st>>>(M, indptr, nnz, x, out, scale);
+  return cudaGetLastError();
+}
+
 }  // namespace stile

@@ -103,6 +103,8 @@ struct SddmmArgs {
 };
 
 cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st);
+cudaError_t launch_csr_row_softmax(int M, const int* indptr, long nnz, const float* x, float* out, float scale,
+                                   int batch, cudaStream_t st);
 cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const int* outs, const void* X, bool x_bf16,
                               long ldx, const void* Y, bool y_bf16, long ldy, float* out, int F, cudaStream_t st);
 

@@ -223,3 +223,36 @@ def pad_shape(A, multiple=128):
     A = A.tocsr()
     indptr = np.concatenate([A.indptr, np.full(m - A.shape[0], A.indptr[-1])])
     return sp.csr_matrix((A.data, A.indices, indptr), shape=(m, k))
+
+
+def logsparse_pattern(n):
+    """LogSparse attention mask (Li et al., 2019), n x n: row i attends to
+    itself, to i - 2^j for 2^j <= i and to i + 2^j for j <
+    floor(log2(n - i - 1)) -- the definition of the reference's
+    test_LogSparse (MY_sparse/gen_formats_v2.py:2926-2964).  Values 1."""
+    rows, cols = [], []
+    for i in range(n):
+        back = [i - (1 << j) for j in range(int(math.log(i, 2)) + 1)] if i > 0 else []
+        fwd = [i + (1 << j) for j in range(int(math.log(n - i - 1, 2)))] if i < n - 1 and n - i - 1 > 0 else []
+        c = sorted(set(back + [i] + fwd))
+        rows.extend([i] * len(c))
+        cols.extend(c)
+    return _to_pattern(n, n, np.asarray(rows), np.asarray(cols))
+
+
+def strided_pattern(n):
+    """Strided attention mask (Child et al., 2019), n x n with stride
+    s = floor(sqrt(n)): row i attends to the window |i - j| < s and to
+    i +- k s for 1 <= k < (n - 1 - i) / s (forward) and k < i / s (backward)
+    -- the reference's test_Strided (MY_sparse/gen_formats_v2.py:2970-3003).
+    Values 1."""
+    s = int(n ** 0.5)
+    rows, cols = [], []
+    for i in range(n):
+        c = set(range(max(i - s + 1, 0), min(i + s, n)))
+        c.update(i + k * s for k in range(1, int((n - 1 - i) / s)))
+        c.update(i - k * s for k in range(1, int(i / s)))
+        c = sorted(c)
+        rows.extend([i] * len(c))
+        cols.extend(c)
+    return _to_pattern(n, n, np.asarray(rows), np.asarray(cols))
