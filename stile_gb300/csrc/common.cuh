@@ -52,6 +52,16 @@ __device__ __forceinline__ void red_row4(float* row, int f, int N, float4 v) {
   }
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while the previous kernel on the stream drains.
+// griddep_wait() returns once that kernel has completed and its writes are
+// visible (at once when the launch was an ordinary one);
+// griddep_launch_dependents() lets the next such kernel start.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // bf16 rows: 16-byte vectors of 8 features
 __device__ __forceinline__ uint4 ldg_u4(const void* p) {
   return __ldg(reinterpret_cast<const uint4*>(p));

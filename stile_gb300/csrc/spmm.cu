@@ -24,6 +24,24 @@
 
 namespace stile {
 
+// Launch with programmatic stream serialization (see griddep_wait): the
+// kernel may start while the previous kernel on the stream drains.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_dependent(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                    Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // ===========================================================================
 // plain CSR SpMM (the comparator)
 // ===========================================================================
@@ -115,7 +133,9 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int M, const int* __restr
 // ===========================================================================
 __global__ void zero_rows_kernel(const int* __restrict__ rows, int n_rows, float* __restrict__ C,
                                  long ldc, int N) {
-  // one warp per row, float4 stores
+  // one warp per row, float4 stores; the ELL kernel may launch meanwhile
+  // (it waits for this grid before touching C)
+  griddep_launch_dependents();
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp_global >= n_rows) return;
@@ -459,6 +479,9 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
     __syncwarp();
   } else {
     // ---------------- epilogue ----------------
+    // launched dependent on the ELL kernel: the producers and the MMA start
+    // while it drains, the C writes (adds to rows it stores) wait for it
+    griddep_wait();
     const int quarter = warp & 3;
     int u = 0;  // accumulation groups consumed so far
 #pragma unroll 1
@@ -531,6 +554,10 @@ template <int LPR, int VEC, bool kFull, bool kOff32, bool kSpanY = false>
 __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   constexpr int kBatch = 4 / VEC;  // entries per batch: 4 float4 in flight per lane
   static_assert(VEC == 1 || kFull, "wide lanes need full feature slices");
+  // launched dependent on the zero-rows kernel (it zeroes rows this one adds
+  // to); the tensor-core kernel may launch once this grid is running
+  griddep_wait();
+  griddep_launch_dependents();
   const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
   const unsigned mask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
   const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
@@ -602,6 +629,10 @@ template <int LPR, bool kFull, bool kOff32, bool kSpanY = false>
 __global__ void __launch_bounds__(256, 4) spmm_ell_seg_bf16_kernel(SpmmArgs p) {
   constexpr int kBatch = 4;
   static_assert(LPR % kBatch == 0, "batches stay inside one record block");
+  // launched dependent on the zero-rows kernel (it zeroes rows this one adds
+  // to); the tensor-core kernel may launch once this grid is running
+  griddep_wait();
+  griddep_launch_dependents();
   const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
   const unsigned mask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
   const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
@@ -806,8 +837,8 @@ static cudaError_t launch_ws_t(const SpmmArgs& p, cudaStream_t st) {
   e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
   if (p.tc_n_chunks == 0 || p.tc_grid == 0) return cudaSuccess;
-  k<<<dim3(p.tc_grid, (p.n_fchunks + p.tc_slice_per - 1) / p.tc_slice_per), kWsThreads, kWsBytes, st>>>(p);
-  return cudaGetLastError();
+  return launch_dependent(k, dim3(p.tc_grid, (p.n_fchunks + p.tc_slice_per - 1) / p.tc_slice_per), dim3(kWsThreads),
+                          kWsBytes, st, p);
 }
 
 // resident CTAs of the tensor-core kernel on the current device, computed
@@ -891,9 +922,9 @@ struct EllLaunch {
   static cudaError_t run(SpmmArgs p, cudaStream_t st) {
     if (p.ell_n_groups == 0) return cudaSuccess;
     const dim3 grid = ell_grid(p, 256 / LPR, 4 * LPR);
-    if (grid.y > 1) spmm_ell_seg_kernel<LPR, 1, false, false, true><<<grid, 256, 0, st>>>(p);
-    else spmm_ell_seg_kernel<LPR, 1, false, false><<<grid, 256, 0, st>>>(p);
-    return cudaGetLastError();
+    if (grid.y > 1)
+      return launch_dependent(spmm_ell_seg_kernel<LPR, 1, false, false, true>, grid, dim3(256), 0, st, p);
+    return launch_dependent(spmm_ell_seg_kernel<LPR, 1, false, false>, grid, dim3(256), 0, st, p);
   }
 };
 
@@ -901,9 +932,9 @@ template <int LPR>
 struct EllBf16Launch {
   static cudaError_t run(SpmmArgs p, cudaStream_t st) {
     const dim3 grid = ell_grid(p, 256 / LPR, 8 * LPR);
-    if (grid.y > 1) spmm_ell_seg_bf16_kernel<LPR, false, false, true><<<grid, 256, 0, st>>>(p);
-    else spmm_ell_seg_bf16_kernel<LPR, false, false><<<grid, 256, 0, st>>>(p);
-    return cudaGetLastError();
+    if (grid.y > 1)
+      return launch_dependent(spmm_ell_seg_bf16_kernel<LPR, false, false, true>, grid, dim3(256), 0, st, p);
+    return launch_dependent(spmm_ell_seg_bf16_kernel<LPR, false, false>, grid, dim3(256), 0, st, p);
   }
 };
 
@@ -923,20 +954,20 @@ cudaError_t launch_ell(const SpmmArgs& args, cudaStream_t st) {
     if (p.N % 128 == 0) {
       // 16-lane sub-groups of 8 features per lane (two groups per warp)
       const dim3 grid = ell_grid(p, 16, 128);
-      if (grid.y > 1) spmm_ell_seg_bf16_kernel<16, true, false, true><<<grid, 256, 0, st>>>(p);
-      else if (off32) spmm_ell_seg_bf16_kernel<16, true, true><<<grid, 256, 0, st>>>(p);
-      else spmm_ell_seg_bf16_kernel<16, true, false><<<grid, 256, 0, st>>>(p);
-      return cudaGetLastError();
+      if (grid.y > 1)
+      return launch_dependent(spmm_ell_seg_bf16_kernel<16, true, false, true>, grid, dim3(256), 0, st, p);
+      else if (off32) return launch_dependent(spmm_ell_seg_bf16_kernel<16, true, true>, grid, dim3(256), 0, st, p);
+      return launch_dependent(spmm_ell_seg_bf16_kernel<16, true, false>, grid, dim3(256), 0, st, p);
     }
     return dispatch_lpr<EllBf16Launch>(lpr_for_bf16(p.N), p, st);
   }
   if (p.N % 128 == 0) {
     // 16-lane sub-groups of 8 features per lane (two groups per warp)
     const dim3 grid = ell_grid(p, 16, 128);
-    if (grid.y > 1) spmm_ell_seg_kernel<16, 2, true, false, true><<<grid, 256, 0, st>>>(p);
-    else if (off32) spmm_ell_seg_kernel<16, 2, true, true><<<grid, 256, 0, st>>>(p);
-    else spmm_ell_seg_kernel<16, 2, true, false><<<grid, 256, 0, st>>>(p);
-    return cudaGetLastError();
+    if (grid.y > 1)
+      return launch_dependent(spmm_ell_seg_kernel<16, 2, true, false, true>, grid, dim3(256), 0, st, p);
+    else if (off32) return launch_dependent(spmm_ell_seg_kernel<16, 2, true, true>, grid, dim3(256), 0, st, p);
+    return launch_dependent(spmm_ell_seg_kernel<16, 2, true, false>, grid, dim3(256), 0, st, p);
   }
   return dispatch_lpr<EllLaunch>(lpr_for(p.N), p, st);
 }
