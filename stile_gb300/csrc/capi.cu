@@ -535,6 +535,7 @@ static int spmm_run(const StileSpmmPlan* plan, const void* B, bool b_bf16, int64
   // rows without an owned writer start at zero; when they are the majority,
   // one strided memset of C is cheaper than the row list (owned rows are
   // overwritten by their writer anyway)
+  bool zero_kernel = false;  // the zero-rows kernel runs right before the ELL kernel
   if (2L * plan->n_zero_rows >= plan->M) {
     e = cudaMemset2DAsync(C, (size_t)ldc * 4, 0, (size_t)N * 4, (size_t)plan->M, st);
     if (e != cudaSuccess) return cuda_fail(e, "zeroing C");
@@ -542,6 +543,7 @@ static int spmm_run(const StileSpmmPlan* plan, const void* B, bool b_bf16, int64
     e = stile::launch_zero_rows(plan->zero_rows, plan->n_zero_rows, C, ldc, N, st);
     if (e != cudaSuccess) return cuda_fail(e, "zero_rows launch");
     if (plan->n_zero_rows) g_launches++;
+    zero_kernel = plan->n_zero_rows > 0;
   }
   stile::SpmmArgs a = plan->args;
   a.B = static_cast<const float*>(B);
@@ -553,6 +555,7 @@ static int spmm_run(const StileSpmmPlan* plan, const void* B, bool b_bf16, int64
   a.n_fchunks = (N + 127) / 128;
   // the ELL kernel initialises the rows it stores; the tensor-core kernel
   // adds to them afterwards (write modes chosen at upload)
+  a.ell_lazy_wait = zero_kernel ? 1 : 0;
   e = stile::launch_ell(a, st);
   if (e != cudaSuccess) return cuda_fail(e, "ELL SpMM launch");
   if (a.ell_n_groups) g_launches++;

@@ -554,14 +554,21 @@ template <int LPR, int VEC, bool kFull, bool kOff32, bool kSpanY = false>
 __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   constexpr int kBatch = 4 / VEC;  // entries per batch: 4 float4 in flight per lane
   static_assert(VEC == 1 || kFull, "wide lanes need full feature slices");
-  // launched dependent on the zero-rows kernel (it zeroes rows this one adds
-  // to); the tensor-core kernel may launch once this grid is running
-  griddep_wait();
+  // Launched dependent on the previous kernel.  When that is the zero-rows
+  // kernel (p.ell_lazy_wait), only the atomic adds (into rows it zeroes)
+  // wait for it, and every thread waits before it exits, so that this
+  // grid's completion implies that kernel's; otherwise (B may come from the
+  // previous kernel) everything waits.  The tensor-core kernel may launch
+  // once this grid is running.
+  if (!p.ell_lazy_wait) griddep_wait();
   griddep_launch_dependents();
   const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
   const unsigned mask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
   const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
-  if (g >= p.ell_n_groups) return;  // the whole sub-group leaves together
+  if (g >= p.ell_n_groups) {  // the whole sub-group leaves together
+    if (p.ell_lazy_wait) griddep_wait();
+    return;
+  }
   const int p0 = __ldg(p.ell_group_ptr + g);
   const int n = __ldg(p.ell_group_ptr + g + 1) - p0;
   const int4* __restrict__ ent = p.ell_entry + p0;
@@ -606,6 +613,7 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
 #pragma unroll
             for (int w = 0; w < VEC; ++w) {
               const int fw = f + 4 * w;
+              if (code < 0 && p.ell_lazy_wait) griddep_wait();
               if (kFull) {
                 if (code >= 0) *reinterpret_cast<float4*>(row + fw) = acc[w];
                 else atomicAdd(reinterpret_cast<float4*>(row + fw), acc[w]);
@@ -620,6 +628,7 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
       mcur = mnext;
     }
   }
+  if (p.ell_lazy_wait) griddep_wait();
 }
 
 // The same entry stream over a bf16 B: each lane covers 8 features with one
@@ -629,14 +638,21 @@ template <int LPR, bool kFull, bool kOff32, bool kSpanY = false>
 __global__ void __launch_bounds__(256, 4) spmm_ell_seg_bf16_kernel(SpmmArgs p) {
   constexpr int kBatch = 4;
   static_assert(LPR % kBatch == 0, "batches stay inside one record block");
-  // launched dependent on the zero-rows kernel (it zeroes rows this one adds
-  // to); the tensor-core kernel may launch once this grid is running
-  griddep_wait();
+  // Launched dependent on the previous kernel.  When that is the zero-rows
+  // kernel (p.ell_lazy_wait), only the atomic adds (into rows it zeroes)
+  // wait for it, and every thread waits before it exits, so that this
+  // grid's completion implies that kernel's; otherwise (B may come from the
+  // previous kernel) everything waits.  The tensor-core kernel may launch
+  // once this grid is running.
+  if (!p.ell_lazy_wait) griddep_wait();
   griddep_launch_dependents();
   const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
   const unsigned mask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
   const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
-  if (g >= p.ell_n_groups) return;  // the whole sub-group leaves together
+  if (g >= p.ell_n_groups) {  // the whole sub-group leaves together
+    if (p.ell_lazy_wait) griddep_wait();
+    return;
+  }
   const int p0 = __ldg(p.ell_group_ptr + g);
   const int n = __ldg(p.ell_group_ptr + g + 1) - p0;
   const int4* __restrict__ ent = p.ell_entry + p0;
@@ -673,6 +689,7 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_seg_bf16_kernel(SpmmArgs p) {
           if (ce & 1) {
             const int code = ce >> 1;
             float* row = p.C + (long)(code >= 0 ? code : -code - 1) * p.ldc;
+            if (code < 0 && p.ell_lazy_wait) griddep_wait();
             if (kFull) {
               if (code >= 0) {
                 *reinterpret_cast<float4*>(row + f) = acc0;
@@ -696,6 +713,7 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_seg_bf16_kernel(SpmmArgs p) {
       mcur = mnext;
     }
   }
+  if (p.ell_lazy_wait) griddep_wait();
 }
 
 // ===========================================================================

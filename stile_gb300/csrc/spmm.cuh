@@ -14,6 +14,7 @@ struct SpmmArgs {
   long ldb;
   int b_bf16;
   int ell_fc_span;  // features per ELL block row (blockIdx.y); set by the launcher
+  int ell_lazy_wait;  // the ELL kernel's predecessor is the zero-rows kernel: only its adds wait
   int tc_slice_per;      // 128-feature slices per tensor-core CTA (blockIdx.y); set by the launcher
   int tc_max_cta_steps;  // most k-steps the chunk schedule gives one CTA
   float* C;
