@@ -62,6 +62,24 @@ __device__ __forceinline__ void griddep_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Launch with programmatic stream serialization (see griddep_wait): the
+// kernel may start while the previous kernel on the stream drains.
+template <typename... KArgs, typename... Args>
+static inline cudaError_t launch_dependent(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                    Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // bf16 rows: 16-byte vectors of 8 features
 __device__ __forceinline__ uint4 ldg_u4(const void* p) {
   return __ldg(reinterpret_cast<const uint4*>(p));

@@ -59,6 +59,10 @@ __global__ void __launch_bounds__(256, kSddmmBlocks) sddmm_list_kernel(long n, c
                                                                      float* __restrict__ out, int F) {
   static_assert(V % 4 == 0, "entries are gathered 4 at a time");
   static_assert(VEC == 1 || kVec || kXb || kYb, "wide fp32 lanes need F % 4 == 0");
+  // launched dependent on the previous kernel: wait for its results (X or Y
+  // may be one of them), then let the next dependent kernel launch
+  griddep_wait();
+  griddep_launch_dependents();
   using TX = typename std::conditional<kXb, uint16_t, float>::type;
   using TY = typename std::conditional<kYb, uint16_t, float>::type;
   const TX* __restrict__ X = static_cast<const TX*>(Xv);
@@ -183,16 +187,17 @@ static cudaError_t launch_list_b16(long n, const int* rows, const int* cols, con
   long grid = (groups + (256 / lpr) - 1) / (256 / lpr);
   if (grid > 152L * 32) grid = 152L * 32;
 #define STILE_SDDMM_B16(L)                                                                                      \
-  sddmm_list_kernel<L, kSddmmV, false, 2, kXb, kYb><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, \
-                                                                                  Y, ldy, out, F)
+  launch_dependent(sddmm_list_kernel<L, kSddmmV, false, 2, kXb, kYb>, dim3((unsigned)grid), dim3(256), 0, st, n, \
+                   rows, cols, outs, X, ldx, Y, ldy, out, F)
+  cudaError_t e;
   switch (lpr) {
-    case 4: STILE_SDDMM_B16(4); break;
-    case 8: STILE_SDDMM_B16(8); break;
-    case 16: STILE_SDDMM_B16(16); break;
-    default: STILE_SDDMM_B16(32); break;
+    case 4: e = STILE_SDDMM_B16(4); break;
+    case 8: e = STILE_SDDMM_B16(8); break;
+    case 16: e = STILE_SDDMM_B16(16); break;
+    default: e = STILE_SDDMM_B16(32); break;
   }
 #undef STILE_SDDMM_B16
-  return cudaGetLastError();
+  return e;
 }
 
 cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const int* outs, const void* X, bool x_bf16,
@@ -211,13 +216,16 @@ cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const in
     long groups2 = (n + kSddmmV - 1) / kSddmmV;
     long grid2 = (groups2 + 15) / 16;
     if (grid2 > 152L * 32) grid2 = 152L * 32;
-    sddmm_list_kernel<16, kSddmmV, true, 2><<<(unsigned)grid2, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F);
-    return cudaGetLastError();
+    return launch_dependent(sddmm_list_kernel<16, kSddmmV, true, 2>, dim3((unsigned)grid2), dim3(256), 0, st, n, rows,
+                            cols, outs, X, ldx, Y, ldy, out, F);
   }
   const bool vec = F % 4 == 0;
+  cudaError_t e;
 #define STILE_SDDMM_CASE(L)                                                                                   \
-  if (vec) sddmm_list_kernel<L, kSddmmV, true><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F); \
-  else sddmm_list_kernel<L, kSddmmV, false><<<(unsigned)grid, 256, 0, st>>>(n, rows, cols, outs, X, ldx, Y, ldy, out, F);
+  e = vec ? launch_dependent(sddmm_list_kernel<L, kSddmmV, true>, dim3((unsigned)grid), dim3(256), 0, st, n, rows,  \
+                             cols, outs, X, ldx, Y, ldy, out, F)                                               \
+          : launch_dependent(sddmm_list_kernel<L, kSddmmV, false>, dim3((unsigned)grid), dim3(256), 0, st, n, rows, \
+                             cols, outs, X, ldx, Y, ldy, out, F);
   switch (lpr) {
     case 4: STILE_SDDMM_CASE(4) break;
     case 8: STILE_SDDMM_CASE(8) break;
@@ -225,7 +233,7 @@ cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const in
     default: STILE_SDDMM_CASE(32) break;
   }
 #undef STILE_SDDMM_CASE
-  return cudaGetLastError();
+  return e;
 }
 
 constexpr int kChunk = 128;

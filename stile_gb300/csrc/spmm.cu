@@ -24,24 +24,6 @@
 
 namespace stile {
 
-// Launch with programmatic stream serialization (see griddep_wait): the
-// kernel may start while the previous kernel on the stream drains.
-template <typename... KArgs, typename... Args>
-static cudaError_t launch_dependent(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
-                                    Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k, args...);
-}
-
 // ===========================================================================
 // plain CSR SpMM (the comparator)
 // ===========================================================================
@@ -133,8 +115,10 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int M, const int* __restr
 // ===========================================================================
 __global__ void zero_rows_kernel(const int* __restrict__ rows, int n_rows, float* __restrict__ C,
                                  long ldc, int N) {
-  // one warp per row, float4 stores; the ELL kernel may launch meanwhile
-  // (it waits for this grid before touching C)
+  // one warp per row, float4 stores.  Launched dependent on the previous
+  // kernel, whose reads of C must be done first; the ELL kernel may launch
+  // meanwhile (it waits for this grid before adding into these rows)
+  griddep_wait();
   griddep_launch_dependents();
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -237,6 +221,7 @@ template <int MODE, bool kFull, bool kIn16>
 __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc_ws_kernel(SpmmArgs p) {
   using W = WsCfg<MODE, kIn16>;
   constexpr int kWsSlots = W::kSlots;
+  griddep_launch_dependents();  // the next kernel waits for this grid before using its results
   extern __shared__ uint8_t smem_raw[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t slots = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -811,8 +796,7 @@ cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const 
 cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   const int grid = (n + 7) / 8;
-  zero_rows_kernel<<<grid, 256, 0, st>>>(rows, n, C, ldc, N);
-  return cudaGetLastError();
+  return launch_dependent(zero_rows_kernel, dim3(grid), dim3(256), 0, st, rows, n, C, ldc, N);
 }
 
 // CTAs of `kernel` resident per SM at `threads` threads and `smem` bytes of
