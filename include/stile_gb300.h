@@ -156,6 +156,24 @@ int stile_spmm_run_bf16(const StileSpmmPlan* plan, const uint16_t* B,
                         int64_t ldb, float* C, int64_t ldc, int32_t N,
                         void* stream);
 
+/*
+ * Batched (multi-head) SpMM: H value sets on the plan's pattern, one launch
+ * of each kernel for all of them.  stile_spmm_values_pack packs
+ * vals[H][nnz] (CSR order, fp32) into `packed`, caller-owned device memory
+ * of stile_spmm_values_bytes(plan, H) bytes, 256-byte aligned; then
+ *   C + h * c_head_stride  =  A_h @ (B + h * b_head_stride)   for h < H
+ * (strides in elements, multiples of 4; heads may not overlap).  fp32 B.
+ * Counterpart: batched_spmm, the reference's multi-head SpMM whose value
+ * buffer carries a batch dimension (MY_sparse/my_fuse_formats.py:1296-1428).
+ */
+int64_t stile_spmm_values_bytes(const StileSpmmPlan* plan, int32_t heads);
+int stile_spmm_values_pack(const StileSpmmPlan* plan, const float* vals,
+                           int32_t heads, void* packed, void* stream);
+int stile_spmm_run_batched(const StileSpmmPlan* plan, const void* packed,
+                           int32_t heads, const float* B, int64_t ldb,
+                           int64_t b_head_stride, float* C, int64_t ldc,
+                           int64_t c_head_stride, int32_t N, void* stream);
+
 /* dvals[nnz] = <dY[row(t)], B[col(t)]> for every nonzero t of A (CSR order),
  * walking the forward plan's tiles. */
 int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy,

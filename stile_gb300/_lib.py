@@ -110,6 +110,12 @@ EXPORTS = {
     "stile_sddmm_plan_free": (ctypes.c_int, [ctypes.c_void_p]),
     "stile_spmm_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                       ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),
+    "stile_spmm_values_bytes": (ctypes.c_int64, [ctypes.c_void_p, ctypes.c_int32]),
+    "stile_spmm_values_pack": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                              ctypes.c_void_p]),
+    "stile_spmm_run_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                              ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                              ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),
     "stile_spmm_run_bf16": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                            ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),
     "stile_spmm_dvals": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,

@@ -96,6 +96,12 @@ class SpmmOperator:
     def dvals(self, dC: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
         return self.handle.dvals(dC, B)
 
+    def batched(self, vals: torch.Tensor, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """C[h] = A(vals[h]) @ B[h] for H value sets on A's pattern (vals
+        [H, nnz] in CSR order, B [H, K, N]): the multi-head SpMM, one launch
+        of each kernel for all heads."""
+        return self.handle.run_batched(self.handle.pack_values(vals), B, out)
+
     def set_values(self, vals: torch.Tensor):
         self.handle.set_values(vals)
         if self._transposed is not None:
@@ -149,7 +155,8 @@ class SparseAttention:
     """softmax(scale * Q K^T on a sparse pattern) @ V for every head: the
     SDDMM of the scores over the pattern, a row softmax over each row's
     entries (``stile_csr_row_softmax``, all heads in one launch), then the
-    hybrid SpMM with the probabilities as its values.  The sparse-attention
+    batched hybrid SpMM with each head's probabilities as its values (one
+    launch of each kernel for all heads).  The sparse-attention
     pipeline the reference's LogSparse / Strided operators come from
     (MY_sparse/gen_formats_v2.py:2926-3003); both plans are searched once
     per pattern (and cached with ``cfg.cache_dir``).
@@ -188,10 +195,7 @@ class SparseAttention:
             self.scores(Q[h], K[h], out=S[h])
         _lib.check(self.lib.stile_csr_row_softmax(self.n, self.indptr.data_ptr(), nnz, S.data_ptr(), S.data_ptr(),
                                                   self.scale, H, _stream()), "stile_csr_row_softmax")
-        out = torch.empty((H, self.n, V.shape[2]), dtype=torch.float32, device=Q.device)
-        for h in range(H):
-            self.product.set_values(S[h])
-            self.product(V[h], out=out[h])
+        out = self.product.batched(S, V)
         return out[0] if single else out
 
 

@@ -514,8 +514,24 @@ static int check_dense(long ld, int N, const void* ptr, const char* name) {
   return STILE_OK;
 }
 
+// value sets of a batched run: ELL records, then tensor-tile images, per head
+static size_t values_ell_bytes(const StileSpmmPlan* plan) { return (size_t)plan->ell_n_slots * 16; }
+static size_t values_tc_bytes(const StileSpmmPlan* plan) {
+  const size_t kb = plan->args.tc_mode == STILE_TC_SPLIT_BF16 ? 1024 : 512;
+  return (size_t)plan->args.tc_n_ksteps * kb;
+}
+static size_t values_tc_offset(const StileSpmmPlan* plan, int heads) {
+  return ((size_t)heads * values_ell_bytes(plan) + 255) / 256 * 256;
+}
+
+struct Heads {
+  int n = 0;                // 0: a single run with the plan's own values
+  const void* packed = nullptr;
+  long b_stride = 0, c_stride = 0;
+};
+
 static int spmm_run(const StileSpmmPlan* plan, const void* B, bool b_bf16, int64_t ldb, float* C, int64_t ldc,
-                    int32_t N, void* stream) {
+                    int32_t N, void* stream, const Heads& hd = Heads()) {
   if (!plan) return fail(STILE_E_INVALID, "null plan");
   if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
   int rc;
@@ -536,11 +552,18 @@ static int spmm_run(const StileSpmmPlan* plan, const void* B, bool b_bf16, int64
   // one strided memset of C is cheaper than the row list (owned rows are
   // overwritten by their writer anyway)
   bool zero_kernel = false;  // the zero-rows kernel runs right before the ELL kernel
+  const int heads = hd.n > 0 ? hd.n : 1;
   if (2L * plan->n_zero_rows >= plan->M) {
-    e = cudaMemset2DAsync(C, (size_t)ldc * 4, 0, (size_t)N * 4, (size_t)plan->M, st);
+    if (heads == 1 || hd.c_stride == (long)plan->M * ldc) {
+      e = cudaMemset2DAsync(C, (size_t)ldc * 4, 0, (size_t)N * 4, (size_t)plan->M * heads, st);
+    } else {
+      e = cudaSuccess;
+      for (int h = 0; h < heads && e == cudaSuccess; ++h)
+        e = cudaMemset2DAsync(C + (long)h * hd.c_stride, (size_t)ldc * 4, 0, (size_t)N * 4, (size_t)plan->M, st);
+    }
     if (e != cudaSuccess) return cuda_fail(e, "zeroing C");
   } else {
-    e = stile::launch_zero_rows(plan->zero_rows, plan->n_zero_rows, C, ldc, N, st);
+    e = stile::launch_zero_rows(plan->zero_rows, plan->n_zero_rows, C, ldc, N, st, heads, hd.c_stride);
     if (e != cudaSuccess) return cuda_fail(e, "zero_rows launch");
     if (plan->n_zero_rows) g_launches++;
     zero_kernel = plan->n_zero_rows > 0;
@@ -556,6 +579,15 @@ static int spmm_run(const StileSpmmPlan* plan, const void* B, bool b_bf16, int64
   // the ELL kernel initialises the rows it stores; the tensor-core kernel
   // adds to them afterwards (write modes chosen at upload)
   a.ell_lazy_wait = zero_kernel ? 1 : 0;
+  if (hd.n > 0) {
+    a.heads = hd.n;
+    a.b_head_stride = hd.b_stride;
+    a.c_head_stride = hd.c_stride;
+    const uint8_t* pk = static_cast<const uint8_t*>(hd.packed);
+    a.ell_entry = reinterpret_cast<const int4*>(pk);
+    a.tc_vals = pk + values_tc_offset(plan, hd.n);
+    a.tc_vals_head_stride = (long)values_tc_bytes(plan);
+  }
   e = stile::launch_ell(a, st);
   if (e != cudaSuccess) return cuda_fail(e, "ELL SpMM launch");
   if (a.ell_n_groups) g_launches++;
@@ -573,6 +605,44 @@ int stile_spmm_run(const StileSpmmPlan* plan, const float* B, int64_t ldb, float
 int stile_spmm_run_bf16(const StileSpmmPlan* plan, const uint16_t* B, int64_t ldb, float* C, int64_t ldc,
                         int32_t N, void* stream) {
   return spmm_run(plan, B, true, ldb, C, ldc, N, stream);
+}
+
+int64_t stile_spmm_values_bytes(const StileSpmmPlan* plan, int32_t heads) {
+  if (!plan || heads < 0) return fail(STILE_E_INVALID, "bad arguments");
+  return (int64_t)(values_tc_offset(plan, heads) + (size_t)heads * values_tc_bytes(plan));
+}
+
+int stile_spmm_values_pack(const StileSpmmPlan* plan, const float* vals, int32_t heads, void* packed, void* stream) {
+  if (!plan || heads < 0) return fail(STILE_E_INVALID, "bad arguments");
+  if (heads == 0) return STILE_OK;
+  if (!vals || !packed) return fail(STILE_E_INVALID, "null argument");
+  if ((reinterpret_cast<uintptr_t>(packed) & 255) != 0) return fail(STILE_E_INVALID, "packed: must be 256-byte aligned");
+  if ((plan->args.tc_n_items && !plan->args.tc_nnz_id) || (plan->args.ell_n_groups && !plan->args.ell_nnz_id))
+    return fail(STILE_E_INVALID, "plan was uploaded without nonzero ids");
+  uint8_t* pk = static_cast<uint8_t*>(packed);
+  cudaError_t e = stile::launch_pack_values(plan->args, vals, plan->nnz, heads, pk, pk + values_tc_offset(plan, heads),
+                                            plan->ell_n_slots, (long)values_tc_bytes(plan),
+                                            static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "value pack launch");
+  g_launches++;
+  return STILE_OK;
+}
+
+int stile_spmm_run_batched(const StileSpmmPlan* plan, const void* packed, int32_t heads, const float* B, int64_t ldb,
+                           int64_t b_head_stride, float* C, int64_t ldc, int64_t c_head_stride, int32_t N,
+                           void* stream) {
+  if (!plan) return fail(STILE_E_INVALID, "null plan");
+  if (heads <= 0 || !packed) return fail(STILE_E_INVALID, "heads must be positive and packed non-null");
+  if (b_head_stride < (int64_t)plan->K * ldb && heads > 1) return fail(STILE_E_INVALID, "B heads overlap");
+  if (c_head_stride < (int64_t)plan->M * ldc && heads > 1) return fail(STILE_E_INVALID, "C heads overlap");
+  if ((b_head_stride % 4) != 0 || (c_head_stride % 4) != 0)
+    return fail(STILE_E_INVALID, "head strides must be multiples of 4 elements");
+  Heads hd;
+  hd.n = heads;
+  hd.packed = packed;
+  hd.b_stride = b_head_stride;
+  hd.c_stride = c_head_stride;
+  return spmm_run(plan, B, false, ldb, C, ldc, N, stream, hd);
 }
 
 static int spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, const void* B, bool b_bf16,

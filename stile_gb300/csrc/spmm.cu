@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int M, const int* __restr
 // zero rows
 // ===========================================================================
 __global__ void zero_rows_kernel(const int* __restrict__ rows, int n_rows, float* __restrict__ C,
-                                 long ldc, int N) {
+                                 long ldc, int N, long c_head_stride) {
   // one warp per row, float4 stores.  Launched dependent on the previous
   // kernel, whose reads of C must be done first; the ELL kernel may launch
   // meanwhile (it waits for this grid before adding into these rows)
@@ -123,7 +123,7 @@ __global__ void zero_rows_kernel(const int* __restrict__ rows, int n_rows, float
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp_global >= n_rows) return;
-  float* row = C + (long)rows[warp_global] * ldc;
+  float* row = C + blockIdx.y * c_head_stride + (long)rows[warp_global] * ldc;
   for (int f = 4 * lane; f < N; f += 128) st_row4(row, f, N, make_float4(0.f, 0.f, 0.f, 0.f));
 }
 
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
 
   if (warp < kProdWarps) {
     // ---------------- producers ----------------
-    const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals);
+    const uint8_t* vals = reinterpret_cast<const uint8_t*>(p.tc_vals) + blockIdx.z * p.tc_vals_head_stride;
     const uint32_t stage = ring + (uint32_t)warp * W::kRaw;
     // step g is k-step s_beg + loc of feature slice f0 / 128 (g = f0 / 128 * S + loc)
     long g = warp;
@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
       }
     };
     if constexpr (kIn16) {
-      const uint16_t* B16 = reinterpret_cast<const uint16_t*>(p.B);
+      const uint16_t* B16 = reinterpret_cast<const uint16_t*>(p.B) + blockIdx.z * p.b_head_stride;
       const int ch = lane & 15, rh = lane >> 4;  // this lane's 16-byte chunk (8 features) and row parity
       // the step at (l, ff) into `slot`: rows 2j + rh, features ff + 8 ch ..
       auto issue16 = [&](int cols, int l, int ff, int slot) {
@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
 #pragma unroll
       for (int r = 0; r < 16; ++r) {
         const int col = __shfl_sync(0xffffffffu, cols, r);
-        const float* row = p.B + (long)col * p.ldb;
+        const float* row = p.B + blockIdx.z * p.b_head_stride + (long)col * p.ldb;
         cp_async16(stage + r * 512 + lane * 16, bytes ? (const void*)(row + f) : (const void*)row, bytes);
       }
 #pragma unroll
@@ -507,7 +507,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
         for (int i = 0; i < 16; ++i) {
           const int row = __ldg(orows + i);
           if (row < 0) continue;
-          float* dst = p.C + (long)row * p.ldc + f;
+          float* dst = p.C + blockIdx.z * p.c_head_stride + (long)row * p.ldc + f;
           if (atomic) atomicAdd(dst, acc[i]); else *dst = acc[i];
         }
       }
@@ -535,7 +535,8 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
 // kOff32: every B row offset col * ldb fits in 32 bits.
 // kSpanY: blockIdx.y takes features [y span, (y + 1) span) (a wide B over
 // few groups; span = p.ell_fc_span, a multiple of the pass width).
-template <int LPR, int VEC, bool kFull, bool kOff32, bool kSpanY = false>
+// kHeads: a batched run (blockIdx.z = head offsets B, C and the records).
+template <int LPR, int VEC, bool kFull, bool kOff32, bool kSpanY = false, bool kHeads = false>
 __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   constexpr int kBatch = 4 / VEC;  // entries per batch: 4 float4 in flight per lane
   static_assert(VEC == 1 || kFull, "wide lanes need full feature slices");
@@ -556,14 +557,15 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   }
   const int p0 = __ldg(p.ell_group_ptr + g);
   const int n = __ldg(p.ell_group_ptr + g + 1) - p0;
-  const int4* __restrict__ ent = p.ell_entry + p0;
+  const long head = kHeads ? blockIdx.z : 0;
+  const int4* __restrict__ ent = p.ell_entry + head * p.ell_n_pos + p0;
   const int N = p.N;
   const int ldb32 = (int)p.ldb;
   auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, 0); };
   for (int fc = kSpanY ? blockIdx.y * p.ell_fc_span : 0;
        fc < (kSpanY ? min(N, (int)(blockIdx.y + 1) * p.ell_fc_span) : N); fc += 4 * VEC * LPR) {
     const int f = fc + 4 * VEC * sl;
-    const float* Bf = p.B + f;
+    const float* Bf = p.B + head * p.b_head_stride + f;
     float4 acc[VEC];
 #pragma unroll
     for (int w = 0; w < VEC; ++w) acc[w] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -583,7 +585,8 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
 #pragma unroll
             for (int w = 0; w < VEC; ++w) bv[u][w] = ldg4(row + 4 * w);
           } else {
-            bv[u][0] = b0 + u < n ? ld_row4(p.B + (long)c * p.ldb, f, N) : make_float4(0.f, 0.f, 0.f, 0.f);
+            bv[u][0] = b0 + u < n ? ld_row4(p.B + head * p.b_head_stride + (long)c * p.ldb, f, N)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
           }
         }
 #pragma unroll
@@ -594,7 +597,7 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
           for (int w = 0; w < VEC; ++w) fma4(acc[w], v, bv[u][w]);  // records past n: value 0, no run end
           if (ce & 1) {
             const int code = ce >> 1;
-            float* row = p.C + (long)(code >= 0 ? code : -code - 1) * p.ldc;
+            float* row = p.C + head * p.c_head_stride + (long)(code >= 0 ? code : -code - 1) * p.ldc;
 #pragma unroll
             for (int w = 0; w < VEC; ++w) {
               const int fw = f + 4 * w;
@@ -640,8 +643,9 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_seg_bf16_kernel(SpmmArgs p) {
   }
   const int p0 = __ldg(p.ell_group_ptr + g);
   const int n = __ldg(p.ell_group_ptr + g + 1) - p0;
-  const int4* __restrict__ ent = p.ell_entry + p0;
-  const uint16_t* __restrict__ B16 = reinterpret_cast<const uint16_t*>(p.B);
+  const int4* __restrict__ ent = p.ell_entry + blockIdx.z * p.ell_n_pos + p0;
+  const uint16_t* __restrict__ B16 = reinterpret_cast<const uint16_t*>(p.B) + blockIdx.z * p.b_head_stride;
+  float* __restrict__ Ch = p.C + blockIdx.z * p.c_head_stride;
   const int N = p.N;
   const int ldb32 = (int)p.ldb;
   auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, 0); };
@@ -673,7 +677,7 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_seg_bf16_kernel(SpmmArgs p) {
           fma4(acc1, v, hi);
           if (ce & 1) {
             const int code = ce >> 1;
-            float* row = p.C + (long)(code >= 0 ? code : -code - 1) * p.ldc;
+            float* row = Ch + (long)(code >= 0 ? code : -code - 1) * p.ldc;
             if (code < 0 && p.ell_lazy_wait) griddep_wait();
             if (kFull) {
               if (code >= 0) {
@@ -740,6 +744,53 @@ __global__ void repack_values_kernel(SpmmArgs p, const float* __restrict__ vals,
   }
 }
 
+// Value sets of a batched run: for head blockIdx.y, the tensor-tile images
+// (in the plan's k-step order and mode) and the ELL records (the plan's
+// column and row code, the head's value) built from vals + head * nnz.
+__global__ void pack_values_kernel(SpmmArgs p, const float* __restrict__ vals, long nnz, int4* __restrict__ ell_out,
+                                   uint16_t* __restrict__ tc_out, long n_ell, long tc_head_elems) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long h = blockIdx.y;
+  const float* hv = vals + h * nnz;
+  const long n_tc = (long)p.tc_n_ksteps * 256;
+  if (i < n_tc) {
+    const long ks = i >> 8;
+    const int e = (int)(i & 255), n = e >> 4, k = e & 15;
+    const int id = p.tc_nnz_id[i];
+    const float v = id >= 0 ? hv[id] : 0.f;
+    const int img = (n >> 3) * 128 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7);
+    uint16_t* out = tc_out + h * tc_head_elems;
+    if (p.tc_mode == STILE_TC_F16) {
+      __half x = __float2half_rn(v);
+      out[ks * 256 + img] = *reinterpret_cast<uint16_t*>(&x);
+    } else {
+      __nv_bfloat16 x = __float2bfloat16_rn(v);
+      if (p.tc_mode == STILE_TC_SPLIT_BF16) {
+        __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(x));
+        out[ks * 512 + img] = *reinterpret_cast<uint16_t*>(&x);
+        out[ks * 512 + 256 + img] = *reinterpret_cast<uint16_t*>(&l);
+      } else {
+        out[ks * 256 + img] = *reinterpret_cast<uint16_t*>(&x);
+      }
+    }
+  } else if (i - n_tc < n_ell) {
+    const long s = i - n_tc;
+    const int id = p.ell_nnz_id[s];
+    int4 r = p.ell_entry[s];
+    r.y = __float_as_int(id >= 0 ? hv[id] : 0.f);
+    ell_out[h * n_ell + s] = r;
+  }
+}
+
+cudaError_t launch_pack_values(const SpmmArgs& p, const float* vals, long nnz, int heads, void* ell_out,
+                               void* tc_out, long n_ell, long tc_head_bytes, cudaStream_t st) {
+  const long total = (long)p.tc_n_ksteps * 256 + n_ell;
+  if (total == 0 || heads == 0) return cudaSuccess;
+  pack_values_kernel<<<dim3((unsigned)((total + 255) / 256), heads), 256, 0, st>>>(
+      p, vals, nnz, static_cast<int4*>(ell_out), static_cast<uint16_t*>(tc_out), n_ell, tc_head_bytes / 2);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_repack(const SpmmArgs& p, const float* vals, long n_ell_slots, cudaStream_t st) {
   const long total = (long)p.tc_n_ksteps * 256 + n_ell_slots;
   if (total == 0) return cudaSuccess;
@@ -793,10 +844,11 @@ cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const 
   return dispatch_lpr<CsrLaunch>(lpr_for(N), M, indptr, indices, vals, B, ldb, C, ldc, N, nnz, group_rows, st);
 }
 
-cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
+cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st, int heads,
+                             long c_head_stride) {
+  if (n == 0 || heads == 0) return cudaSuccess;
   const int grid = (n + 7) / 8;
-  return launch_dependent(zero_rows_kernel, dim3(grid), dim3(256), 0, st, rows, n, C, ldc, N);
+  return launch_dependent(zero_rows_kernel, dim3(grid, heads), dim3(256), 0, st, rows, n, C, ldc, N, c_head_stride);
 }
 
 // CTAs of `kernel` resident per SM at `threads` threads and `smem` bytes of
@@ -839,7 +891,8 @@ static cudaError_t launch_ws_t(const SpmmArgs& p, cudaStream_t st) {
   e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
   if (p.tc_n_chunks == 0 || p.tc_grid == 0) return cudaSuccess;
-  return launch_dependent(k, dim3(p.tc_grid, (p.n_fchunks + p.tc_slice_per - 1) / p.tc_slice_per), dim3(kWsThreads),
+  return launch_dependent(k, dim3(p.tc_grid, (p.n_fchunks + p.tc_slice_per - 1) / p.tc_slice_per, std::max(1, p.heads)),
+                          dim3(kWsThreads),
                           kWsBytes, st, p);
 }
 
@@ -916,7 +969,7 @@ static dim3 ell_grid(SpmmArgs& p, int groups_per_block, int pass) {
   const int per = (int)((n_pass + gy - 1) / gy);
   gy = (n_pass + per - 1) / per;
   p.ell_fc_span = per * pass;
-  return dim3((unsigned)gx, (unsigned)gy, 1);
+  return dim3((unsigned)gx, (unsigned)gy, (unsigned)std::max(1, p.heads));
 }
 
 template <int LPR>
@@ -924,6 +977,8 @@ struct EllLaunch {
   static cudaError_t run(SpmmArgs p, cudaStream_t st) {
     if (p.ell_n_groups == 0) return cudaSuccess;
     const dim3 grid = ell_grid(p, 256 / LPR, 4 * LPR);
+    if (grid.z > 1)
+      return launch_dependent(spmm_ell_seg_kernel<LPR, 1, false, false, true, true>, grid, dim3(256), 0, st, p);
     if (grid.y > 1)
       return launch_dependent(spmm_ell_seg_kernel<LPR, 1, false, false, true>, grid, dim3(256), 0, st, p);
     return launch_dependent(spmm_ell_seg_kernel<LPR, 1, false, false>, grid, dim3(256), 0, st, p);
@@ -966,6 +1021,8 @@ cudaError_t launch_ell(const SpmmArgs& args, cudaStream_t st) {
   if (p.N % 128 == 0) {
     // 16-lane sub-groups of 8 features per lane (two groups per warp)
     const dim3 grid = ell_grid(p, 16, 128);
+    if (grid.z > 1)
+      return launch_dependent(spmm_ell_seg_kernel<16, 2, true, false, true, true>, grid, dim3(256), 0, st, p);
     if (grid.y > 1)
       return launch_dependent(spmm_ell_seg_kernel<16, 2, true, false, true>, grid, dim3(256), 0, st, p);
     else if (off32) return launch_dependent(spmm_ell_seg_kernel<16, 2, true, true>, grid, dim3(256), 0, st, p);

@@ -15,6 +15,12 @@ struct SpmmArgs {
   int b_bf16;
   int ell_fc_span;  // features per ELL block row (blockIdx.y); set by the launcher
   int ell_lazy_wait;  // the ELL kernel's predecessor is the zero-rows kernel: only its adds wait
+  // heads of a batched run (blockIdx.z; 0 and unused otherwise): per head, B
+  // and C start head * stride elements further, the value images head *
+  // tc_vals_head_stride bytes further and the ELL records head * ell_n_pos
+  // records further
+  long b_head_stride, c_head_stride, tc_vals_head_stride;
+  int heads;  // grid.z of the ELL and tensor-core launches (0 or 1: one head)
   int tc_slice_per;      // 128-feature slices per tensor-core CTA (blockIdx.y); set by the launcher
   int tc_max_cta_steps;  // most k-steps the chunk schedule gives one CTA
   float* C;
@@ -68,7 +74,8 @@ cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const 
                             const int* group_rows, cudaStream_t st);
 constexpr int kCsrGroupNnz = 64;  // nonzeros per warp group of the CSR kernel
 constexpr int kSegNnz = 64;       // entries per group of the ELL stream kernel
-cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st);
+cudaError_t launch_zero_rows(const int* rows, int n, float* C, long ldc, int N, cudaStream_t st, int heads = 1,
+                             long c_head_stride = 0);
 cudaError_t launch_tc(const SpmmArgs& p, cudaStream_t st);
 // C-ABI bookkeeping shared by the entry points of every translation unit:
 // record `msg` as the calling thread's last error and return `code`; count
@@ -81,6 +88,8 @@ int tc_persistent_ctas(int mode);
 cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st);
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st);
 constexpr int kChunkSteps = 32;
+cudaError_t launch_pack_values(const SpmmArgs& p, const float* vals, long nnz, int heads, void* ell_out,
+                               void* tc_out, long n_ell, long tc_head_bytes, cudaStream_t st);
 cudaError_t launch_repack(const SpmmArgs& p, const float* vals, long n_ell_slots, cudaStream_t st);
 
 struct SddmmArgs {

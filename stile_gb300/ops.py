@@ -70,6 +70,14 @@ def new_output(rows, cols, device):
     return buf[:, :cols], ldp
 
 
+class PackedValues:
+    """H value sets of one plan packed on the device (pack_values)."""
+
+    def __init__(self, buf, off, heads):
+        self.buf, self.heads = buf, heads
+        self.ptr = buf.data_ptr() + off
+
+
 class DeviceSpmmPlan:
     """A packed SpMM plan resident on the current CUDA device."""
 
@@ -128,6 +136,44 @@ class DeviceSpmmPlan:
         fn = self.lib.stile_spmm_run_bf16 if bf16 else self.lib.stile_spmm_run
         _lib.check(fn(self.handle, B.data_ptr(), ldb, out.data_ptr(), ldc, N, _stream()),
                    "stile_spmm_run_bf16" if bf16 else "stile_spmm_run")
+        return out
+
+    def pack_values(self, vals: torch.Tensor) -> "PackedValues":
+        """Pack H value sets (vals [H, nnz], CSR order) for run_batched."""
+        _require_cuda(vals, "vals")
+        vals = vals.float().contiguous()
+        if vals.dim() != 2 or vals.shape[1] != self.nnz:
+            raise ValueError("vals must be [heads, nnz]")
+        H = vals.shape[0]
+        nbytes = int(self.lib.stile_spmm_values_bytes(self.handle, H))
+        if nbytes < 0:
+            _lib.check(nbytes, "stile_spmm_values_bytes")
+        buf = torch.empty(nbytes + 256, dtype=torch.uint8, device=vals.device)
+        off = (-buf.data_ptr()) % 256
+        _lib.check(self.lib.stile_spmm_values_pack(self.handle, vals.data_ptr(), H, buf.data_ptr() + off, _stream()),
+                   "stile_spmm_values_pack")
+        return PackedValues(buf, off, H)
+
+    def run_batched(self, packed: "PackedValues", B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """C[h] = A_h @ B[h] for the H value sets of ``packed``; B [H, K, N]
+        fp32; one launch of each kernel for all heads."""
+        _require_cuda(B, "B")
+        B = B.float()
+        H, K, N = B.shape
+        if H != packed.heads or K != self.K:
+            raise ValueError("B must be [heads, K, N] for the packed heads")
+        ldb = (N + 3) // 4 * 4
+        if B.stride() != (K * ldb, ldb, 1) or B.data_ptr() % 16:
+            buf = torch.zeros((H, K, ldb), dtype=torch.float32, device=B.device)
+            buf[:, :, :N] = B
+            B = buf
+        if out is None:
+            out = torch.empty((H, self.M, ldb), dtype=torch.float32, device=B.device)[:, :, :N]
+        if out.stride(2) != 1 or out.stride(1) % 4 or out.stride(0) % 4 or out.data_ptr() % 16:
+            raise ValueError("out rows must be 16-byte aligned with strides that are multiples of 4")
+        _lib.check(self.lib.stile_spmm_run_batched(self.handle, packed.ptr, H, B.data_ptr(), B.stride(1),
+                                                   B.stride(0), out.data_ptr(), out.stride(1), out.stride(0), N,
+                                                   _stream()), "stile_spmm_run_batched")
         return out
 
     def dvals(self, dY: torch.Tensor, B: torch.Tensor) -> torch.Tensor:

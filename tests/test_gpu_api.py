@@ -160,3 +160,25 @@ def test_autograd_with_bf16_operand():
     assert S.rel_fro(C.detach().cpu().numpy(), S.spmm_fp64(A, Bf)) <= 1e-2
     assert S.rel_fro(gv.cpu().numpy(), S.sddmm_fp64(A, dC, Bf)) <= 1e-5
     assert S.rel_fro(gB.float().cpu().numpy(), S.spmm_fp64(A.T.tocsr(), dC)) <= 1e-2
+
+
+@pytest.mark.parametrize("N", [64, 128])
+@pytest.mark.parametrize("mode", [D.TC_BF16, D.TC_SPLIT_BF16], ids=["bf16", "split"])
+def test_batched_heads_match_one_head_at_a_time(N, mode):
+    """Several value sets on one pattern in one launch per kernel give what
+    set_values + a single run give for each head."""
+    A = _graph(seed=10)
+    op = plan_spmm(A, N, PlanConfig(tc_mode=mode))
+    H = 3
+    rng = np.random.default_rng(4)
+    vals = torch.as_tensor(rng.uniform(-1, 1, (H, A.nnz)).astype(np.float32), device="cuda")
+    B = torch.as_tensor(rng.standard_normal((H, A.shape[1], N)).astype(np.float32), device="cuda")
+    C = op.batched(vals, B).cpu().numpy()
+    for h in range(H):
+        Ah = sp.csr_matrix((vals[h].cpu().numpy().astype(np.float64), A.indices, A.indptr), shape=A.shape)
+        ref = S.spmm_fp64(Ah, B[h].cpu().numpy())
+        assert S.rel_fro(C[h], ref) <= (1e-2 if mode == D.TC_BF16 else 1e-5)
+        op.set_values(vals[h])
+        one = op(B[h]).cpu().numpy()
+        assert np.allclose(C[h], one, rtol=1e-5, atol=1e-5)
+    assert op.handle.error_flag() == 0
