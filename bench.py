@@ -469,7 +469,7 @@ def run_gpu(args):
     h2d = hB.numel() * 4 + hdC.numel() * 4
     d2h = hC.numel() * 4 + hdv.numel() * 4 + hdB.numel() * 4
 
-    # the learned cost model: its plan's measured forward time judges it
+    # the learned cost model, measured by the forward time of the plan it chooses
     learned = None
     try:
         t0 = time.time()
