@@ -101,15 +101,15 @@ class EllOp:
         self.short_begin = len(self.hyb_new_rows) if sb == len(rn_sorted) else int(self.hyb_ori_row_ends[sb])
         self.n_folded = len(self.hyb_new_rows)
         # entries in position order: rows in i_perm order, each row's entries
-        # in column order, chunks of mbs -> folded rows
-        rows_of_ids = pat.row_of[ids]
-        inv = np.empty(pat.M, dtype=np.int64)
-        inv[self.i_perm] = np.arange(pat.M)
-        pos_row = inv[rows_of_ids]
-        order = np.lexsort((pat.indices[ids], pos_row))
+        # in column order, chunks of mbs -> folded rows.  ``ids`` is in CSR
+        # order (rows ascending, columns ascending within a row), so the
+        # order is the subset's row segments taken in i_perm order.
+        sub_start = np.concatenate([[0], np.cumsum(rn)[:-1]])
+        out_start = np.concatenate([[0], np.cumsum(rn_sorted)[:-1]])
+        order = np.repeat(sub_start[self.i_perm] - out_start, rn_sorted) + np.arange(len(ids), dtype=np.int64)
         self.ids = ids[order]
         self.cols = pat.indices[self.ids]
-        pos_row = pos_row[order]
+        pos_row = np.repeat(np.arange(pat.M, dtype=np.int64), rn_sorted)
         # folded row of every entry
         row_start = np.concatenate([[0], np.cumsum(rn_sorted)[:-1]])
         within = np.arange(len(self.ids)) - row_start[pos_row]
@@ -210,7 +210,7 @@ class TcOp:
         col = pat.indices[ids]
         # per (block, column) counts -> order within block by (-count, col)
         code = blk * pat.K + col
-        ucode, cnt = np.unique(code, return_counts=True)
+        ucode, uinv, cnt = np.unique(code, return_inverse=True, return_counts=True)
         ublk = ucode // pat.K
         ucol = ucode % pat.K
         o = np.lexsort((ucol, -cnt, ublk))
@@ -221,7 +221,7 @@ class TcOp:
         rank = np.empty(len(ucode), dtype=np.int64)
         rank[o] = np.arange(len(ucode)) - self.kstart[ublk]
         # entry -> position within its block's order
-        pos = rank[np.searchsorted(np.unique(code), code)] if len(code) else np.zeros(0, np.int64)
+        pos = rank[uinv.reshape(-1)] if len(code) else np.zeros(0, np.int64)
         eo = np.lexsort((pos, blk))
         self.ids = ids[eo]
         self.blk = blk[eo]
