@@ -60,6 +60,15 @@ class Pattern:
         return np.bincount(self.row_of[ids], minlength=self.M)
 
 
+def _run_counts(code):
+    """(values, counts) of a nondecreasing integer array: np.unique's result
+    without its sort."""
+    if len(code) == 0:
+        return code, np.zeros(0, dtype=np.int64)
+    starts = np.flatnonzero(np.concatenate([[True], code[1:] != code[:-1]]))
+    return code[starts], np.diff(np.append(starts, len(code)))
+
+
 def estimate_max_bucket_size(nnz, sm_num=108):
     """Bucket (fold) length of ELL rows from the expected occupancy
     (my_search_formats.py:965-981; 256-thread blocks, 2048 threads / SM)."""
@@ -159,15 +168,18 @@ class EllOp:
         key = I
         if key not in self._kis_cache:
             n_t = math.ceil(self.n_folded / I)
-            if not hasattr(self, "_cf_order"):
-                self._cf_order = np.lexsort((self.frow, self.cols))
-            col = self.cols[self._cf_order]
-            seg = self.frow[self._cf_order] // I
+            if not hasattr(self, "_cf_col"):
+                o = np.lexsort((self.frow, self.cols))
+                self._cf_col = self.cols[o]
+                self._cf_frow = self.frow[o]
+                self._cf_colchg = self._cf_col[1:] != self._cf_col[:-1]
+            col = self._cf_col
+            seg = self._cf_frow // I
             # entries sorted by (column, folded row): a (segment, column) pair
             # is new wherever the column or the segment changes
             first = np.ones(len(col), dtype=bool)
             if len(col) > 1:
-                first[1:] = (col[1:] != col[:-1]) | (seg[1:] != seg[:-1])
+                first[1:] = self._cf_colchg | (seg[1:] != seg[:-1])
             distinct = np.bincount(seg[first], minlength=n_t)
             has0 = np.zeros(n_t, dtype=bool)
             has0[seg[col == 0]] = True
@@ -604,7 +616,9 @@ class SpmmPlanner:
             if len(blk):
                 win = rel // w
                 span = int(win.max()) + 1
-                code, cnt = np.unique(blk * span + win, return_counts=True)
+                # entries come sorted by (block, position), so the codes are
+                # nondecreasing and their runs are np.unique's groups
+                code, cnt = _run_counts(blk * span + win)
                 mp = int(np.argmax(cnt))
                 r, c = int(code[mp] // span), int(code[mp] % span)
                 cost = self.cost.tc_cost(Kt, True, self.penalty)
