@@ -13,8 +13,10 @@
 //                        horizontally fused kernel (my_fuse_formats.py:2437):
 //                        the same tiles, split by template into two grids so
 //                        that each gets its own block shape and shared memory.
-//  * spmm_dvals_kernel   value gradient <dY[row], B[col]> for every nonzero,
-//                        walking the same tiles.
+//  * dvals               value gradient <dY[row], B[col]> for every nonzero,
+//                        over an entry list built from the same tiles (the
+//                        SDDMM entry-list kernel of sddmm.cu)
+//  * pack_values_kernel  per-head value sets of a batched run
 #include "common.cuh"
 #include <algorithm>
 #include <map>
