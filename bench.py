@@ -648,6 +648,21 @@ def run_config(args):
             out["bf16_B"] = {"forward_ms": timed(lambda: op(B16, out=C16), args.steps),
                              "C_rel_fro": S.rel_fro(C16.cpu().numpy(),
                                                     S.spmm_fp64(A, B16.float().cpu().numpy()))}
+            # tensor-core tiles as 16x16 blocks on the column grid
+            # (TC_k_notsorted): the block-pruned blocks go to the tensor
+            # cores as they are, the scattered rest to row tiles
+            t0 = time.time()
+            op_b = SpmmOperator(A, N, PlanConfig(tc_mode=tc_mode, tc_k_notsorted=True))
+            t_b = time.time() - t0
+            Cb = torch.empty_like(C)
+            op_b(B, out=Cb)
+            torch.cuda.synchronize()
+            out["column_blocks"] = {"plan": plan_summary(op_b.plan), "plan_search_s": round(t_b, 2),
+                                    "tc_ksteps": op_b.device_layout.stats()["tc_ksteps"],
+                                    "forward_ms": timed(lambda: op_b(B, out=Cb), args.steps),
+                                    "bf16_B_forward_ms": timed(lambda: op_b(B16, out=C16), args.steps),
+                                    "C_rel_fro": S.rel_fro(Cb.cpu().numpy(), S.spmm_fp64(A, B_np))}
+            op_b.handle.close()
             # the plan chosen by the learned cost model against the analytic one
             try:
                 t0 = time.time()

@@ -91,7 +91,10 @@ def spmm_from_arrays(formats, fmt_args, B, out_shape, check_owned=True):
     fmt_args : per format, the tuple of arrays ``prepare_inputs_BSPMM``
                emits (my_fuse_formats.py:3321-3537):
                ELL -> (a, indices_k, indices_reordered_i)
-               TC  -> (a, i_indices, indptr, indices)
+               TC  -> (a, i_indices, indptr, indices); ``indices`` is
+                      [blocks, klen] columns, or, for TC_k_notsorted
+                      tiles, one k-block position per block whose columns
+                      are [p * klen, (p + 1) * klen) (:3501-3502)
     B        : dense [K, max_j] (zero-padded columns allowed).
     Returns C [out_shape] in float64 and the list of owned-row conflicts.
     """
@@ -120,6 +123,12 @@ def spmm_from_arrays(formats, fmt_args, B, out_shape, check_owned=True):
             a = a.astype(np.float64)
             tsz = int(fmt["tile_sizes"][0][1])
             mb = len(indptr) - 1
+            if indices.ndim == 1:
+                klen = a.shape[2]
+                cols = indices[:, None] * klen + np.arange(klen)[None, :]
+                if cols.size and cols.max() >= B.shape[0]:
+                    B = np.concatenate([B, np.zeros((int(cols.max()) + 1 - B.shape[0], B.shape[1]))])
+                indices = cols
             part = np.zeros((mb, tsz, max_j))
             for io in range(mb):
                 for blk in range(indptr[io], indptr[io + 1]):

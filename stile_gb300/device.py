@@ -140,6 +140,10 @@ def build_spmm_device(tiles, A, N=32, tc_mode=TC_BF16, emitted=None):
         a, i_idx, indptr, indices = arr
         tsz = int(f.tile_sizes[0][1])
         nnzb, _, kw = a.shape
+        if indices.ndim == 1:
+            # column-ordered blocks (TC_k_notsorted): a k-block position per
+            # block; columns past K carry zero values and read row K - 1
+            indices = np.minimum(indices.astype(np.int64)[:, None] * kw + np.arange(kw)[None, :], K - 1)
         assert tsz == 16 and kw % 16 == 0, "tensor-core blocks are 16 rows x 16k columns"
         nsub = kw // 16
         tiles_sorted = sorted(f.tiles, key=lambda t: tuple(t.tile_pos))

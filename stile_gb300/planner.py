@@ -80,7 +80,11 @@ def estimate_max_bucket_size(nnz, sm_num=108):
     return cands[-1] // 8
 
 
-def tc_tile_sizes(op_type="spmm"):
+def tc_tile_sizes(op_type="spmm", k_notsorted=False):
+    """get_TC_tile_sizes (gen_formats_v2.py:1237-1283): with the columns kept
+    in order (TC_k_notsorted) only 16x32x16 tiles, for both operators."""
+    if k_notsorted:
+        return [((None, 16), (None, 32), (None, 16))]
     if op_type == "sddmm":
         return [((None, 16), (None, 16 * (2 ** j)), (None, 16)) for j in range(3)]
     return [((None, 16), (None, 32), (None, 16 * i)) for i in range(10, 0, -1)]
@@ -203,13 +207,17 @@ class EllOp:
 # ---------------------------------------------------------------------------
 class TcOp:
     """16-row blocks of a row order; in each block the columns are stably
-    sorted by decreasing count (condense_for_TC_tile :1004-1039)."""
+    sorted by decreasing count (condense_for_TC_tile :1004-1039), or, with
+    ``k_notsorted`` (TC_k_notsorted, :1025-1031 and set_init_blk_nums
+    :1328-1335), kept in column order, so that a tile at k position p is the
+    16-column block [16p, 16p + 16) and only non-empty blocks are tiles."""
 
-    def __init__(self, pat: Pattern, i_perm, op_id, op_type="spmm", ids=None, bs=16):
+    def __init__(self, pat: Pattern, i_perm, op_id, op_type="spmm", ids=None, bs=16, k_notsorted=False):
         self.pat = pat
         self.op_id = op_id
         self.bs = bs
         self.op_type = op_type
+        self.k_notsorted = bool(k_notsorted)
         self.i_perm = np.asarray(i_perm, dtype=np.int64)
         self.reordered = not np.array_equal(self.i_perm, np.arange(pat.M))
         inv = np.empty(pat.M, dtype=np.int64)
@@ -225,15 +233,21 @@ class TcOp:
         ucode, uinv, cnt = np.unique(code, return_inverse=True, return_counts=True)
         ublk = ucode // pat.K
         ucol = ucode % pat.K
-        o = np.lexsort((ucol, -cnt, ublk))
+        if self.k_notsorted:
+            o = np.arange(len(ucode))
+        else:
+            o = np.lexsort((ucol, -cnt, ublk))
         ublk, ucol, cnt = ublk[o], ucol[o], cnt[o]
         self.nonempty = np.bincount(ublk, minlength=self.n_blk)
         self.kstart = np.concatenate([[0], np.cumsum(self.nonempty)])
         self.kord_cols = ucol                       # concatenated per block
-        rank = np.empty(len(ucode), dtype=np.int64)
-        rank[o] = np.arange(len(ucode)) - self.kstart[ublk]
-        # entry -> position within its block's order
-        pos = rank[uinv.reshape(-1)] if len(code) else np.zeros(0, np.int64)
+        if self.k_notsorted:
+            pos = col
+        else:
+            rank = np.empty(len(ucode), dtype=np.int64)
+            rank[o] = np.arange(len(ucode)) - self.kstart[ublk]
+            # entry -> position within its block's order
+            pos = rank[uinv.reshape(-1)] if len(code) else np.zeros(0, np.int64)
         eo = np.lexsort((pos, blk))
         self.ids = ids[eo]
         self.blk = blk[eo]
@@ -241,10 +255,35 @@ class TcOp:
         self.prow = prow[eo]
         self.bptr = np.concatenate([[0], np.cumsum(np.bincount(self.blk, minlength=self.n_blk))])
         self.maxne = int(self.nonempty.max()) if self.n_blk else 0
+        # positions a block's counts run over: its non-empty prefix, or (in
+        # column order) up to its last non-empty column
+        if self.k_notsorted:
+            self.extent = np.zeros(self.n_blk, dtype=np.int64)
+            np.maximum.at(self.extent, ublk, ucol + 1)
+        else:
+            self.extent = self.nonempty
         self.blk_nums = {}
-        for ts in tc_tile_sizes(op_type):
+        self.blk_ks = {}
+        for ts in tc_tile_sizes(op_type, self.k_notsorted):
             Kt = ts[2][1]
-            self.blk_nums[ts] = np.ceil(self.nonempty / Kt).astype(np.int64)
+            if self.k_notsorted:
+                nch = -(-pat.K // Kt)
+                ch = np.unique(ublk * nch + ucol // Kt)
+                cb = ch // nch
+                self.blk_nums[ts] = np.bincount(cb, minlength=self.n_blk).astype(np.int64)
+                cptr = np.concatenate([[0], np.cumsum(self.blk_nums[ts])])
+                self.blk_ks[ts] = (ch % nch, cptr)
+            else:
+                self.blk_nums[ts] = np.ceil(self.nonempty / Kt).astype(np.int64)
+
+    def row_positions(self, ts, b):
+        """k positions of the tiles that cover block b whole: the first
+        blk_nums of its order, or (in column order) its non-empty column
+        blocks (``blk_ks``)."""
+        if self.k_notsorted:
+            ks, cptr = self.blk_ks[ts]
+            return [int(x) for x in ks[cptr[b]:cptr[b + 1]]]
+        return list(range(int(self.blk_nums[ts][b])))
 
     def density(self):
         """select_the_densest_tensor_for_TC_tiles (:1286-1309): nnz over
@@ -256,6 +295,8 @@ class TcOp:
         """Columns at ``positions`` of block b's order (non-empty columns, then
         the remaining columns ascending)."""
         positions = np.asarray(positions, dtype=np.int64)
+        if self.k_notsorted:
+            return positions.copy()
         ne = int(self.nonempty[b])
         head = self.kord_cols[self.kstart[b]:self.kstart[b + 1]]
         out = np.empty(positions.shape, dtype=np.int64)
@@ -288,7 +329,7 @@ class TcOp:
         block's non-empty column count, at least 1)."""
         s, e = self.bptr[b], self.bptr[b + 1]
         live = uncovered[self.ids[s:e]]
-        return np.bincount(self.pos[s:e][live], minlength=max(1, int(self.nonempty[b])))
+        return np.bincount(self.pos[s:e][live], minlength=max(1, int(self.extent[b])))
 
     def tile_entries(self, b, k0, k1, uncovered=None):
         """Entries of block b in positions [k0, k1]: (local row, local col, id)."""
@@ -310,7 +351,7 @@ class TcOp:
         return OpSpace(op_id=self.op_id, template=TC if self.op_type == "spmm" else TC_SDDMM,
                        i_perm=self.i_perm, k_perm=np.arange(self.pat.K, dtype=np.int64),
                        idx_reordered=(self.reordered, False, False),
-                       blk_k_vals=_LazyKvals(self))
+                       blk_k_vals=_LazyKvals(self), TC_k_notsorted=self.k_notsorted)
 
 
 class _BlockOrder:
@@ -415,9 +456,11 @@ def _sum_pred(tiles):
 class SpmmPlanner:
     def __init__(self, A, N, cost: CostModel = A100_FP16, max_bucket_size=None, only_TC=False,
                  only_ELL=False, max_avg_cost_diff=0.2, penalty=1, max_level_num=float("inf"),
-                 single_level=False, no_withdraw=False):
+                 single_level=False, no_withdraw=False, tc_k_notsorted=False):
         self.pat = Pattern(A)
         self.N = int(N)
+        self.tc_k_notsorted = bool(tc_k_notsorted)
+        self.tc_sizes = tc_tile_sizes("spmm", self.tc_k_notsorted)
         self.cost = cost
         self.mbs = max_bucket_size or estimate_max_bucket_size(self.pat.nnz, cost.sm_num)
         self.only_TC, self.only_ELL = only_TC, only_ELL
@@ -440,9 +483,10 @@ class SpmmPlanner:
         if not self.only_ELL:
             ident = np.arange(pat.M, dtype=np.int64)
             by_len = np.argsort(-pat.row_nnz, kind="stable")
-            cands = [TcOp(pat, ident, nid)]
+            kn = self.tc_k_notsorted
+            cands = [TcOp(pat, ident, nid, k_notsorted=kn)]
             if not np.array_equal(by_len, ident):
-                cands.append(TcOp(pat, by_len, nid))
+                cands.append(TcOp(pat, by_len, nid, k_notsorted=kn))
             best, bd = None, 0
             for c in cands:
                 d = c.density()
@@ -610,7 +654,7 @@ class SpmmPlanner:
         tot = np.bincount(blk, minlength=tc.n_blk)
         rel = pos // 16 - first[blk]
         best_key, best_cost = None, float("inf")
-        for ts in tc_tile_sizes():
+        for ts in self.tc_sizes:
             Kt = ts[2][1]
             w = Kt // 16
             if len(blk):
@@ -640,7 +684,7 @@ class SpmmPlanner:
             mc = np.nanmin(pavgs)
             if mc < best_cost:
                 best_cost = mc
-                best_key = (ts, [(mr, i) for i in range(int(nonempty[mr]))], False)
+                best_key = (ts, [(mr, i) for i in tc.row_positions(ts, mr)], False)
         return best_key, best_cost
 
     def _search_tc_block(self, b, counts, selected_row, best_possible_ell):
@@ -657,7 +701,7 @@ class SpmmPlanner:
         cs = np.concatenate([[0], np.cumsum(base)])
         best_key, best_cost = None, float("inf")
         unit = {}
-        for ts in tc_tile_sizes():
+        for ts in self.tc_sizes:
             Kt = ts[2][1]
             w = Kt // 16
             tmp = np.concatenate([cs, np.full(w - 1, cs[-1])])
@@ -684,7 +728,7 @@ class SpmmPlanner:
             pavgs = extra / tot / ts[1][1]
             if pavgs < best_cost and pavgs < best_possible_ell:
                 best_cost = pavgs
-                best_key = (ts, list(range(nonempty)), False)
+                best_key = (ts, tc.row_positions(ts, b), False)
         return best_key, best_cost, unit
 
     def _local_tc_block(self, b, counts, ts, target, no_atomic, atomic_cost, selected_row):
@@ -707,7 +751,7 @@ class SpmmPlanner:
         pavg = extra / np.sum(nnz_upd) / ts[1][1]
         if pavg <= target:
             out = []
-            for i in range(nonempty):
+            for i in self.tc.row_positions(ts, b):
                 t = self._tc_tile(b, ts, i, False, False)
                 t.pred_cost = no_atomic
                 out.append(t)
@@ -732,7 +776,7 @@ class SpmmPlanner:
         if self.single_level:
             first = first * 0
         tot = np.bincount(blk, minlength=tc.n_blk)
-        tsl = tc_tile_sizes()
+        tsl = self.tc_sizes
         nonempty = np.asarray([tc.blk_nums[t] for t in tsl])
         no_atomic = np.asarray([self.cost.tc_cost(t[2][1], False, self.penalty) for t in tsl])
         extra = no_atomic.reshape(-1, 1) * nonempty - TC_row_costs
@@ -746,7 +790,7 @@ class SpmmPlanner:
         good = []
         for r in sel_rows:
             t_ts = tsl[cand[r]]
-            for i in range(int(nonempty[cand[r]][r])):
+            for i in tc.row_positions(t_ts, int(r)):
                 t = self._tc_tile(int(r), t_ts, i, False, False)
                 t.pred_cost = no_atomic[cand[r]]
                 t.best_ts = t_ts
@@ -1005,9 +1049,10 @@ class SddmmPlanner:
     local_search_1D_BSDDMM; post_process_for_withdraw_BSDDMM :1709-1751)."""
 
     def __init__(self, A, F, cost: CostModel = A100_FP16, max_bucket_size=32, only_TC=False, only_ELL=False,
-                 max_avg_cost_diff=0.2, max_level_num=float("inf"), single_level=False):
+                 max_avg_cost_diff=0.2, max_level_num=float("inf"), single_level=False, tc_k_notsorted=False):
         self.pat = Pattern(A)
         self.F = int(F)
+        self.tc_k_notsorted = bool(tc_k_notsorted)
         self.cost = cost
         self.mbs = max_bucket_size
         self.only_TC, self.only_ELL = only_TC, only_ELL
@@ -1017,6 +1062,8 @@ class SddmmPlanner:
         self.uncovered = np.ones(self.pat.nnz, dtype=bool)
         js = [j for j in (16, 32, 64) if j <= self.F]
         self.tile_j = max(js) if js else None
+        if self.tc_k_notsorted:
+            self.tile_j = tc_tile_sizes("sddmm", True)[0][1][1]
 
     def _ts(self):
         return ((None, 16), (None, self.tile_j), (None, 16))
@@ -1036,9 +1083,10 @@ class SddmmPlanner:
         if not self.only_ELL and self.tile_j is not None:
             ident = np.arange(pat.M, dtype=np.int64)
             by_len = np.argsort(-pat.row_nnz, kind="stable")
-            cands = [TcOp(pat, ident, nid, op_type="sddmm")]
+            kn = self.tc_k_notsorted
+            cands = [TcOp(pat, ident, nid, op_type="sddmm", k_notsorted=kn)]
             if not np.array_equal(by_len, ident):
-                cands.append(TcOp(pat, by_len, nid, op_type="sddmm"))
+                cands.append(TcOp(pat, by_len, nid, op_type="sddmm", k_notsorted=kn))
             best, bd = None, 0
             for c in cands:
                 d = c.density()

@@ -173,6 +173,14 @@ def _cases():
         "spmm_pruned_256x192_tc": dict(op="spmm",
                                        A=lambda: _ones(syn.pruned_weight(256, 192, seed=6)),
                                        N=64, only_TC=True, only_ELL=False),
+        # block-structured weights with the tensor-core columns kept in their
+        # order (TC_k_notsorted): tiles are 16x16 blocks on the column grid
+        "spmm_blockpruned_768x512_knots": dict(
+            op="spmm", A=lambda: _ones(syn.pruned_weight(768, 512, sparsity=0.95, block_frac=0.8, seed=21)),
+            N=64, only_TC=False, only_ELL=False, TC_k_notsorted=True),
+        "spmm_blockpruned_768x512_knots_tc": dict(
+            op="spmm", A=lambda: _ones(syn.pruned_weight(768, 512, sparsity=0.95, block_frac=0.8, seed=22)),
+            N=64, only_TC=True, only_ELL=False, TC_k_notsorted=True),
         # SDDMM mask: power-law rows + dense 32x16 blocks
         "sddmm_mask_1024": dict(op="sddmm",
                                 A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
@@ -180,6 +188,9 @@ def _cases():
         "sddmm_mask_2048": dict(op="sddmm",
                                 A=lambda: syn.sddmm_mask(n=2048, target_nnz=40000, seed=8, max_len=512),
                                 N=32, only_TC=False, only_ELL=False),
+        "sddmm_mask_1024_knots": dict(op="sddmm",
+                                      A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
+                                      N=64, only_TC=False, only_ELL=False, TC_k_notsorted=True),
     }
 
 
@@ -251,7 +262,8 @@ def run_reference(mods, case):
     op_type = case["op"]
     os.environ["op_type"] = op_type
     os.environ["single_level"] = "False"
-    os.environ["TC_k_notsorted"] = "False"
+    knots = bool(case.get("TC_k_notsorted", False))
+    os.environ["TC_k_notsorted"] = str(knots)
     os.environ["no_withdraw"] = "False"
     os.environ["REMAP"] = "False"
     os.environ.pop("TC_tile_sizes", None)
@@ -275,7 +287,7 @@ def run_reference(mods, case):
     with contextlib.redirect_stdout(log):
         res = S.greedy_search_use_cost_model_lower_bound(
             op, dsize, {"summarize_nnz_iter_space": (True, True)}, mbs, cache_set,
-            kernel_tile_size_options, only_TC, only_ELL, 1, False,
+            kernel_tile_size_options, only_TC, only_ELL, 1, knots,
             reorder_k_by_nnz=True, max_level_num=float("inf"),
             max_avg_cost_diff=max_avg_cost_diff, use_faster_tuner=True,
             log_file="log.py", cuda_i=0, dtype="float16", dtype_str='"float16"',
@@ -297,7 +309,8 @@ def serialise(mods, case_name, case, op, A, mbs, selected, TC_row_costs, reverse
     out = {}
     meta = {"name": case_name, "op": case["op"], "N": case["N"], "idx_lens": list(map(int, op.idx_lens)),
             "orig_shape": list(map(int, A.shape)), "max_bucket_size": int(mbs),
-            "only_TC": case["only_TC"], "only_ELL": case["only_ELL"], "search_s": t_search}
+            "only_TC": case["only_TC"], "only_ELL": case["only_ELL"],
+            "TC_k_notsorted": bool(case.get("TC_k_notsorted", False)), "search_s": t_search}
     Ar = op.inps[0]
     out["A_indptr"] = Ar.indptr.astype(np.int32)
     out["A_indices"] = Ar.indices.astype(np.int32)
@@ -317,7 +330,8 @@ def serialise(mods, case_name, case, op, A, mbs, selected, TC_row_costs, reverse
         pre = f"op{oid}_"
         out[pre + "i_vals"] = np.asarray(o.idx_values_list[0][0], dtype=np.int32)
         out[pre + "k_vals"] = np.asarray(o.idx_values_list[0][2], dtype=np.int32)
-        om = {"op_id": int(oid), "template": tpl, "idx_reordered": [bool(x) for x in o.idx_reordered[0]]}
+        om = {"op_id": int(oid), "template": tpl, "idx_reordered": [bool(x) for x in o.idx_reordered[0]],
+              "TC_k_notsorted": bool(getattr(o, "TC_k_notsorted", False))}
         if tpl == "sparse_template_ell":
             out[pre + "hyb_new_rows"] = np.asarray(o.hyb_new_rows[0], dtype=np.int32)
             out[pre + "hyb_ori_row_ends"] = np.asarray(o.hyb_ori_row_ends, dtype=np.int32)
@@ -408,6 +422,9 @@ def serialise(mods, case_name, case, op, A, mbs, selected, TC_row_costs, reverse
         if n < n_dense:
             continue
         a = np.asarray(a)
+        if a.dtype == object:
+            # k-block positions of TC_k_notsorted tiles (integral Fractions)
+            a = a.astype(np.int64)
         if a.dtype.kind == "f" and a.size and np.all(a == 0):
             meta.setdefault("zero_args", {})[str(n)] = list(a.shape)
             continue

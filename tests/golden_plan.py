@@ -22,7 +22,8 @@ def plan_from_fixture(meta, arrays):
         op = OpSpace(op_id=oid, template=om["template"],
                      i_perm=arrays[pre + "i_vals"].astype(np.int64),
                      k_perm=arrays[pre + "k_vals"].astype(np.int64),
-                     idx_reordered=tuple(om["idx_reordered"]))
+                     idx_reordered=tuple(om["idx_reordered"]),
+                     TC_k_notsorted=bool(om.get("TC_k_notsorted", False)))
         if om["template"] == ELL:
             op.hyb_new_rows = arrays[pre + "hyb_new_rows"].astype(np.int64)
             op.hyb_ori_row_ends = arrays[pre + "hyb_ori_row_ends"].astype(np.int64)

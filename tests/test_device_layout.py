@@ -30,6 +30,27 @@ def test_device_layout_executes_to_fp64(path):
     assert len(ids) == A.nnz
 
 
+@pytest.mark.parametrize("shape", [(768, 512), (200, 300)])
+def test_column_block_plan_layout(shape):
+    """A searched plan with the tensor-core columns kept in order
+    (TC_k_notsorted): every tensor-core k-step reads 16 consecutive columns
+    from a multiple of 16 (clamped at the last column when K is not a
+    multiple of 16) and the layout executes to the float64 product."""
+    from stile_gb300 import synthetic as syn
+    from stile_gb300.planner import search_spmm
+    A = syn.pruned_weight(*shape, sparsity=0.93, block_frac=0.7, seed=3)
+    plan = search_spmm(A, 64, tc_k_notsorted=True)
+    dev = D.build_spmm_device(plan.tiles, A, N=64)
+    cols = dev.tc_cols.astype(np.int64).reshape(-1, 16)
+    assert len(cols) > 0
+    assert np.all(cols[:, 0] % 16 == 0)
+    assert np.array_equal(cols, np.minimum(cols[:, :1] + np.arange(16), A.shape[1] - 1))
+    B = np.random.default_rng(1).standard_normal((A.shape[1], 64))
+    C = spmm_device_exec(dev, B)
+    assert not np.isnan(C).any()
+    assert S.rel_fro(C, S.spmm_fp64(A, B)) < 1e-6
+
+
 def test_bf16_rounding_matches_torch():
     import torch
     x = np.random.default_rng(0).standard_normal(10000).astype(np.float32) * 100

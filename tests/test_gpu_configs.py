@@ -16,8 +16,8 @@ from stile_gb300.api import PlanConfig, SddmmOperator, SpmmOperator
 pytestmark = pytest.mark.gpu
 
 
-def _spmm_products(w, tc_mode):
-    op = SpmmOperator(w.A, w.width, PlanConfig(tc_mode=tc_mode))
+def _spmm_products(w, tc_mode, **cfg):
+    op = SpmmOperator(w.A, w.width, PlanConfig(tc_mode=tc_mode, **cfg))
     B = torch.as_tensor(w.dense["B"], device="cuda")
     dC = torch.as_tensor(w.dense["dC"], device="cuda")
     C = op(B)
@@ -29,8 +29,8 @@ def _spmm_products(w, tc_mode):
     return op, C.cpu().numpy(), dB.cpu().numpy(), dv.cpu().numpy()
 
 
-def _check_spmm(w, tc_mode, tol):
-    op, C, dB, dv = _spmm_products(w, tc_mode)
+def _check_spmm(w, tc_mode, tol, **cfg):
+    op, C, dB, dv = _spmm_products(w, tc_mode, **cfg)
     A = op.A
     assert S.rel_fro(C, S.spmm_fp64(A, w.dense["B"])) <= tol
     assert S.rel_fro(dB, S.spmm_fp64(A.T.tocsr(), w.dense["dC"])) <= tol
@@ -51,6 +51,19 @@ def test_config3_pruned_weight_bf16_tiles(name):
     op = _check_spmm(w, D.TC_BF16, 1e-2)
     # the block-pruned half of the weight goes to the tensor cores
     assert op.device_layout.stats()["tc_ksteps"] > 0
+
+
+@pytest.mark.parametrize("name", ["pruned", "pruned_t"])
+def test_config3_pruned_weight_column_blocks(name):
+    """Tensor-core tiles as 16x16 blocks on the column grid (TC_k_notsorted):
+    every tensor-core k-step reads 16 consecutive columns starting at a
+    multiple of 16, and the products match float64."""
+    w = W.BY_NAME[name]()
+    op = _check_spmm(w, D.TC_BF16, 1e-2, tc_k_notsorted=True)
+    cols = op.device_layout.tc_cols.astype(np.int64).reshape(-1, 16)
+    assert len(cols) > 0
+    assert np.all(cols[:, 0] % 16 == 0)
+    assert np.all(cols == np.minimum(cols[:, :1] + np.arange(16), w.A.shape[1] - 1))
 
 
 def test_config3_pruned_weight_fp32_path():

@@ -15,7 +15,7 @@ def test_spmm_plan_matches_reference(path):
     meta, arr = S.load_fixture(path)
     A = S.fixture_matrix(meta, arr)
     plan = plan_spmm(A, meta["N"], max_bucket_size=meta["max_bucket_size"], only_TC=meta["only_TC"],
-                     only_ELL=meta["only_ELL"])
+                     only_ELL=meta["only_ELL"], tc_k_notsorted=meta.get("TC_k_notsorted", False))
     fm, args, out_shape = emit.emit_spmm_reference(plan.tiles, meta["idx_lens"][0], meta["N"])
     assert list(out_shape) == meta["out_shape"]
     assert [f.template for f in fm] == [f["template"] for f in meta["formats"]]
@@ -40,7 +40,8 @@ def test_sddmm_plan_matches_reference(path):
     from stile_gb300.planner import plan_sddmm
     meta, arr = S.load_fixture(path)
     A = S.fixture_matrix(meta, arr)
-    plan = plan_sddmm(A, meta["N"], max_bucket_size=meta["max_bucket_size"])
+    plan = plan_sddmm(A, meta["N"], max_bucket_size=meta["max_bucket_size"],
+                      tc_k_notsorted=meta.get("TC_k_notsorted", False))
     fm, args = emit.emit_sddmm_reference(plan.tiles)
     assert [f.template for f in fm] == [f["template"] for f in meta["formats"]]
     assert [len(f.tiles) for f in fm] == [f["n_tiles"] for f in meta["formats"]]
