@@ -188,6 +188,12 @@ def _cases():
         "sddmm_mask_2048": dict(op="sddmm",
                                 A=lambda: syn.sddmm_mask(n=2048, target_nnz=40000, seed=8, max_len=512),
                                 N=32, only_TC=False, only_ELL=False),
+        "sddmm_mask_1024_tc": dict(op="sddmm",
+                                   A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
+                                   N=64, only_TC=True, only_ELL=False),
+        "sddmm_mask_1024_knots_tc": dict(op="sddmm",
+                                         A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
+                                         N=64, only_TC=True, only_ELL=False, TC_k_notsorted=True),
         "sddmm_mask_1024_knots": dict(op="sddmm",
                                       A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
                                       N=64, only_TC=False, only_ELL=False, TC_k_notsorted=True),

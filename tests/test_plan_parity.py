@@ -40,8 +40,8 @@ def test_sddmm_plan_matches_reference(path):
     from stile_gb300.planner import plan_sddmm
     meta, arr = S.load_fixture(path)
     A = S.fixture_matrix(meta, arr)
-    plan = plan_sddmm(A, meta["N"], max_bucket_size=meta["max_bucket_size"],
-                      tc_k_notsorted=meta.get("TC_k_notsorted", False))
+    plan = plan_sddmm(A, meta["N"], max_bucket_size=meta["max_bucket_size"], only_TC=meta["only_TC"],
+                      only_ELL=meta["only_ELL"], tc_k_notsorted=meta.get("TC_k_notsorted", False))
     fm, args = emit.emit_sddmm_reference(plan.tiles)
     assert [f.template for f in fm] == [f["template"] for f in meta["formats"]]
     assert [len(f.tiles) for f in fm] == [f["n_tiles"] for f in meta["formats"]]
