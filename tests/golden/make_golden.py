@@ -188,6 +188,16 @@ def _cases():
         "sddmm_mask_2048": dict(op="sddmm",
                                 A=lambda: syn.sddmm_mask(n=2048, target_nnz=40000, seed=8, max_len=512),
                                 N=32, only_TC=False, only_ELL=False),
+        # the ablation switches: one level of operators (max_level_num 1) and
+        # whole-row tensor-core tiles costed without withdraw
+        "spmm_community_1024_single_level": dict(
+            op="spmm", A=lambda: syn.community_graph(n=1024, target_nnz=12000, seed=3, values="ones", max_deg=256),
+            N=128, only_TC=False, only_ELL=False, single_level=True),
+        "spmm_hubblocks_4096_no_withdraw": dict(op="spmm", A=lambda: _hub_blocks(4096, 4, 60, 1500), N=64,
+                                                only_TC=False, only_ELL=False, no_withdraw=True),
+        "sddmm_mask_1024_single_level": dict(
+            op="sddmm", A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
+            N=64, only_TC=False, only_ELL=False, single_level=True),
         "sddmm_mask_1024_tc": dict(op="sddmm",
                                    A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
                                    N=64, only_TC=True, only_ELL=False),
@@ -267,10 +277,11 @@ def run_reference(mods, case):
     G, S, BB, F, CM = mods
     op_type = case["op"]
     os.environ["op_type"] = op_type
-    os.environ["single_level"] = "False"
+    single = bool(case.get("single_level", False))
+    os.environ["single_level"] = str(single)
     knots = bool(case.get("TC_k_notsorted", False))
     os.environ["TC_k_notsorted"] = str(knots)
-    os.environ["no_withdraw"] = "False"
+    os.environ["no_withdraw"] = str(bool(case.get("no_withdraw", False)))
     os.environ["REMAP"] = "False"
     os.environ.pop("TC_tile_sizes", None)
     os.environ["other_cost_model"] = "analytic"
@@ -294,7 +305,7 @@ def run_reference(mods, case):
         res = S.greedy_search_use_cost_model_lower_bound(
             op, dsize, {"summarize_nnz_iter_space": (True, True)}, mbs, cache_set,
             kernel_tile_size_options, only_TC, only_ELL, 1, knots,
-            reorder_k_by_nnz=True, max_level_num=float("inf"),
+            reorder_k_by_nnz=True, max_level_num=1 if single else float("inf"),
             max_avg_cost_diff=max_avg_cost_diff, use_faster_tuner=True,
             log_file="log.py", cuda_i=0, dtype="float16", dtype_str='"float16"',
             zerotype="T.float16(0)")
@@ -316,7 +327,9 @@ def serialise(mods, case_name, case, op, A, mbs, selected, TC_row_costs, reverse
     meta = {"name": case_name, "op": case["op"], "N": case["N"], "idx_lens": list(map(int, op.idx_lens)),
             "orig_shape": list(map(int, A.shape)), "max_bucket_size": int(mbs),
             "only_TC": case["only_TC"], "only_ELL": case["only_ELL"],
-            "TC_k_notsorted": bool(case.get("TC_k_notsorted", False)), "search_s": t_search}
+            "TC_k_notsorted": bool(case.get("TC_k_notsorted", False)),
+            "single_level": bool(case.get("single_level", False)),
+            "no_withdraw": bool(case.get("no_withdraw", False)), "search_s": t_search}
     Ar = op.inps[0]
     out["A_indptr"] = Ar.indptr.astype(np.int32)
     out["A_indices"] = Ar.indices.astype(np.int32)

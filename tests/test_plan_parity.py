@@ -10,12 +10,21 @@ from stile_gb300 import emit
 from stile_gb300.planner import search_spmm as plan_spmm
 
 
+def _switches(meta):
+    """The search switches the fixture was made with (the reference's
+    TC_k_notsorted and single_level env variables; single_level runs with
+    max_level_num 1, as the reference asserts)."""
+    single = meta.get("single_level", False)
+    return dict(tc_k_notsorted=meta.get("TC_k_notsorted", False), single_level=single,
+                max_level_num=1 if single else float("inf"))
+
+
 @pytest.mark.parametrize("path", golden_files("spmm"), ids=lambda p: p.split("/")[-1][:-4])
 def test_spmm_plan_matches_reference(path):
     meta, arr = S.load_fixture(path)
     A = S.fixture_matrix(meta, arr)
     plan = plan_spmm(A, meta["N"], max_bucket_size=meta["max_bucket_size"], only_TC=meta["only_TC"],
-                     only_ELL=meta["only_ELL"], tc_k_notsorted=meta.get("TC_k_notsorted", False))
+                     only_ELL=meta["only_ELL"], no_withdraw=meta.get("no_withdraw", False), **_switches(meta))
     fm, args, out_shape = emit.emit_spmm_reference(plan.tiles, meta["idx_lens"][0], meta["N"])
     assert list(out_shape) == meta["out_shape"]
     assert [f.template for f in fm] == [f["template"] for f in meta["formats"]]
@@ -41,7 +50,7 @@ def test_sddmm_plan_matches_reference(path):
     meta, arr = S.load_fixture(path)
     A = S.fixture_matrix(meta, arr)
     plan = plan_sddmm(A, meta["N"], max_bucket_size=meta["max_bucket_size"], only_TC=meta["only_TC"],
-                      only_ELL=meta["only_ELL"], tc_k_notsorted=meta.get("TC_k_notsorted", False))
+                      only_ELL=meta["only_ELL"], **_switches(meta))
     fm, args = emit.emit_sddmm_reference(plan.tiles)
     assert [f.template for f in fm] == [f["template"] for f in meta["formats"]]
     assert [len(f.tiles) for f in fm] == [f["n_tiles"] for f in meta["formats"]]
