@@ -198,6 +198,12 @@ def _cases():
         "sddmm_mask_1024_single_level": dict(
             op="sddmm", A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
             N=64, only_TC=False, only_ELL=False, single_level=True),
+        # the local-search ablation (my_run_localsearch.py: cost window 1e-6)
+        "spmm_mixed_2048_window0": dict(op="spmm", A=lambda: _mixed_blocks(2048, 1, 40, 8, 256), N=64,
+                                        only_TC=False, only_ELL=False, max_avg_cost_diff=1e-6),
+        "sddmm_mask_1024_1d": dict(op="sddmm",
+                                   A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
+                                   N=64, only_TC=False, only_ELL=True),
         "sddmm_mask_1024_tc": dict(op="sddmm",
                                    A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
                                    N=64, only_TC=True, only_ELL=False),
@@ -292,7 +298,7 @@ def run_reference(mods, case):
     dsize = 16
     cache_set = ["A"]
     kernel_tile_size_options = ([1], [1], [1])
-    max_avg_cost_diff = 0.2
+    max_avg_cost_diff = case.get("max_avg_cost_diff", 0.2)
     only_TC, only_ELL = case["only_TC"], case["only_ELL"]
     if only_ELL:
         max_avg_cost_diff = float("inf")
@@ -329,7 +335,8 @@ def serialise(mods, case_name, case, op, A, mbs, selected, TC_row_costs, reverse
             "only_TC": case["only_TC"], "only_ELL": case["only_ELL"],
             "TC_k_notsorted": bool(case.get("TC_k_notsorted", False)),
             "single_level": bool(case.get("single_level", False)),
-            "no_withdraw": bool(case.get("no_withdraw", False)), "search_s": t_search}
+            "no_withdraw": bool(case.get("no_withdraw", False)),
+            "max_avg_cost_diff": case.get("max_avg_cost_diff", 0.2), "search_s": t_search}
     Ar = op.inps[0]
     out["A_indptr"] = Ar.indptr.astype(np.int32)
     out["A_indices"] = Ar.indices.astype(np.int32)

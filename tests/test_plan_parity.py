@@ -16,7 +16,8 @@ def _switches(meta):
     max_level_num 1, as the reference asserts)."""
     single = meta.get("single_level", False)
     return dict(tc_k_notsorted=meta.get("TC_k_notsorted", False), single_level=single,
-                max_level_num=1 if single else float("inf"))
+                max_level_num=1 if single else float("inf"),
+                max_avg_cost_diff=meta.get("max_avg_cost_diff", 0.2))
 
 
 @pytest.mark.parametrize("path", golden_files("spmm"), ids=lambda p: p.split("/")[-1][:-4])
