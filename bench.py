@@ -663,6 +663,17 @@ def run_config(args):
                                     "bf16_B_forward_ms": timed(lambda: op_b(B16, out=C16), args.steps),
                                     "C_rel_fro": S.rel_fro(Cb.cpu().numpy(), S.spmm_fp64(A, B_np))}
             op_b.handle.close()
+            # context: the zero-filled weight as a dense bf16 GEMM (cuBLAS
+            # through torch.matmul, bf16 output) on the same activations
+            Wd = torch.as_tensor(A.toarray(), device=dev).to(torch.bfloat16)
+            Cd = torch.empty((A.shape[0], N), device=dev, dtype=torch.bfloat16)
+            torch.matmul(Wd, B16, out=Cd)
+            torch.cuda.synchronize()
+            out["dense_bf16_gemm"] = {"forward_ms": timed(lambda: torch.matmul(Wd, B16, out=Cd), args.steps),
+                                      "flop": 2 * A.shape[0] * A.shape[1] * N,
+                                      "C_rel_fro": S.rel_fro(Cd.float().cpu().numpy(),
+                                                             S.spmm_fp64(A, B16.float().cpu().numpy()))}
+            del Wd, Cd
             # the plan chosen by the learned cost model against the analytic one
             try:
                 t0 = time.time()

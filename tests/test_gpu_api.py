@@ -164,11 +164,14 @@ def test_autograd_with_bf16_operand():
 
 @pytest.mark.parametrize("N", [64, 128])
 @pytest.mark.parametrize("mode", [D.TC_BF16, D.TC_SPLIT_BF16], ids=["bf16", "split"])
-def test_batched_heads_match_one_head_at_a_time(N, mode):
+@pytest.mark.parametrize("knots", [False, True], ids=["sorted", "column_blocks"])
+def test_batched_heads_match_one_head_at_a_time(N, mode, knots):
     """Several value sets on one pattern in one launch per kernel give what
-    set_values + a single run give for each head."""
+    set_values + a single run give for each head (tensor-core columns
+    count-sorted, or in column order: the reference's batched TC_k_notsorted
+    kernel)."""
     A = _graph(seed=10)
-    op = plan_spmm(A, N, PlanConfig(tc_mode=mode))
+    op = plan_spmm(A, N, PlanConfig(tc_mode=mode, tc_k_notsorted=knots))
     H = 3
     rng = np.random.default_rng(4)
     vals = torch.as_tensor(rng.uniform(-1, 1, (H, A.nnz)).astype(np.float32), device="cuda")
