@@ -36,6 +36,16 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def errors(name, x, ref):
+    """Relative Frobenius and max-abs error of x against its float64
+    reference."""
+    x = np.asarray(x, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    den = np.linalg.norm(ref)
+    return {f"{name}_rel_fro": float(np.linalg.norm(x - ref) / (den if den > 0 else 1.0)),
+            f"{name}_max_abs": float(np.abs(x - ref).max()) if x.size else 0.0}
+
+
 def make_workload(seed=0):
     from stile_gb300 import workloads as W
     w = W.graph(seed)
@@ -357,10 +367,10 @@ def run_gpu(args):
     hybrid_step()
     torch.cuda.synchronize()
     dv = op.dvals(dC, B)
-    acc = {"C_rel_fro": S.rel_fro(C.cpu().numpy(), S.spmm_fp64(A, B_np)),
-           "dvals_rel_fro": S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC_np, B_np)),
-           "dB_rel_fro": S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(AT, dC_np))}
-    acc["C_max_abs"] = float(np.abs(C.cpu().numpy() - S.spmm_fp64(A, B_np)).max())
+    acc = {}
+    acc.update(errors("C", C.cpu().numpy(), S.spmm_fp64(A, B_np)))
+    acc.update(errors("dvals", dv.cpu().numpy(), S.sddmm_fp64(A, dC_np, B_np)))
+    acc.update(errors("dB", dB.cpu().numpy(), S.spmm_fp64(AT, dC_np)))
     log(f"[bench] accuracy {acc}")
 
     def timed(fn, steps, per_step_events=False):
@@ -609,9 +619,9 @@ def run_config(args):
         dv = op.dvals(dC, B)
         torch.cuda.synchronize()
         ids, ref = W.sddmm_fp64_sample(A, dC_np, B_np)
-        out["accuracy"] = {"C_rel_fro": S.rel_fro(C.cpu().numpy(), S.spmm_fp64(A, B_np)),
-                           "dB_rel_fro": S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(AT, dC_np)),
-                           "dvals_rel_fro_sampled": S.rel_fro(dv.cpu().numpy()[ids], ref),
+        out["accuracy"] = {**errors("C", C.cpu().numpy(), S.spmm_fp64(A, B_np)),
+                           **errors("dB", dB.cpu().numpy(), S.spmm_fp64(AT, dC_np)),
+                           **errors("dvals_sampled", dv.cpu().numpy()[ids], ref),
                            "dvals_sample": int(len(ids))}
         ms_step = timed(step, args.steps)
         ms_fwd = timed(lambda: op(B, out=C), args.steps)
@@ -699,7 +709,7 @@ def run_config(args):
         res = op(X, Y)
         torch.cuda.synchronize()
         ids, ref = W.sddmm_fp64_sample(A, X_np, Y_np)
-        out["accuracy"] = {"rel_fro_sampled": S.rel_fro(res.cpu().numpy()[ids], ref), "sample": int(len(ids))}
+        out["accuracy"] = {**errors("out_sampled", res.cpu().numpy()[ids], ref), "sample": int(len(ids))}
         ms = timed(lambda: op(X, Y), args.steps)
         plain_dev = D.SddmmDevice(M=A.shape[0], K=A.shape[1], nnz=A.nnz,
                                   mid_idx=np.repeat(np.arange(A.shape[0]), np.diff(A.indptr)).astype(np.int32),
