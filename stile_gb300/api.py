@@ -47,6 +47,9 @@ class PlanConfig:
     # tensor-core tiles as 16x16 blocks on the column grid, columns kept in
     # order (the reference's TC_k_notsorted, for block-structured sparsity)
     tc_k_notsorted: bool = False
+    # count-sorted tensor-core columns (the reference's reorder_k_by_nnz);
+    # False: non-empty columns first, in column order
+    reorder_k_by_nnz: bool = True
 
     def search_kwargs(self):
         cost = self.cost_model
@@ -56,7 +59,7 @@ class PlanConfig:
         return dict(cost=cost, max_bucket_size=self.max_bucket_size, only_TC=self.only_TC,
                     only_ELL=self.only_ELL, max_avg_cost_diff=self.max_avg_cost_diff,
                     single_level=self.single_level, max_level_num=self.max_level_num,
-                    tc_k_notsorted=self.tc_k_notsorted)
+                    tc_k_notsorted=self.tc_k_notsorted, reorder_k_by_nnz=self.reorder_k_by_nnz)
 
 
 def _csr(A):
@@ -279,9 +282,6 @@ def greedy_search_use_cost_model_lower_bound(op: Op, dsize=16, run_params=None, 
                                              zerotype=None, cost_model: CostModel | None = None):
     """Returns (plan, None, None, None, level_num) in the reference's tuple
     shape; the withdraw bookkeeping is already folded into ``plan``."""
-    if not reorder_k_by_nnz:
-        raise NotImplementedError("reorder_k_by_nnz=False (non-empty columns first, in column order) "
-                                  "is not supported")
     cost = cost_model or (A100_FP16 if dsize == 16 else gb300_model())
     if op.op_type == "spmm":
         plan = search_spmm(op.A, op.idx_lens[1], cost=cost, max_bucket_size=max_bucket_size, only_TC=only_TC,

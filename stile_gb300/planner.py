@@ -210,9 +210,12 @@ class TcOp:
     sorted by decreasing count (condense_for_TC_tile :1004-1039), or, with
     ``k_notsorted`` (TC_k_notsorted, :1025-1031 and set_init_blk_nums
     :1328-1335), kept in column order, so that a tile at k position p is the
-    16-column block [16p, 16p + 16) and only non-empty blocks are tiles."""
+    16-column block [16p, 16p + 16) and only non-empty blocks are tiles.
+    ``k_by_count=False`` (reorder_k_by_nnz=False, :1036-1038) puts the
+    non-empty columns first in column order instead of by decreasing count."""
 
-    def __init__(self, pat: Pattern, i_perm, op_id, op_type="spmm", ids=None, bs=16, k_notsorted=False):
+    def __init__(self, pat: Pattern, i_perm, op_id, op_type="spmm", ids=None, bs=16, k_notsorted=False,
+                 k_by_count=True):
         self.pat = pat
         self.op_id = op_id
         self.bs = bs
@@ -233,7 +236,8 @@ class TcOp:
         ucode, uinv, cnt = np.unique(code, return_inverse=True, return_counts=True)
         ublk = ucode // pat.K
         ucol = ucode % pat.K
-        if self.k_notsorted:
+        if self.k_notsorted or not k_by_count:
+            # np.unique's order: by block, then column
             o = np.arange(len(ucode))
         else:
             o = np.lexsort((ucol, -cnt, ublk))
@@ -456,10 +460,11 @@ def _sum_pred(tiles):
 class SpmmPlanner:
     def __init__(self, A, N, cost: CostModel = A100_FP16, max_bucket_size=None, only_TC=False,
                  only_ELL=False, max_avg_cost_diff=0.2, penalty=1, max_level_num=float("inf"),
-                 single_level=False, no_withdraw=False, tc_k_notsorted=False):
+                 single_level=False, no_withdraw=False, tc_k_notsorted=False, reorder_k_by_nnz=True):
         self.pat = Pattern(A)
         self.N = int(N)
         self.tc_k_notsorted = bool(tc_k_notsorted)
+        self.k_by_count = bool(reorder_k_by_nnz)
         self.tc_sizes = tc_tile_sizes("spmm", self.tc_k_notsorted)
         self.cost = cost
         self.mbs = max_bucket_size or estimate_max_bucket_size(self.pat.nnz, cost.sm_num)
@@ -483,10 +488,10 @@ class SpmmPlanner:
         if not self.only_ELL:
             ident = np.arange(pat.M, dtype=np.int64)
             by_len = np.argsort(-pat.row_nnz, kind="stable")
-            kn = self.tc_k_notsorted
-            cands = [TcOp(pat, ident, nid, k_notsorted=kn)]
+            kw = dict(k_notsorted=self.tc_k_notsorted, k_by_count=self.k_by_count)
+            cands = [TcOp(pat, ident, nid, **kw)]
             if not np.array_equal(by_len, ident):
-                cands.append(TcOp(pat, by_len, nid, k_notsorted=kn))
+                cands.append(TcOp(pat, by_len, nid, **kw))
             best, bd = None, 0
             for c in cands:
                 d = c.density()
@@ -1049,10 +1054,12 @@ class SddmmPlanner:
     local_search_1D_BSDDMM; post_process_for_withdraw_BSDDMM :1709-1751)."""
 
     def __init__(self, A, F, cost: CostModel = A100_FP16, max_bucket_size=32, only_TC=False, only_ELL=False,
-                 max_avg_cost_diff=0.2, max_level_num=float("inf"), single_level=False, tc_k_notsorted=False):
+                 max_avg_cost_diff=0.2, max_level_num=float("inf"), single_level=False, tc_k_notsorted=False,
+                 reorder_k_by_nnz=True):
         self.pat = Pattern(A)
         self.F = int(F)
         self.tc_k_notsorted = bool(tc_k_notsorted)
+        self.k_by_count = bool(reorder_k_by_nnz)
         self.cost = cost
         self.mbs = max_bucket_size
         self.only_TC, self.only_ELL = only_TC, only_ELL
@@ -1083,10 +1090,10 @@ class SddmmPlanner:
         if not self.only_ELL and self.tile_j is not None:
             ident = np.arange(pat.M, dtype=np.int64)
             by_len = np.argsort(-pat.row_nnz, kind="stable")
-            kn = self.tc_k_notsorted
-            cands = [TcOp(pat, ident, nid, op_type="sddmm", k_notsorted=kn)]
+            kw = dict(op_type="sddmm", k_notsorted=self.tc_k_notsorted, k_by_count=self.k_by_count)
+            cands = [TcOp(pat, ident, nid, **kw)]
             if not np.array_equal(by_len, ident):
-                cands.append(TcOp(pat, by_len, nid, op_type="sddmm", k_notsorted=kn))
+                cands.append(TcOp(pat, by_len, nid, **kw))
             best, bd = None, 0
             for c in cands:
                 d = c.density()

@@ -204,6 +204,12 @@ def _cases():
         "sddmm_mask_1024_1d": dict(op="sddmm",
                                    A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
                                    N=64, only_TC=False, only_ELL=True),
+        # tensor-core columns: non-empty first in column order
+        # (reorder_k_by_nnz=False)
+        "spmm_community_2048_kfirst": dict(op="spmm",
+                                           A=lambda: syn.community_graph(n=2048, target_nnz=30000, seed=4,
+                                                                         values="ones", max_deg=512),
+                                           N=128, only_TC=False, only_ELL=False, reorder_k_by_nnz=False),
         "sddmm_mask_1024_tc": dict(op="sddmm",
                                    A=lambda: syn.sddmm_mask(n=1024, target_nnz=16000, seed=7, max_len=256),
                                    N=64, only_TC=True, only_ELL=False),
@@ -311,7 +317,7 @@ def run_reference(mods, case):
         res = S.greedy_search_use_cost_model_lower_bound(
             op, dsize, {"summarize_nnz_iter_space": (True, True)}, mbs, cache_set,
             kernel_tile_size_options, only_TC, only_ELL, 1, knots,
-            reorder_k_by_nnz=True, max_level_num=1 if single else float("inf"),
+            reorder_k_by_nnz=case.get("reorder_k_by_nnz", True), max_level_num=1 if single else float("inf"),
             max_avg_cost_diff=max_avg_cost_diff, use_faster_tuner=True,
             log_file="log.py", cuda_i=0, dtype="float16", dtype_str='"float16"',
             zerotype="T.float16(0)")
@@ -336,7 +342,8 @@ def serialise(mods, case_name, case, op, A, mbs, selected, TC_row_costs, reverse
             "TC_k_notsorted": bool(case.get("TC_k_notsorted", False)),
             "single_level": bool(case.get("single_level", False)),
             "no_withdraw": bool(case.get("no_withdraw", False)),
-            "max_avg_cost_diff": case.get("max_avg_cost_diff", 0.2), "search_s": t_search}
+            "max_avg_cost_diff": case.get("max_avg_cost_diff", 0.2),
+            "reorder_k_by_nnz": case.get("reorder_k_by_nnz", True), "search_s": t_search}
     Ar = op.inps[0]
     out["A_indptr"] = Ar.indptr.astype(np.int32)
     out["A_indices"] = Ar.indices.astype(np.int32)

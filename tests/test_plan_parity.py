@@ -17,7 +17,8 @@ def _switches(meta):
     single = meta.get("single_level", False)
     return dict(tc_k_notsorted=meta.get("TC_k_notsorted", False), single_level=single,
                 max_level_num=1 if single else float("inf"),
-                max_avg_cost_diff=meta.get("max_avg_cost_diff", 0.2))
+                max_avg_cost_diff=meta.get("max_avg_cost_diff", 0.2),
+                reorder_k_by_nnz=meta.get("reorder_k_by_nnz", True))
 
 
 @pytest.mark.parametrize("path", golden_files("spmm"), ids=lambda p: p.split("/")[-1][:-4])
