@@ -286,11 +286,13 @@ def greedy_search_use_cost_model_lower_bound(op: Op, dsize=16, run_params=None, 
     if op.op_type == "spmm":
         plan = search_spmm(op.A, op.idx_lens[1], cost=cost, max_bucket_size=max_bucket_size, only_TC=only_TC,
                            only_ELL=only_ELL, max_avg_cost_diff=max_avg_cost_diff, penalty=penalty,
-                           max_level_num=max_level_num, tc_k_notsorted=TC_k_notsorted)
+                           max_level_num=max_level_num, tc_k_notsorted=TC_k_notsorted,
+                           reorder_k_by_nnz=reorder_k_by_nnz)
     else:
         plan = search_sddmm(op.A, op.idx_lens[1], cost=cost, max_bucket_size=max_bucket_size or 32,
                             only_TC=only_TC, only_ELL=only_ELL, max_avg_cost_diff=max_avg_cost_diff,
-                            max_level_num=max_level_num, tc_k_notsorted=TC_k_notsorted)
+                            max_level_num=max_level_num, tc_k_notsorted=TC_k_notsorted,
+                            reorder_k_by_nnz=reorder_k_by_nnz)
     return plan, None, None, None, plan.level_num
 
 
