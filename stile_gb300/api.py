@@ -12,6 +12,7 @@ nonzero of A, computed by walking the forward plan's own tiles.
 """
 from __future__ import annotations
 
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -281,18 +282,23 @@ def greedy_search_use_cost_model_lower_bound(op: Op, dsize=16, run_params=None, 
                                              log_file=None, cuda_i=0, dtype="float16", dtype_str=None,
                                              zerotype=None, cost_model: CostModel | None = None):
     """Returns (plan, None, None, None, level_num) in the reference's tuple
-    shape; the withdraw bookkeeping is already folded into ``plan``."""
+    shape; the withdraw bookkeeping is already folded into ``plan``.  The
+    reference's ablation switches arrive, as there, through the environment
+    variables ``single_level`` and ``no_withdraw`` ("True" / "False",
+    my_branch_and_bound.py:457-1313, my_search_formats.py:392-782)."""
     cost = cost_model or (A100_FP16 if dsize == 16 else gb300_model())
+    single_level = os.environ.get("single_level", "False") == "True"
     if op.op_type == "spmm":
         plan = search_spmm(op.A, op.idx_lens[1], cost=cost, max_bucket_size=max_bucket_size, only_TC=only_TC,
                            only_ELL=only_ELL, max_avg_cost_diff=max_avg_cost_diff, penalty=penalty,
                            max_level_num=max_level_num, tc_k_notsorted=TC_k_notsorted,
-                           reorder_k_by_nnz=reorder_k_by_nnz)
+                           reorder_k_by_nnz=reorder_k_by_nnz, single_level=single_level,
+                           no_withdraw=os.environ.get("no_withdraw", "False") == "True")
     else:
         plan = search_sddmm(op.A, op.idx_lens[1], cost=cost, max_bucket_size=max_bucket_size or 32,
                             only_TC=only_TC, only_ELL=only_ELL, max_avg_cost_diff=max_avg_cost_diff,
                             max_level_num=max_level_num, tc_k_notsorted=TC_k_notsorted,
-                            reorder_k_by_nnz=reorder_k_by_nnz)
+                            reorder_k_by_nnz=reorder_k_by_nnz, single_level=single_level)
     return plan, None, None, None, plan.level_num
 
 
