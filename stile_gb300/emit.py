@@ -166,9 +166,16 @@ def _emit_tc_sddmm(fmt):
     tiles = fmt.tiles
     ts_i, ts_k = int(fmt.tile_sizes[0][1]), int(fmt.tile_sizes[2][1])
     op = tiles[0].op
-    i_indices = np.asarray([op.i_perm[t.tile_i_rng[0]:t.tile_i_rng[1] + 1] for t in tiles])
-    j_indices = np.asarray([op.k_perm[op.blk_k_vals[int(t.tile_pos[0])][t.tile_k_rng[0]:t.tile_k_rng[1] + 1]]
-                            for t in tiles])
+    # a block cut short by the matrix edge (the reference pads its shapes to
+    # full blocks, so it never has one) repeats its last row / column, as
+    # the SpMM packer pads its column indices; only live entries are computed
+    i_indices = np.empty((len(tiles), ts_i), dtype=np.int64)
+    j_indices = np.empty((len(tiles), ts_k), dtype=np.int64)
+    for c, t in enumerate(tiles):
+        rows = op.i_perm[t.tile_i_rng[0]:t.tile_i_rng[1] + 1]
+        cols = op.k_perm[op.blk_k_vals[int(t.tile_pos[0])][t.tile_k_rng[0]:t.tile_k_rng[1] + 1]]
+        i_indices[c, :len(rows)], i_indices[c, len(rows):] = rows, rows[-1]
+        j_indices[c, :len(cols)], j_indices[c, len(cols):] = cols, cols[-1]
     cache = {}
     dense_pos, ids, counts = [], [], []
     for t in tiles:

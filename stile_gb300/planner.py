@@ -912,6 +912,18 @@ class SpmmPlanner:
                 best_avg * (1 - self.max_avg_cost_diff)
             if chosen[0].kind == TC:
                 good = self._local_tc_op(chosen[0], target, TC_row_tile_dict, TC_row_costs, len(selected), TC_is)
+                J = chosen[0].ts[1][1]
+                if not good and self.j_num < J:
+                    # the search ranks tensor-core tiles per J = 32 columns
+                    # of B (tile_sizes[1][1], my_branch_and_bound.py:531,
+                    # :683) and the local search per min(N, 32) columns
+                    # (selected_tile.j_num, :1322, :1374); for N < 32 the
+                    # chosen tile fails its own window and the reference's
+                    # loop never ends.  Widen the window by J / j_num, which
+                    # puts both on one scale (an empty result changed
+                    # nothing, so the retry starts from the same state).
+                    good = self._local_tc_op(chosen[0], target * J / self.j_num, TC_row_tile_dict,
+                                             TC_row_costs, len(selected), TC_is)
             else:
                 good = self._local_search_ell(chosen[0], target, TC_row_tile_dict, TC_row_costs,
                                               len(selected), reverse_idx)
