@@ -186,7 +186,8 @@ int stile_spmm_dvals_bf16(const StileSpmmPlan* plan, const float* dY,
                           int64_t lddy, const uint16_t* B, int64_t ldb,
                           float* dvals, int32_t N, void* stream);
 
-/* out[nnz] = <X[row(t)], Y[col(t)]> (fp32), CSR order of the mask. */
+/* out[nnz] = <X[row(t)], Y[col(t)]> (fp32), CSR order of the mask.  A plan
+ * of an empty mask returns 0 without reading any pointer. */
 int stile_sddmm_run(const StileSddmmPlan* plan, const float* X, int64_t ldx,
                     const float* Y, int64_t ldy, float* out, int32_t F,
                     void* stream);

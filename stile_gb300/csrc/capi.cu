@@ -816,6 +816,7 @@ static int sddmm_run(const StileSddmmPlan* plan, const void* X, int64_t ldx, con
                      float* out, int32_t F, void* stream) {
   if (!plan) return fail(STILE_E_INVALID, "null plan");
   if (F <= 0) return fail(STILE_E_INVALID, "F must be positive");
+  if (plan->nnz == 0) return STILE_OK;  // an empty mask: nothing to compute
   if (!out) return fail(STILE_E_INVALID, "null out");
   int rc;
   if ((rc = bf16 ? check_dense_bf16(ldx, F, X, "X") : check_dense(ldx, F, X, "X")) != 0) return rc;
