@@ -69,6 +69,19 @@ def _run_counts(code):
     return code[starts], np.diff(np.append(starts, len(code)))
 
 
+def _tile_csr(rows, cols, shape):
+    """The 0/1 CSR of a tile's covered entries (unique (row, column) pairs),
+    canonical as scipy's COO -> CSR conversion makes it (rows, then columns
+    ascending), built directly."""
+    R, C = shape
+    rows = np.asarray(rows, dtype=np.int64)
+    cols = np.asarray(cols, dtype=np.int64)
+    o = np.argsort(rows * C + cols)
+    indptr = np.zeros(R + 1, dtype=np.int32)
+    np.cumsum(np.bincount(rows, minlength=R), out=indptr[1:])
+    return sp.csr_matrix((np.ones(len(rows)), cols[o].astype(np.int32), indptr), shape=shape)
+
+
 def estimate_max_bucket_size(nnz, sm_num=108):
     """Bucket (fold) length of ELL rows from the expected occupancy
     (my_search_formats.py:965-981; 256-thread blocks, 2048 threads / SM)."""
@@ -173,7 +186,8 @@ class EllOp:
         if key not in self._kis_cache:
             n_t = math.ceil(self.n_folded / I)
             if not hasattr(self, "_cf_col"):
-                o = np.lexsort((self.frow, self.cols))
+                # by column, then folded row (pairs are unique)
+                o = np.argsort(self.cols * max(self.n_folded, 1) + self.frow)
                 self._cf_col = self.cols[o]
                 self._cf_frow = self.frow[o]
                 self._cf_colchg = self._cf_col[1:] != self._cf_col[:-1]
@@ -240,7 +254,10 @@ class TcOp:
             # np.unique's order: by block, then column
             o = np.arange(len(ucode))
         else:
-            o = np.lexsort((ucol, -cnt, ublk))
+            # by block, decreasing count, column: one integer key (unique,
+            # so any sort gives the order a stable lexsort would)
+            cmax = int(cnt.max()) if len(cnt) else 0
+            o = np.argsort((ublk * (cmax + 1) + (cmax - cnt)) * pat.K + ucol)
         ublk, ucol, cnt = ublk[o], ucol[o], cnt[o]
         self.nonempty = np.bincount(ublk, minlength=self.n_blk)
         self.kstart = np.concatenate([[0], np.cumsum(self.nonempty)])
@@ -252,7 +269,9 @@ class TcOp:
             rank[o] = np.arange(len(ucode)) - self.kstart[ublk]
             # entry -> position within its block's order
             pos = rank[uinv.reshape(-1)] if len(code) else np.zeros(0, np.int64)
-        eo = np.lexsort((pos, blk))
+        # by block, then position; ties (one column, several rows) keep the
+        # order of ``ids``
+        eo = np.argsort(blk * pat.K + pos, kind="stable")
         self.ids = ids[eo]
         self.blk = blk[eo]
         self.pos = pos[eo]
@@ -324,8 +343,9 @@ class TcOp:
         """First uncovered 16-column chunk of every block (0 if none)."""
         first = np.zeros(self.n_blk, dtype=np.int64)
         if len(blk):
-            u, idx = np.unique(blk, return_index=True)
-            first[u] = pos[idx] // 16
+            # blk is sorted: each block's first entry starts its run
+            starts = np.flatnonzero(np.concatenate([[True], blk[1:] != blk[:-1]]))
+            first[blk[starts]] = pos[starts] // 16
         return first
 
     def block_position_counts(self, b, uncovered):
@@ -478,6 +498,7 @@ class SpmmPlanner:
         self.j_num = min(32, self.N)
         self.uncovered = np.ones(self.pat.nnz, dtype=bool)
         self._upd_cache = {}
+        self._tc_unc = None
 
     # ---------------- candidate operators ----------------
     def _level1(self):
@@ -647,27 +668,49 @@ class SpmmPlanner:
         lr, lc, ids = self.tc.tile_entries(t.pos[0], t.k_rng[0], t.k_rng[1], uncovered)
         return len(ids)
 
+    def _tc_uncovered(self):
+        """Uncovered tensor-core entries: (block, position, each block's
+        first uncovered 16-column chunk, per (block, chunk relative to it)
+        the code b * span16 + chunk and its entry count, span16), kept until
+        the uncovered set changes."""
+        if self._tc_unc is None:
+            blk, pos = self.tc.uncovered_entries(self.uncovered)
+            first = self.tc.first_chunks(blk, pos)
+            if self.single_level:
+                first = first * 0
+            rel = pos // 16 - first[blk]
+            span16 = int(rel.max()) + 1 if len(rel) else 1
+            # entries come sorted by (block, position), so the codes are
+            # nondecreasing and their runs are np.unique's groups
+            c16, n16 = _run_counts(blk * span16 + rel)
+            self._tc_unc = (blk, pos, first, c16, n16, span16)
+        return self._tc_unc
+
+    def _tc_windows(self, w):
+        """(codes b * span + window, entry counts, span) of the uncovered
+        entries in windows of w 16-column chunks from each block's first
+        uncovered chunk, summed from the per-chunk counts."""
+        blk, pos, first, c16, n16, span16 = self._tc_uncovered()
+        b16, r16 = c16 // span16, c16 % span16
+        win = r16 // w
+        span = int(win.max()) + 1
+        code2 = b16 * span + win
+        starts = np.flatnonzero(np.concatenate([[True], code2[1:] != code2[:-1]]))
+        return code2[starts], np.add.reduceat(n16, starts), span
+
     def _search_tc_op(self, TC_row_costs):
         """search_best_TC_tile_given_op (:558-696): best atomic tile over
         windows aligned to every block's first uncovered chunk, and the best
         whole-row (owned, withdraw) alternative."""
         tc = self.tc
-        blk, pos = tc.uncovered_entries(self.uncovered)
-        first = tc.first_chunks(blk, pos)
-        if self.single_level:
-            first = first * 0
+        blk, pos, first = self._tc_uncovered()[:3]
         tot = np.bincount(blk, minlength=tc.n_blk)
-        rel = pos // 16 - first[blk]
         best_key, best_cost = None, float("inf")
         for ts in self.tc_sizes:
             Kt = ts[2][1]
             w = Kt // 16
             if len(blk):
-                win = rel // w
-                span = int(win.max()) + 1
-                # entries come sorted by (block, position), so the codes are
-                # nondecreasing and their runs are np.unique's groups
-                code, cnt = _run_counts(blk * span + win)
+                code, cnt, span = self._tc_windows(w)
                 mp = int(np.argmax(cnt))
                 r, c = int(code[mp] // span), int(code[mp] % span)
                 cost = self.cost.tc_cost(Kt, True, self.penalty)
@@ -776,10 +819,7 @@ class SpmmPlanner:
         tc = self.tc
         ts = sel.ts
         Kt = ts[2][1]
-        blk, pos = tc.uncovered_entries(self.uncovered)
-        first = tc.first_chunks(blk, pos)
-        if self.single_level:
-            first = first * 0
+        blk, pos, first = self._tc_uncovered()[:3]
         tot = np.bincount(blk, minlength=tc.n_blk)
         tsl = self.tc_sizes
         nonempty = np.asarray([tc.blk_nums[t] for t in tsl])
@@ -805,9 +845,7 @@ class SpmmPlanner:
         atomic_cost = self.cost.tc_cost(Kt, True, self.penalty)
         poses = []
         if len(blk):
-            win = (pos - first[blk] * 16) // Kt
-            span = int(win.max()) + 1
-            code, cnt = np.unique(blk * span + win, return_counts=True)
+            code, cnt, span = self._tc_windows(Kt // 16)
             ok = atomic_cost / cnt / sel.j_num <= target
             sel_set = set(int(x) for x in sel_rows)
             for cd in code[ok]:
@@ -852,6 +890,7 @@ class SpmmPlanner:
         for t in tiles:
             self.uncovered[t.cov_ids] = False
         self._upd_cache = {}
+        self._tc_unc = None
 
     # ---------------- main ----------------
     def search(self):
@@ -981,6 +1020,7 @@ class SpmmPlanner:
             if row_sel:
                 TC_is[b * 16:(b + 1) * 16] = True
         self._upd_cache = {}
+        self._tc_unc = None
         return selected
 
     # ---------------- withdraw post-processing ----------------
@@ -1000,11 +1040,12 @@ class SpmmPlanner:
                 spaces[op.op_id] = op.space()
             return spaces[op.op_id]
 
+        everything = np.ones(self.pat.nnz, dtype=bool)
         for t in remains:
             if t.kind == TC:
                 if not t.atomic:
-                    self._finalise(t, np.ones(self.pat.nnz, dtype=bool))
-                cov = sp.csr_matrix((np.ones(len(t.cov_ids)), (t.cov_rows, t.cov_cols)), shape=t.cov_shape)
+                    self._finalise(t, everything)
+                cov = _tile_csr(t.cov_rows, t.cov_cols, t.cov_shape)
                 nt = Tile(op=space_of(t.op), tile_sizes=t.ts, tile_pos=t.pos, params=dict(TC_PARAMS),
                           best_tile_sizes=t.best_ts, best_params=dict(TC_PARAMS), is_atomic=bool(t.atomic),
                           tile_i_rng=t.i_rng, tile_k_rng=None,
@@ -1035,8 +1076,7 @@ class SpmmPlanner:
                             atomic = False
                 if not atomic:
                     i_vals[cov_nnz_rows == 0] = M
-                cov = sp.csr_matrix((np.ones(len(t.cov_ids)), (t.cov_rows, t.cov_cols)),
-                                    shape=(r1 - r0 + 1, self.pat.K))
+                cov = _tile_csr(t.cov_rows, t.cov_cols, (r1 - r0 + 1, self.pat.K))
                 nt = Tile(op=space_of(op), tile_sizes=t.ts, tile_pos=t.pos, params=t.params,
                           best_tile_sizes=t.best_ts, best_params=t.params, is_atomic=atomic,
                           tile_i_rng=None, tile_k_rng=None, i_vals=i_vals, covered=cov,
@@ -1332,7 +1372,7 @@ class SddmmPlanner:
                         (np.arange(1, pat.nnz + 1), (inv[pat.row_of], pat.indices)), shape=(pat.M, pat.K))
                 spaces[t.op.op_id] = sp_
             if t.kind == TC_SDDMM:
-                cov = sp.csr_matrix((np.ones(len(t.cov_ids)), (t.cov_rows, t.cov_cols)), shape=t.cov_shape)
+                cov = _tile_csr(t.cov_rows, t.cov_cols, t.cov_shape)
                 tiles_tc.append(Tile(op=spaces[t.op.op_id], tile_sizes=t.ts, tile_pos=t.pos, params=dict(TC_PARAMS),
                                      best_tile_sizes=t.best_ts, best_params=dict(TC_PARAMS), is_atomic=False,
                                      tile_i_rng=t.i_rng, tile_k_rng=t.k_rng, covered=cov,
