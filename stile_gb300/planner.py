@@ -142,8 +142,7 @@ class EllOp:
         fold_first = self.hyb_ori_row_ends - self.new_row_nums + 1
         self.frow = fold_first[pos_row] + within // mbs
         self.indptr = np.zeros(self.n_folded + 1, dtype=np.int64)
-        np.add.at(self.indptr, self.frow + 1, 1)
-        self.indptr = np.cumsum(self.indptr)
+        np.cumsum(np.bincount(self.frow, minlength=self.n_folded), out=self.indptr[1:])
         self.init_nnz = np.diff(self.indptr)
         self.getnnz_minus = -self.init_nnz[self.short_begin:]
         self._kis_cache = {}
