@@ -308,9 +308,12 @@ def post_process_for_withdraw(op, selected, TC_row_tile_dict=None, TC_row_costs=
 
 def measure_seleted_formats(ori_op: Op, op_type, batch_num, selected, cuda_i=0, cache_set=("A",), dsize=16,
                             gened_inputs=None, dtype="float16", dtype_str=None, zerotype=None):
-    """Pack and upload the plan; returns the tuple measure_latency consumes."""
+    """Pack and upload the plan; returns the tuple measure_latency consumes.
+    op_type "batched_spmm" runs batch_num heads of the plan in one launch
+    per kernel (the reference replicates A's values and B per head,
+    my_fuse_formats.py:3502-3527)."""
     tc_mode = D.TC_F16 if dtype == "float16" else D.TC_BF16
-    if op_type == "spmm":
+    if op_type in ("spmm", "batched_spmm"):
         opx = SpmmOperator(ori_op.A, ori_op.idx_lens[1], PlanConfig(tc_mode=tc_mode), plan=selected)
     else:
         opx = SddmmOperator(ori_op.A, ori_op.idx_lens[1], plan=selected)
@@ -323,10 +326,22 @@ def measure_latency(ori_op, op_type, batch_num, f, args_nd, out_shape, dtype, de
     against scipy at the reference's tolerance (rtol = atol = 1e-2)."""
     dense = [torch.as_tensor(np.asarray(x.data if hasattr(x, "data") else x, dtype=np.float32), device="cuda")
              for x in ori_op.inps[1:]]
-    run = (lambda: f(dense[0])) if op_type == "spmm" else (lambda: f(dense[0], dense[1]))
+    if op_type == "batched_spmm":
+        H = int(batch_num)
+        vals = torch.as_tensor(np.tile(ori_op.A.data.astype(np.float32), (H, 1)), device="cuda")
+        packed = f.handle.pack_values(vals)
+        Bh = dense[0].unsqueeze(0).expand(H, -1, -1).contiguous()
+        run = lambda: f.handle.run_batched(packed, Bh)  # noqa: E731
+    elif op_type == "spmm":
+        run = lambda: f(dense[0])  # noqa: E731
+    else:
+        run = lambda: f(dense[0], dense[1])  # noqa: E731
     out = run()
     torch.cuda.synchronize()
-    if op_type == "spmm":
+    if op_type == "batched_spmm":
+        one = ori_op.A @ np.asarray(dense[0].cpu(), dtype=np.float64)
+        ref = np.broadcast_to(one, (H,) + one.shape)
+    elif op_type == "spmm":
         ref = ori_op.A @ np.asarray(dense[0].cpu(), dtype=np.float64)
     else:
         A = ori_op.A

@@ -102,7 +102,11 @@ def test_plan_sddmm_api():
     assert S.rel_fro(out, S.sddmm_fp64(M, X, Y)) <= 1e-5
 
 
-def test_reference_named_facade():
+@pytest.mark.parametrize("op_type,batch_num", [("spmm", 1), ("batched_spmm", 3)])
+def test_reference_named_facade(op_type, batch_num):
+    """The reference's driver sequence; measure_latency checks the result
+    (every head of a batched run) against scipy at rtol = atol = 1e-2
+    before it times."""
     from stile_gb300.api import (Op, greedy_search_use_cost_model_lower_bound, measure_latency,
                                  measure_seleted_formats, post_process_for_withdraw)
     from stile_gb300.synthetic import power_law_rows
@@ -112,7 +116,7 @@ def test_reference_named_facade():
     res = greedy_search_use_cost_model_lower_bound(op, 16, None, 8, ["A"], ([1], [1], [1]), False, False, 1,
                                                    False, max_avg_cost_diff=0.2)
     tiles = post_process_for_withdraw(op, *res[:4])
-    ms = measure_latency(*measure_seleted_formats(op, "spmm", 1, tiles, 0, ["A"], 16))
+    ms = measure_latency(*measure_seleted_formats(op, op_type, batch_num, tiles, 0, ["A"], 16))
     assert ms > 0
 
 
