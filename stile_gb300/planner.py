@@ -748,28 +748,33 @@ class SpmmPlanner:
         cs = np.concatenate([[0], np.cumsum(base)])
         best_key, best_cost = None, float("inf")
         unit = {}
-        for ts in self.tc_sizes:
+        sel_pred = _sum_pred(selected_row)
+        if not self.single_level:
+            # entries in the window of w chunks from every chunk, for all
+            # tile widths at once (windows end at the block's last chunk)
+            ws = np.asarray([ts[2][1] // 16 for ts in self.tc_sizes])
+            per_all = cs[np.minimum(np.arange(L)[None, :] + ws[:, None], L)] - cs[None, :L]
+            mps = np.argmax(per_all, axis=1)
+        for n, ts in enumerate(self.tc_sizes):
             Kt = ts[2][1]
             w = Kt // 16
-            tmp = np.concatenate([cs, np.full(w - 1, cs[-1])])
-            per = tmp[np.arange(w, w + len(cs) - 1)] - tmp[:len(cs) - 1]
             if self.single_level:
                 per = np.add.reduceat(base, np.arange(0, nchunk, w))
-            mp = int(np.argmax(per))
+                mp = int(np.argmax(per))
+            else:
+                per = per_all[n]
+                mp = int(mps[n])
             cost = self.cost.tc_cost(Kt, True, self.penalty)
             unit[ts] = [None, cost]
             with np.errstate(divide="ignore", invalid="ignore"):
                 pavg = cost / per[mp] / ts[1][1]
-            kpos = mp * Fraction(16, Kt)
-            if self.single_level:
-                kpos = mp
             if pavg < best_cost and pavg < best_possible_ell:
                 best_cost = pavg
-                best_key = (ts, [kpos], True)
+                best_key = (ts, [mp if self.single_level else mp * Fraction(16, Kt)], True)
             nonempty = int(tc.blk_nums[ts][b])
             no_atomic = self.cost.tc_cost(Kt, False, self.penalty)
             unit[ts][0] = no_atomic
-            extra = no_atomic * nonempty - _sum_pred(selected_row)
+            extra = no_atomic * nonempty - sel_pred
             if self.no_withdraw:
                 extra = no_atomic * nonempty
             pavgs = extra / tot / ts[1][1]
