@@ -190,16 +190,35 @@ class EllOp:
                 self._cf_col = self.cols[o]
                 self._cf_frow = self.frow[o]
                 self._cf_colchg = self._cf_col[1:] != self._cf_col[:-1]
+                # highest bit in which each entry's folded row differs from
+                # the previous entry's of the same column (63: first entry of
+                # its column): for I = 2^t the entry opens a new (segment,
+                # column) pair exactly when that bit is >= t
+                fr = self._cf_frow
+                lvl = np.full(len(fr), 63, dtype=np.int8)
+                if len(fr) > 1:
+                    x = fr[1:] ^ fr[:-1]
+                    hb = (np.frexp(np.maximum(x, 1).astype(np.float64))[1] - 1).astype(np.int8)
+                    lvl[1:] = np.where(self._cf_colchg, 63, hb)
+                self._cf_lvl = lvl
+                self._cf_zero_frow = fr[self._cf_col == 0]
             col = self._cf_col
-            seg = self._cf_frow // I
-            # entries sorted by (column, folded row): a (segment, column) pair
-            # is new wherever the column or the segment changes
-            first = np.ones(len(col), dtype=bool)
-            if len(col) > 1:
-                first[1:] = self._cf_colchg | (seg[1:] != seg[:-1])
-            distinct = np.bincount(seg[first], minlength=n_t)
-            has0 = np.zeros(n_t, dtype=bool)
-            has0[seg[col == 0]] = True
+            if I & (I - 1) == 0:
+                t = I.bit_length() - 1
+                first = self._cf_lvl >= t
+                distinct = np.bincount(self._cf_frow[first] >> t, minlength=n_t)
+                has0 = np.zeros(n_t, dtype=bool)
+                has0[self._cf_zero_frow >> t] = True
+            else:
+                seg = self._cf_frow // I
+                # entries sorted by (column, folded row): a (segment, column)
+                # pair is new wherever the column or the segment changes
+                first = np.ones(len(col), dtype=bool)
+                if len(col) > 1:
+                    first[1:] = self._cf_colchg | (seg[1:] != seg[:-1])
+                distinct = np.bincount(seg[first], minlength=n_t)
+                has0 = np.zeros(n_t, dtype=bool)
+                has0[seg[col == 0]] = True
             self._kis_cache[key] = (distinct, has0)
         distinct, has0 = self._kis_cache[key]
         pos_is = np.asarray(pos_is, dtype=np.int64)
