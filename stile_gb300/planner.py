@@ -115,7 +115,9 @@ class EllOp:
         self.pat = pat
         self.op_id = op_id
         self.mbs = mbs
-        ids = np.sort(np.asarray(ids, dtype=np.int64))   # CSR order of the subset
+        ids = np.asarray(ids, dtype=np.int64)   # CSR order of the subset
+        if len(ids) > 1 and not np.all(ids[1:] > ids[:-1]):
+            ids = np.sort(ids)
         rn = pat.sub_row_nnz(ids)
         self.row_nnz_pos = None
         self.i_perm = np.argsort(-rn, kind="stable")
@@ -135,14 +137,15 @@ class EllOp:
         order = np.repeat(sub_start[self.i_perm] - out_start, rn_sorted) + np.arange(len(ids), dtype=np.int64)
         self.ids = ids[order]
         self.cols = pat.indices[self.ids]
-        pos_row = np.repeat(np.arange(pat.M, dtype=np.int64), rn_sorted)
-        # folded row of every entry
-        row_start = np.concatenate([[0], np.cumsum(rn_sorted)[:-1]])
-        within = np.arange(len(self.ids)) - row_start[pos_row]
+        # entries per folded row: mbs for every fold of a row but its last,
+        # which holds the rest (0 for an empty row's single fold)
         fold_first = self.hyb_ori_row_ends - self.new_row_nums + 1
-        self.frow = fold_first[pos_row] + within // mbs
+        j = np.arange(self.n_folded, dtype=np.int64) - fold_first[self.hyb_new_rows]
+        fold_len = np.clip(rn_sorted[self.hyb_new_rows] - j * mbs, 0, mbs)
         self.indptr = np.zeros(self.n_folded + 1, dtype=np.int64)
-        np.cumsum(np.bincount(self.frow, minlength=self.n_folded), out=self.indptr[1:])
+        np.cumsum(fold_len, out=self.indptr[1:])
+        # folded row of every entry
+        self.frow = np.repeat(np.arange(self.n_folded, dtype=np.int64), fold_len)
         self.init_nnz = np.diff(self.indptr)
         self.getnnz_minus = -self.init_nnz[self.short_begin:]
         self._kis_cache = {}
