@@ -298,7 +298,6 @@ class TcOp:
         self.pos = pos[eo]
         self.prow = prow[eo]
         self.bptr = np.concatenate([[0], np.cumsum(np.bincount(self.blk, minlength=self.n_blk))])
-        self.maxne = int(self.nonempty.max()) if self.n_blk else 0
         # positions a block's counts run over: its non-empty prefix, or (in
         # column order) up to its last non-empty column
         if self.k_notsorted:
