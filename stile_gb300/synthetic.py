@@ -212,19 +212,6 @@ def dense_operand(rows, cols, seed=1, dist="normal", dtype=np.float32):
     return x.astype(dtype)
 
 
-def pad_shape(A, multiple=128):
-    """Pad the matrix shape with empty rows/columns to a multiple of
-    ``multiple`` (the reference pads graph operators this way:
-    gen_formats_v2.py:2730-2735)."""
-    m = int(math.ceil(A.shape[0] / multiple) * multiple)
-    k = int(math.ceil(A.shape[1] / multiple) * multiple)
-    if (m, k) == A.shape:
-        return A
-    A = A.tocsr()
-    indptr = np.concatenate([A.indptr, np.full(m - A.shape[0], A.indptr[-1])])
-    return sp.csr_matrix((A.data, A.indices, indptr), shape=(m, k))
-
-
 def logsparse_pattern(n):
     """LogSparse attention mask (Li et al., 2019), n x n: row i attends to
     itself, to i - 2^j for 2^j <= i and to i + 2^j for j <
