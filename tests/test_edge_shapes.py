@@ -53,3 +53,22 @@ def test_sddmm_plan_edge_shapes(name, F, knots):
     fmts = [{"template": f.template, "tile_sizes": f.tile_sizes, "params": f.params} for f in fm]
     out = S.sddmm_from_arrays(fmts, args, X, Y, A.nnz)
     assert np.allclose(out, S.sddmm_fp64(A, X, Y), rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.parametrize("kind", ["spmm", "sddmm"])
+@pytest.mark.parametrize("name", sorted(SHAPES))
+def test_plan_file_round_trip_edge_shapes(name, kind, tmp_path):
+    """Plans of the edge-case shapes save and load to the same packed arrays."""
+    from stile_gb300 import plan_io
+    A = SHAPES[name]()
+    plan = search_spmm(A, 8, tc_k_notsorted=True) if kind == "spmm" else search_sddmm(A, 8)
+    path = str(tmp_path / "plan.npz")
+    plan_io.save_plan(plan, path, A=A)
+    back = plan_io.load_plan(path, A=A)
+    if kind == "spmm":
+        a, b = (emit.emit_spmm_reference(p.tiles, A.shape[0], 8)[1] for p in (plan, back))
+    else:
+        a, b = (emit.emit_sddmm_reference(p.tiles)[1] for p in (plan, back))
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        assert all(np.array_equal(np.asarray(u), np.asarray(v)) for u, v in zip(x, y))
