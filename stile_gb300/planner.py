@@ -188,8 +188,11 @@ class EllOp:
         if key not in self._kis_cache:
             n_t = math.ceil(self.n_folded / I)
             if not hasattr(self, "_cf_col"):
-                # by column, then folded row (pairs are unique)
-                o = np.argsort(self.cols * max(self.n_folded, 1) + self.frow)
+                # by column, then folded row: the entries are in folded-row
+                # order, so a CSR -> CSC transposition of their indices is
+                # that order (a counting sort, linear in the entries)
+                o = sp.csr_matrix((np.arange(len(self.cols), dtype=np.int64), self.cols, self.indptr),
+                                  shape=(self.n_folded, self.pat.K)).tocsc().data
                 self._cf_col = self.cols[o]
                 self._cf_frow = self.frow[o]
                 self._cf_colchg = self._cf_col[1:] != self._cf_col[:-1]
