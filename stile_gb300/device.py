@@ -218,42 +218,44 @@ def build_spmm_device(tiles, A, N=32, tc_mode=TC_BF16, emitted=None):
     for f, arr in zip(formats, args):
         if f.template != ELL:
             continue
-        a, kidx, iout = arr
+        _, kidx, iout = arr
         I = int(np.prod([int(x) for x in f.tile_sizes[0][1:]]))
         Kl = kidx.shape[1]
         atomic = bool(f.params["real_atomic"])
-        a = a.reshape(-1, Kl)
+        nt = len(f.tiles)
+        # every tile of the format at once: rows c * I .. (c + 1) * I - 1
+        # belong to tile c, whose first n_real rows are real
+        lens = np.zeros(nt * I, dtype=np.int64)
+        n_real = np.empty(nt, dtype=np.int64)
         for c, t in enumerate(f.tiles):
-            rs = slice(c * I, (c + 1) * I)
             cov = t.covered
-            n_real = cov.shape[0]
-            lens = np.zeros(I, dtype=np.int64)
-            lens[:n_real] = np.diff(sp.csr_matrix(cov).indptr)
-            orow = iout[rs].astype(np.int64).copy()
-            orow[n_real:] = -1
-            orow[orow >= M] = -1
-            if not atomic:
-                orow[lens == 0] = -1
-            ki = kidx[rs].astype(np.int64)
-            live = np.arange(Kl)[None, :] < lens[:, None]
-            live &= (orow >= 0)[:, None]
-            R = np.repeat(np.maximum(orow, 0)[:, None], Kl, axis=1)
-            ids, v = vidx.lookup(np.where(live, R, 0), np.where(live, ki, 0))
-            ids = np.where(live, ids, -1)
-            v = np.where(live, v, 0.0)
-            if np.any(live & (ids < 0)):
-                raise ValueError("plan covers an entry that is not a nonzero of A")
-            eK.append(Kl)
-            eslot.append(n_slots)
-            eflags.append(1 if atomic else 0)
-            eout.append(orow)
-            elen.append(np.where(orow >= 0, lens, 0))
-            evals.append(v.reshape(-1))
-            ekidx.append(ki.reshape(-1))
-            enid.append(ids.reshape(-1))
-            n_rows += I
-            n_slots += I * Kl
-            row0.append(n_rows)
+            n_real[c] = cov.shape[0]
+            lens[c * I:c * I + n_real[c]] = np.diff(sp.csr_matrix(cov).indptr)
+        orow = iout[:nt * I].astype(np.int64).copy()
+        orow[np.arange(nt * I) % I >= np.repeat(n_real, I)] = -1
+        orow[orow >= M] = -1
+        if not atomic:
+            orow[lens == 0] = -1
+        ki = kidx[:nt * I].astype(np.int64)
+        live = np.arange(Kl)[None, :] < lens[:, None]
+        live &= (orow >= 0)[:, None]
+        R = np.repeat(np.maximum(orow, 0)[:, None], Kl, axis=1)
+        ids, v = vidx.lookup(np.where(live, R, 0), np.where(live, ki, 0))
+        ids = np.where(live, ids, -1)
+        v = np.where(live, v, 0.0)
+        if np.any(live & (ids < 0)):
+            raise ValueError("plan covers an entry that is not a nonzero of A")
+        eK.extend([Kl] * nt)
+        eslot.extend((n_slots + I * Kl * np.arange(nt)).tolist())
+        eflags.extend([1 if atomic else 0] * nt)
+        eout.append(orow)
+        elen.append(np.where(orow >= 0, lens, 0))
+        evals.append(v.reshape(-1))
+        ekidx.append(ki.reshape(-1))
+        enid.append(ids.reshape(-1))
+        row0.extend((n_rows + I * (np.arange(nt) + 1)).tolist())
+        n_rows += I * nt
+        n_slots += I * Kl * nt
 
     def cat(xs, dt):
         return np.concatenate(xs).astype(dt) if xs else np.zeros(0, dt)
