@@ -47,3 +47,23 @@ def test_reference_arm_runs_on_rank_zero_only():
                         "--warmup", "0"], env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+def test_reference_arm_prints_the_contract_line():
+    """Rank 0 of the reference arm times the reference's CPU path (the C
+    restatement) on the bench workload and prints one JSON line with the
+    keys the contract names."""
+    import json
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0"], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    out = json.loads(lines[0])
+    assert out["impl"] == "reference" and out["value"] > 0 and out["higher_is_better"] is True
+    for key in ("metric", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "scaling", "dtype", "data", "config"):
+        assert key in out
+    assert out["cpu_baseline"]["value"] == out["value"] and out["cpu_baseline"]["cores"] >= 1
+    assert out["e2e"] == {"value": out["value"], "unit": out["unit"], "h2d_bytes_per_step": 0,
+                          "d2h_bytes_per_step": 0}
