@@ -269,36 +269,38 @@ class TcOp:
         prow = inv[pat.row_of[ids]]
         blk = prow // bs
         col = pat.indices[ids]
-        # per (block, column) counts -> order within block by (-count, col)
+        # entries grouped by (block, column), each group in the order of
+        # ``ids`` (a stable sort: rows are sorted runs, so it merges runs)
         code = blk * pat.K + col
-        ucode, uinv, cnt = np.unique(code, return_inverse=True, return_counts=True)
+        order = np.argsort(code, kind="stable")
+        sc = code[order]
+        starts = np.flatnonzero(np.concatenate([[True], sc[1:] != sc[:-1]])) if len(sc) else np.zeros(0, np.int64)
+        ucode = sc[starts]
+        cnt = np.diff(np.append(starts, len(sc)))
         ublk = ucode // pat.K
         ucol = ucode % pat.K
         if self.k_notsorted or not k_by_count:
-            # np.unique's order: by block, then column
+            # by block, then column
             o = np.arange(len(ucode))
         else:
             # by block, decreasing count, column: one integer key (unique,
             # so any sort gives the order a stable lexsort would)
             cmax = int(cnt.max()) if len(cnt) else 0
             o = np.argsort((ublk * (cmax + 1) + (cmax - cnt)) * pat.K + ucol)
-        ublk, ucol, cnt = ublk[o], ucol[o], cnt[o]
+        ublk, ucol, cnt, starts = ublk[o], ucol[o], cnt[o], starts[o]
         self.nonempty = np.bincount(ublk, minlength=self.n_blk)
         self.kstart = np.concatenate([[0], np.cumsum(self.nonempty)])
         self.kord_cols = ucol                       # concatenated per block
-        if self.k_notsorted:
-            pos = col
-        else:
-            rank = np.empty(len(ucode), dtype=np.int64)
-            rank[o] = np.arange(len(ucode)) - self.kstart[ublk]
-            # entry -> position within its block's order
-            pos = rank[uinv.reshape(-1)] if len(code) else np.zeros(0, np.int64)
-        # by block, then position; ties (one column, several rows) keep the
-        # order of ``ids``
-        eo = np.argsort(blk * pat.K + pos, kind="stable")
+        # entries by block, then position in the block's order (the groups
+        # in that order); ties (one column, several rows) keep ``ids``' order
+        first = np.repeat(np.cumsum(cnt) - cnt, cnt)
+        eo = order[np.repeat(starts, cnt) + np.arange(len(order)) - first]
         self.ids = ids[eo]
         self.blk = blk[eo]
-        self.pos = pos[eo]
+        if self.k_notsorted:
+            self.pos = col[eo]
+        else:
+            self.pos = np.repeat(np.arange(len(ucode)) - self.kstart[ublk], cnt)
         self.prow = prow[eo]
         self.bptr = np.concatenate([[0], np.cumsum(np.bincount(self.blk, minlength=self.n_blk))])
         # positions a block's counts run over: its non-empty prefix, or (in
