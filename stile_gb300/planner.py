@@ -1317,7 +1317,8 @@ class SddmmPlanner:
             first = first * 0
         win = pos // 16 - first[blk]
         span = int(win.max()) + 1
-        code, cnt = np.unique(blk * span + win, return_counts=True)
+        # entries come sorted by (block, position): the codes are nondecreasing
+        code, cnt = _run_counts(blk * span + win)
         mp = int(np.argmax(cnt))
         r, c = int(code[mp] // span), int(code[mp] % span)
         pavg = self._tc_cost() * self._scale() / cnt[mp] / self.F
@@ -1333,7 +1334,8 @@ class SddmmPlanner:
             first = first * 0
         win = (pos - first[blk] * 16) // 16
         span = int(win.max()) + 1
-        code, cnt = np.unique(blk * span + win, return_counts=True)
+        # entries come sorted by (block, position): the codes are nondecreasing
+        code, cnt = _run_counts(blk * span + win)
         ok = cost * scale / cnt / self.F <= target
         good = []
         for cd in code[ok]:
