@@ -1,12 +1,17 @@
-"""Benchmark: hybrid-tile SpMM forward + backward on the graph workload.
+"""Benchmark: hybrid-tile SpMM / SDDMM forward + backward of the two-layer
+GCN workload.
 
-Workload (one step): a 169,343 x 169,343 symmetric power-law graph
-(degree exponent 2.0, ~1.17M nonzeros, ~30% of them in planted 16x16 blocks
-of density >= 0.5, values 1/deg), B = 169,343 x 128 fp32:
-    forward   C     = A @ B                (fused hybrid kernel)
-    backward  dvals = <dC[row], B[col]>    (SDDMM over the forward tiles)
-              dB    = A^T @ dC             (transposed plan)
-FLOPs per step = 3 * 2 * nnz * N.  The dense operands are synthetic N(0,1).
+Workload (one step): a 232,965-node symmetric power-law graph (degree
+exponent 1.9, ~11.4M nonzeros, planted 16x16 communities, values 1/deg) and
+the sparse products of a two-layer graph convolution, 602 -> 128 -> 41, with
+the dense operands synthetic N(0,1):
+    layer 1  C1 = A @ B1 (N = 128)          layer 2  C2 = A @ B2 (N = 41)
+    backward dvals_l = <dC_l[row], B_l[col]> over the forward tiles
+             dB_l = A^T @ dC_l (transposed plan)      for l = 2, 1
+FLOPs per step = 3 * 2 * nnz * (128 + 41).  The dense GEMMs of the GCN
+(X W1, Z1 W2) are cuBLAS work outside the metric; the line times the whole
+training step of the model for context (``gcn_training_step``).  The
+169,343-node graph (one layer, N = 128) is reported in ``secondary``.
 
 Output: one JSON line (metric / value / e2e / roofline / cpu_baseline / ...).
 `--impl reference` times the CPU restatement of the same step on the host
@@ -28,8 +33,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "SpMM/SDDMM GFLOP/s and %HBM roofline: hybrid-TC vs plain CSR, fwd+bwd, GB300"
-WORKLOAD = "hybrid_graph_169343_nnz1.17M_N128_fwd_bwd"
-N_FEAT = 128
+WORKLOAD = "gcn2_232965_nnz11.4M_602-128-41_fwd_bwd"
+WIDTHS = (128, 41)
+GRAPH_WORKLOAD = "hybrid_graph_169343_nnz1.17M_N128_fwd_bwd"
 
 
 def log(*a):
@@ -46,10 +52,28 @@ def errors(name, x, ref):
             f"{name}_max_abs": float(np.abs(x - ref).max()) if x.size else 0.0}
 
 
-def make_workload(seed=0):
+def make_gcn_workload(seed=0):
+    """(A, [(B_l, dC_l) for the two layer widths]): the GCN graph and
+    synthetic N(0, 1) layer operands (float32, C-contiguous)."""
+    from stile_gb300 import synthetic as syn
+    from stile_gb300 import workloads as W
+    w = W.gcn(WIDTHS[0], seed=seed)
+    A = w.A
+    layers = [(w.dense["B"], w.dense["dC"])]
+    for j, N in enumerate(WIDTHS[1:]):
+        layers.append((syn.dense_operand(A.shape[1], N, seed=3 + 2 * j),
+                       syn.dense_operand(A.shape[0], N, seed=4 + 2 * j)))
+    return A, layers
+
+
+def make_graph_workload(seed=0):
     from stile_gb300 import workloads as W
     w = W.graph(seed)
-    return w.A, w.dense["B"], w.dense["dC"]
+    return w.A, [(w.dense["B"], w.dense["dC"])]
+
+
+def step_flops(A, layers):
+    return sum(3 * 2 * A.nnz * B.shape[1] for B, _ in layers)
 
 
 def algorithmic_bytes_spmm(A, N, s_a=4, s_b=4, s_c=4):
@@ -214,31 +238,37 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU (oracle) step
 # ---------------------------------------------------------------------------
-def cpu_step_fn(A, AT, B, dC, threads):
+def cpu_step_fn(A, AT, layers, threads):
+    """The step's sparse products on the host: per layer CSR SpMM for A and
+    A^T and the gather-dot SDDMM (the C restatement of the reference's CPU
+    path)."""
     from oracle import cpu as ocpu
     rows = np.repeat(np.arange(A.shape[0], dtype=np.int32), np.diff(A.indptr))
     ip, ix, vv = A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data.astype(np.float32)
     ipt, ixt, vvt = AT.indptr.astype(np.int32), AT.indices.astype(np.int32), AT.data.astype(np.float32)
-    C = np.empty((A.shape[0], B.shape[1]), np.float32)
-    dB = np.empty((A.shape[1], B.shape[1]), np.float32)
-    dv = np.empty(A.nnz, np.float32)
     cols = A.indices.astype(np.int32)
+    bufs = [(np.ascontiguousarray(B, np.float32), np.ascontiguousarray(dC, np.float32),
+             np.empty((A.shape[0], B.shape[1]), np.float32), np.empty((A.shape[1], B.shape[1]), np.float32),
+             np.empty(A.nnz, np.float32)) for B, dC in layers]
 
     def step():
-        ocpu.csr_spmm(ip, ix, vv, B, threads=threads, out=C)
-        ocpu.sddmm(rows, cols, dC, B, threads=threads, out=dv)
-        ocpu.csr_spmm(ipt, ixt, vvt, dC, threads=threads, out=dB)
-        return C, dv, dB
+        out = []
+        for B, dC, C, dB, dv in bufs:
+            ocpu.csr_spmm(ip, ix, vv, B, threads=threads, out=C)
+            ocpu.sddmm(rows, cols, dC, B, threads=threads, out=dv)
+            ocpu.csr_spmm(ipt, ixt, vvt, dC, threads=threads, out=dB)
+            out.append((C, dv, dB))
+        return out
     return step
 
 
-def run_cpu_baseline(A, B, dC, flops_per_step, budget_s=12.0):
+def run_cpu_baseline(A, layers, flops_per_step, budget_s=12.0):
     from oracle import cpu as ocpu
     ocpu.build()
     AT = A.T.tocsr()
     AT.sort_indices()
     threads = os.cpu_count() or 1
-    step = cpu_step_fn(A, AT, B, dC, threads)
+    step = cpu_step_fn(A, AT, layers, threads)
     step()
     n, t0 = 0, time.perf_counter()
     while True:
@@ -248,8 +278,13 @@ def run_cpu_baseline(A, B, dC, flops_per_step, budget_s=12.0):
             break
     dt = (time.perf_counter() - t0) / n
     return {"value": flops_per_step / dt / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port",
-            "sample": f"{n} full fwd+bwd steps (C restatement of CSR SpMM x2 + gather-dot SDDMM, fp32, "
-                      f"pthreads) on the whole workload"}
+            "sample": f"{n} full fwd+bwd steps of the workload (both layers; C restatement of CSR SpMM x2 + "
+                      f"gather-dot SDDMM per layer, fp32, pthreads)"}
+
+
+def base_config(A, layers, workload):
+    return {"workload": workload, "M": int(A.shape[0]), "K": int(A.shape[1]), "nnz": int(A.nnz),
+            "N": [int(B.shape[1]) for B, _ in layers]}
 
 
 def run_reference(args):
@@ -258,12 +293,12 @@ def run_reference(args):
         return
     from oracle import cpu as ocpu
     ocpu.build()
-    A, B, dC = make_workload()
+    A, layers = make_gcn_workload()
     AT = A.T.tocsr()
     AT.sort_indices()
     threads = os.cpu_count() or 1
-    step = cpu_step_fn(A, AT, B, dC, threads)
-    flops = 3 * 2 * A.nnz * N_FEAT
+    step = cpu_step_fn(A, AT, layers, threads)
+    flops = step_flops(A, layers)
     for _ in range(args.warmup):
         step()
     t0 = time.perf_counter()
@@ -274,10 +309,10 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GFLOP/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "nnz": int(A.nnz), "N": N_FEAT},
+           "config": base_config(A, layers, WORKLOAD),
            "cpu_baseline": {"value": val, "unit": "GFLOP/s", "cores": threads, "kind": "port",
-                            "sample": "the whole fwd+bwd step per iteration (C restatement of the "
-                                      "reference's CPU path: CSR SpMM x2 + gather-dot SDDMM)"},
+                            "sample": "the whole fwd+bwd step of both layers per iteration (C restatement of "
+                                      "the reference's CPU path: CSR SpMM x2 + gather-dot SDDMM per layer)"},
            "e2e": {"value": val, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -297,81 +332,109 @@ def max_over_ranks(x, dev=None):
     return float(t.item())
 
 
-def run_gpu(args):
+def aligned_device(x, dev):
+    """A float32 device copy of x [rows, n] whose row stride is n rounded up
+    to 4 (a view of a padded buffer): what the SpMM kernels read without a
+    copy."""
     import torch
-    import torch.distributed as dist
+    rows, n = x.shape
+    ld = (n + 3) // 4 * 4
+    buf = torch.zeros((rows, ld), dtype=torch.float32, device=dev)
+    buf[:, :n] = torch.as_tensor(np.ascontiguousarray(x, np.float32), device=dev)
+    return buf[:, :n]
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
 
-    from stile_gb300 import device as D
-    from stile_gb300.api import HybridSpMMFunction, PlanConfig, SpmmOperator
-    from stile_gb300.ops import CsrMatrix, DeviceSddmmPlan, launch_count
+def aligned_empty(rows, n, dev, pin=False):
+    import torch
+    ld = (n + 3) // 4 * 4
+    if pin:
+        return torch.empty((rows, ld), dtype=torch.float32, pin_memory=True)[:, :n]
+    return torch.empty((rows, ld), dtype=torch.float32, device=dev)[:, :n]
 
-    t0 = time.time()
-    A, B_np, dC_np = make_workload()
-    log(f"[bench] workload {A.shape} nnz={A.nnz} ({time.time() - t0:.1f}s)")
-    t0 = time.time()
-    tc_mode = D.TC_BF16
-    cfg = PlanConfig(tc_mode=tc_mode)
-    op = SpmmOperator(A, N_FEAT, cfg)
-    opT, perm = op.transposed
-    t_plan = time.time() - t0
-    log(f"[bench] plan {op.plan.summary()} levels={op.plan.level_num} ({t_plan:.1f}s)")
-    nnz = A.nnz
-    flops = 3 * 2 * nnz * N_FEAT
-    B = torch.as_tensor(B_np, device=dev)
-    dC = torch.as_tensor(dC_np, device=dev)
-    C = torch.empty((A.shape[0], N_FEAT), device=dev)
-    dB = torch.empty((A.shape[1], N_FEAT), device=dev)
 
-    # plain CSR comparator: CSR-row SpMM for A and A^T, gather-dot SDDMM
-    csrA = CsrMatrix(A)
-    AT = opT.A
-    csrAT = CsrMatrix(AT)
-    ids = np.arange(nnz, dtype=np.int64)
-    plain_dev = D.SddmmDevice(M=A.shape[0], K=A.shape[1], nnz=nnz,
-                              mid_idx=np.repeat(np.arange(A.shape[0]), np.diff(A.indptr)).astype(np.int32),
-                              j_idx=A.indices.astype(np.int32), remap=ids.astype(np.int32), bm=16, bn=16,
-                              blk_i=np.zeros(0, np.int32), blk_j=np.zeros(0, np.int32),
-                              blk_indptr=np.zeros(1, np.int32), blk_dense_pos=np.zeros(0, np.int32),
-                              blk_out=np.zeros(0, np.int32))
-    plain_sddmm = DeviceSddmmPlan(plain_dev)
+class SparseStep:
+    """The step's sparse products on the GPU for one adjacency and a list of
+    layer widths: operators (one plan per width; the transposed operator of
+    a symmetric pattern reuses the forward plan), device-resident operands
+    and outputs, the plain CSR comparator."""
 
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    def __init__(self, A, layers, dev, tc_mode):
+        from stile_gb300.api import PlanConfig, SpmmOperator
+        self.A, self.dev = A, dev
+        t0 = time.time()
+        self.ops = []
+        for B, _ in layers:
+            op = SpmmOperator(A, B.shape[1], PlanConfig(tc_mode=tc_mode))
+            op.transposed
+            self.ops.append(op)
+        self.plan_s = time.time() - t0
+        self.B = [aligned_device(B, dev) for B, _ in layers]
+        self.dC = [aligned_device(dC, dev) for _, dC in layers]
+        self.C = [aligned_empty(A.shape[0], B.shape[1], dev) for B, _ in layers]
+        self.dB = [aligned_empty(A.shape[1], B.shape[1], dev) for B, _ in layers]
+        self.dv = [None] * len(layers)
+        self.flops = step_flops(A, layers)
 
-    def hybrid_step(ev=None):
-        if ev is not None:
-            ev[0].record()
-        op(B, out=C)
-        if ev is not None:
-            ev[1].record()
-        dv = op.dvals(dC, B)
-        opT(dC, out=dB)
-        if ev is not None:
-            ev[2].record()
-        return dv
+    def forward(self, ev=None):
+        for i, op in enumerate(self.ops):
+            if ev is not None and i == 0:
+                ev[0].record()
+            op(self.B[i], out=self.C[i])
+            if ev is not None and i == 0:
+                ev[1].record()
 
-    def plain_step():
-        csrA.spmm(B, out=C)
-        plain_sddmm.run(dC, B)
-        csrAT.spmm(dC, out=dB)
+    def backward(self):
+        for i in reversed(range(len(self.ops))):
+            op = self.ops[i]
+            self.dv[i] = op.dvals(self.dC[i], self.B[i])
+            op.transposed[0](self.dC[i], out=self.dB[i])
 
-    # accuracy against the FP64 oracle (outside the timed region)
-    import oracle.semantics as S
-    hybrid_step()
-    torch.cuda.synchronize()
-    dv = op.dvals(dC, B)
-    acc = {}
-    acc.update(errors("C", C.cpu().numpy(), S.spmm_fp64(A, B_np)))
-    acc.update(errors("dvals", dv.cpu().numpy(), S.sddmm_fp64(A, dC_np, B_np)))
-    acc.update(errors("dB", dB.cpu().numpy(), S.spmm_fp64(AT, dC_np)))
-    log(f"[bench] accuracy {acc}")
+    def step(self, ev=None):
+        self.forward(ev)
+        self.backward()
+
+    def accuracy(self, layers):
+        import oracle.semantics as S
+        from stile_gb300 import workloads as W
+        AT = self.ops[0].transposed[0].A
+        acc = {}
+        for i, (B, dC) in enumerate(layers):
+            tag = f"N{B.shape[1]}_"
+            acc.update(errors(tag + "C", self.C[i].cpu().numpy(), S.spmm_fp64(self.A, B)))
+            acc.update(errors(tag + "dB", self.dB[i].cpu().numpy(), S.spmm_fp64(AT, dC)))
+            ids, ref = W.sddmm_fp64_sample(self.A, dC, B)
+            acc.update(errors(tag + "dvals_sampled", self.dv[i].cpu().numpy()[ids], ref))
+        return acc
+
+    def plain(self):
+        """The plain CSR path on the same GPU: CSR-row SpMM for A and A^T and
+        the gather-dot SDDMM per layer."""
+        from stile_gb300 import device as D
+        from stile_gb300.ops import CsrMatrix, DeviceSddmmPlan
+        A = self.A
+        csrA, csrAT = CsrMatrix(A), CsrMatrix(self.ops[0].transposed[0].A)
+        plain_dev = D.SddmmDevice(M=A.shape[0], K=A.shape[1], nnz=A.nnz,
+                                  mid_idx=np.repeat(np.arange(A.shape[0]), np.diff(A.indptr)).astype(np.int32),
+                                  j_idx=A.indices.astype(np.int32), remap=np.arange(A.nnz, dtype=np.int32),
+                                  bm=16, bn=16, blk_i=np.zeros(0, np.int32), blk_j=np.zeros(0, np.int32),
+                                  blk_indptr=np.zeros(1, np.int32), blk_dense_pos=np.zeros(0, np.int32),
+                                  blk_out=np.zeros(0, np.int32))
+        sd = DeviceSddmmPlan(plain_dev)
+
+        def step():
+            for i in range(len(self.ops)):
+                csrA.spmm(self.B[i], out=self.C[i])
+            for i in reversed(range(len(self.ops))):
+                sd.run(self.dC[i], self.B[i])
+                csrAT.spmm(self.dC[i], out=self.dB[i])
+        return step
+
+    def plan_summary(self):
+        return [{f"{k[0]}{'/atomic' if k[1] else ''}": v for k, v in op.plan.summary().items()} for op in self.ops]
+
+
+def make_timer(flush):
+    import torch
 
     def timed(fn, steps, per_step_events=False):
         times, fwd = [], []
@@ -379,7 +442,7 @@ def run_gpu(args):
             flush.zero_()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             if per_step_events:
-                ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
                 s.record()
                 fn(ev)
                 e.record()
@@ -393,10 +456,128 @@ def run_gpu(args):
                 e.synchronize()
                 times.append(s.elapsed_time(e))
         return times, fwd
+    return timed
 
+
+def run_secondary_graph(dev, tc_mode, steps, timed, peak):
+    """The 169,343-node graph (one layer, N = 128): step, forward and the
+    plain CSR step, accuracy, forward roofline, and the plan of the learned
+    cost model against the analytic one."""
+    import oracle.semantics as S
+    from stile_gb300.api import PlanConfig, SpmmOperator
+    A, layers = make_graph_workload()
+    st = SparseStep(A, layers, dev, tc_mode)
+    st.step()
+    import torch
+    torch.cuda.synchronize()
+    acc = st.accuracy(layers)
+    for _ in range(3):
+        st.step()
+    t, fwd = timed(st.step, steps, per_step_events=True)
+    ms = float(np.mean(t))
+    fwd_ms = float(np.mean(fwd))
+    plain = st.plain()
+    for _ in range(3):
+        plain()
+    tp, _ = timed(plain, steps)
+    plain_ms = float(np.mean(tp))
+    alg = algorithmic_bytes_spmm(A, layers[0][0].shape[1])
+    out = {"workload": GRAPH_WORKLOAD, "config": base_config(A, layers, GRAPH_WORKLOAD), "plan": st.plan_summary(),
+           "plan_search_s": round(st.plan_s, 2), "value": st.flops / (ms * 1e-3) / 1e9, "unit": "GFLOP/s",
+           "ms_per_step": ms, "forward_ms": fwd_ms, "csr_step_ms": plain_ms,
+           "speedup_hybrid_over_csr": plain_ms / ms,
+           "roofline_forward": {"algorithmic_bytes": int(alg), "achieved_gbs": alg / (fwd_ms * 1e-3) / 1e9,
+                                "frac": alg / (fwd_ms * 1e-3) / 1e9 / peak},
+           "accuracy": acc}
+    # the learned cost model, measured by the forward time of the plan it chooses
+    try:
+        t0 = time.time()
+        op_l = SpmmOperator(A, layers[0][0].shape[1], PlanConfig(tc_mode=tc_mode, learned=True))
+        t_l = time.time() - t0
+        Cl = torch.empty_like(st.C[0])
+        op = st.ops[0]
+        for _ in range(3):
+            op_l(st.B[0], out=Cl)
+            op(st.B[0], out=st.C[0])
+        tl, _ = timed(lambda: op_l(st.B[0], out=Cl), max(steps, 5))
+        ta, _ = timed(lambda: op(st.B[0], out=st.C[0]), max(steps, 5))
+        from stile_gb300.cost_model import gb300_mlp_model
+        mm = gb300_mlp_model().meta
+        out["learned_cost_model"] = {
+            "plan_forward_ms": float(np.median(tl)), "analytic_plan_forward_ms": float(np.median(ta)),
+            "plan": {f"{k[0]}{'/atomic' if k[1] else ''}": v for k, v in op_l.plan.summary().items()},
+            "plan_search_s": round(t_l, 2),
+            "held_out_mean_abs_log_err": {k: {"mlp": v["test_mean_abs_log_err_mlp"],
+                                              "analytic": v["test_mean_abs_log_err_analytic"]} for k, v in mm.items()},
+            "C_rel_fro": S.rel_fro(Cl.cpu().numpy(), S.spmm_fp64(A, layers[0][0]))}
+        op_l.handle.close()
+    except FileNotFoundError as exc:
+        out["learned_cost_model"] = {"unavailable": str(exc)}
+    return out
+
+
+def gcn_training_step_ms(st, dev, timed, steps):
+    """The whole two-layer GCN training step (dense GEMMs, ReLU, the sparse
+    products and their backward; X resident on the device) for context."""
+    import torch
+    from stile_gb300.gcn import TwoLayerGCN
+    n = st.A.shape[0]
+    g = torch.Generator(device=dev).manual_seed(7)
+    X = torch.randn((n, 602), device=dev, generator=g)
+    W1 = torch.randn((602, WIDTHS[0]), device=dev, generator=g) / 602 ** 0.5
+    W2 = torch.randn((WIDTHS[0], WIDTHS[1]), device=dev, generator=g) / WIDTHS[0] ** 0.5
+    G = torch.randn((n, WIDTHS[1]), device=dev, generator=g)
+    model = TwoLayerGCN(st.A, W1, W2, ops=tuple(st.ops))
+    params = [model.lin1.weight, model.lin2.weight, model.vals]
+
+    def train_step():
+        H2 = model(X)
+        torch.autograd.grad(H2, params, grad_outputs=G)
+
+    for _ in range(3):
+        train_step()
+    t, _ = timed(train_step, steps)
+    del X
+    return float(np.mean(t))
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from stile_gb300 import device as D
+    from stile_gb300.api import HybridSpMMFunction
+    from stile_gb300.ops import launch_count
+
+    t0 = time.time()
+    A, layers = make_gcn_workload()
+    log(f"[bench] workload {A.shape} nnz={A.nnz} ({time.time() - t0:.1f}s)")
+    tc_mode = D.TC_BF16
+    st = SparseStep(A, layers, dev, tc_mode)
+    log(f"[bench] plans {st.plan_summary()} ({st.plan_s:.1f}s)")
+    flops = st.flops
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    timed = make_timer(flush)
+    peak, peak_kind = measured_peaks()
+
+    # accuracy against the FP64 oracle (outside the timed region)
+    st.step()
+    torch.cuda.synchronize()
+    acc = st.accuracy(layers)
+    log(f"[bench] accuracy {acc}")
+
+    plain = st.plain()
     for _ in range(max(args.warmup, 3)):
-        hybrid_step()
-        plain_step()
+        st.step()
+        plain()
     torch.cuda.synchronize()
 
     if world > 1:
@@ -405,69 +586,78 @@ def run_gpu(args):
     launches0 = launch_count()
     wall0 = time.perf_counter()
     with ClockSampler(local) as clk:
-        times, fwd_times = timed(hybrid_step, args.steps, per_step_events=True)
+        times, fwd_times = timed(st.step, args.steps, per_step_events=True)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     launches = launch_count() - launches0
     ms = max_over_ranks(float(np.sum(times)) / args.steps, dev)
     value = world * flops / (ms * 1e-3) / 1e9
 
-    plain_times, _ = timed(plain_step, args.steps)
+    plain_times, _ = timed(plain, args.steps)
     plain_ms = float(np.sum(plain_times)) / args.steps
     plain_value = flops / (plain_ms * 1e-3) / 1e9
 
-    # roofline of the dominant kernel: the fused forward SpMM
+    # roofline of the dominant kernel: the layer-1 forward SpMM (N = 128)
     fwd_ms = float(np.mean(fwd_times))
-    alg = algorithmic_bytes_spmm(A, N_FEAT)
-    peak, peak_kind = measured_peaks()
+    alg = algorithmic_bytes_spmm(A, WIDTHS[0])
     achieved = alg / (fwd_ms * 1e-3) / 1e9
-    traffic = profile_traffic("fused_spmm_hybrid_graph.md")
-    step_bytes = 2 * alg + algorithmic_bytes_sddmm(A, N_FEAT)
+    traffic = profile_traffic("fused_spmm_gcn.md")
+    step_bytes = sum(2 * algorithmic_bytes_spmm(A, B.shape[1]) + algorithmic_bytes_sddmm(A, B.shape[1])
+                     for B, _ in layers)
 
-    # end to end through the public autograd API with host buffers
+    # end to end through the public autograd API with host buffers: each
+    # layer's operand and output gradient go up from pinned memory, every
+    # product comes back (C_l, dB_l, and the shared value gradient)
     vals = torch.as_tensor(A.data.astype(np.float32), device=dev)
-    hB = torch.empty((A.shape[1], N_FEAT), dtype=torch.float32, pin_memory=True)
-    hB.copy_(torch.as_tensor(B_np))
-    hdC = torch.empty((A.shape[0], N_FEAT), dtype=torch.float32, pin_memory=True)
-    hdC.copy_(torch.as_tensor(dC_np))
-    hC = torch.empty((A.shape[0], N_FEAT), dtype=torch.float32, pin_memory=True)
-    hdB = torch.empty((A.shape[1], N_FEAT), dtype=torch.float32, pin_memory=True)
-    hdv = torch.empty(nnz, dtype=torch.float32, pin_memory=True)
-
-    # copies run on two side streams so that the two directions of the
-    # host link overlap each other and the kernels: B then dC go up on one,
-    # C comes down while the backward runs, then dvals and dB
+    hB = [aligned_empty(A.shape[1], B.shape[1], dev, pin=True) for B, _ in layers]
+    hdC = [aligned_empty(A.shape[0], B.shape[1], dev, pin=True) for B, _ in layers]
+    for i, (B, dC) in enumerate(layers):
+        hB[i].copy_(torch.as_tensor(B))
+        hdC[i].copy_(torch.as_tensor(dC))
+    hC = [aligned_empty(A.shape[0], B.shape[1], dev, pin=True) for B, _ in layers]
+    hdB = [aligned_empty(A.shape[1], B.shape[1], dev, pin=True) for B, _ in layers]
+    hdv = torch.empty(A.nnz, dtype=torch.float32, pin_memory=True)
+    Bd = [aligned_empty(A.shape[1], B.shape[1], dev) for B, _ in layers]
+    dCd = [aligned_empty(A.shape[0], B.shape[1], dev) for B, _ in layers]
     main = torch.cuda.current_stream(dev)
     up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    B_dev = torch.empty((A.shape[1], N_FEAT), device=dev)
-    dC_dev = torch.empty((A.shape[0], N_FEAT), device=dev)
+    L = len(layers)
 
     def e2e_step():
-        ev_b, ev_dc, ev_c, ev_bw = (torch.cuda.Event() for _ in range(4))
+        ev_b = [torch.cuda.Event() for _ in range(L)]
+        ev_dc = torch.cuda.Event()
         up.wait_stream(main)
         with torch.cuda.stream(up):
-            B_dev.copy_(hB, non_blocking=True)
-            ev_b.record(up)
-            dC_dev.copy_(hdC, non_blocking=True)
+            for i in range(L):
+                Bd[i].copy_(hB[i], non_blocking=True)
+                ev_b[i].record(up)
+            for i in range(L):
+                dCd[i].copy_(hdC[i], non_blocking=True)
             ev_dc.record(up)
-        main.wait_event(ev_b)
-        B_in = B_dev.detach().requires_grad_(True)
         v = vals.detach().requires_grad_(True)
-        Cc = HybridSpMMFunction.apply(v, B_in, op)
-        ev_c.record(main)
-        down.wait_event(ev_c)
-        with torch.cuda.stream(down):
-            hC.copy_(Cc.detach(), non_blocking=True)
-        Cc.record_stream(down)
+        Bin, Cs = [], []
+        for i in range(L):
+            main.wait_event(ev_b[i])
+            b = Bd[i].detach().requires_grad_(True)
+            Bin.append(b)
+            Cs.append(HybridSpMMFunction.apply(v, b, st.ops[i]))
+            ev_c = torch.cuda.Event()
+            ev_c.record(main)
+            down.wait_event(ev_c)
+            with torch.cuda.stream(down):
+                hC[i].copy_(Cs[i].detach(), non_blocking=True)
+            Cs[i].record_stream(down)
         main.wait_event(ev_dc)
-        gv, gB = torch.autograd.grad(Cc, [v, B_in], grad_outputs=dC_dev)
+        grads = torch.autograd.grad(Cs, [v] + Bin, grad_outputs=dCd)
+        ev_bw = torch.cuda.Event()
         ev_bw.record(main)
         down.wait_event(ev_bw)
         with torch.cuda.stream(down):
-            hdv.copy_(gv, non_blocking=True)
-            hdB.copy_(gB, non_blocking=True)
-        gv.record_stream(down)
-        gB.record_stream(down)
+            hdv.copy_(grads[0], non_blocking=True)
+            for i in range(L):
+                hdB[i].copy_(grads[1 + i], non_blocking=True)
+        for g_ in grads:
+            g_.record_stream(down)
         main.wait_stream(down)
 
     for _ in range(2):
@@ -476,65 +666,33 @@ def run_gpu(args):
     e2e_times, _ = timed(e2e_step, args.steps)
     e2e_ms = max_over_ranks(float(np.sum(e2e_times)) / args.steps, dev)
     e2e_val = world * flops / (e2e_ms * 1e-3) / 1e9
-    h2d = hB.numel() * 4 + hdC.numel() * 4
-    d2h = hC.numel() * 4 + hdv.numel() * 4 + hdB.numel() * 4
+    h2d = sum(B.shape[0] * B.shape[1] * 4 + dC.shape[0] * dC.shape[1] * 4 for B, dC in layers)
+    d2h = sum(A.shape[0] * B.shape[1] * 4 + A.shape[1] * B.shape[1] * 4 for B, _ in layers) + A.nnz * 4
 
-    # the learned cost model, measured by the forward time of the plan it chooses
-    learned = None
-    try:
-        t0 = time.time()
-        op_l = SpmmOperator(A, N_FEAT, PlanConfig(tc_mode=tc_mode, learned=True))
-        t_l = time.time() - t0
-        Cl = torch.empty_like(C)
+    train_ms = gcn_training_step_ms(st, dev, timed, args.steps)
+    secondary = run_secondary_graph(dev, tc_mode, args.steps, timed, peak) if rank == 0 else None
 
-        def fwd_learned():
-            op_l(B, out=Cl)
-
-        def fwd_analytic():
-            op(B, out=C)
-
-        for _ in range(3):
-            fwd_learned()
-            fwd_analytic()
-        tl, _ = timed(fwd_learned, max(args.steps, 5))
-        ta, _ = timed(fwd_analytic, max(args.steps, 5))
-        meta = op_l.plan.meta
-        from stile_gb300.cost_model import gb300_mlp_model
-        mm = gb300_mlp_model().meta
-        learned = {"plan_forward_ms": float(np.median(tl)), "analytic_plan_forward_ms": float(np.median(ta)),
-                   "plan": {f"{k[0]}{'/atomic' if k[1] else ''}": v for k, v in op_l.plan.summary().items()},
-                   "plan_search_s": round(t_l, 2), "cost_model": meta.get("cost_model"),
-                   "held_out_mean_abs_log_err": {k: {"mlp": v["test_mean_abs_log_err_mlp"],
-                                                     "analytic": v["test_mean_abs_log_err_analytic"]}
-                                                 for k, v in mm.items()},
-                   "C_rel_fro": S.rel_fro(Cl.cpu().numpy(), S.spmm_fp64(A, B_np))}
-        op_l.handle.close()
-    except FileNotFoundError as exc:
-        learned = {"unavailable": str(exc)}
-
-    cpu = run_cpu_baseline(A, B_np, dC_np, flops) if (rank == 0 and world == 1) else None
+    cpu = run_cpu_baseline(A, layers, flops) if (rank == 0 and world == 1) else None
 
     if rank == 0:
+        cfg = base_config(A, layers, WORKLOAD)
+        cfg.update({"tc_tiles": "bf16 operands, fp32 accumulate (tcgen05, TMEM)", "row_tiles": "fp32 (CUDA cores)",
+                    "plans": st.plan_summary(), "plan_search_s": round(st.plan_s, 2),
+                    "cost_model": st.ops[0].plan.meta.get("cost_model"),
+                    "l2": "flushed between steps (256 MiB write, untimed)",
+                    "parallelism": "replicas" if world > 1 else "single GPU"})
         out = {
             "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "M": int(A.shape[0]), "K": int(A.shape[1]), "nnz": int(nnz),
-                       "N": N_FEAT, "tc_tiles": "bf16 operands, fp32 accumulate"
-                       + " (tcgen05, TMEM)",
-                       "row_tiles": "fp32 (CUDA cores)", "plan": {f"{k[0]}{'/atomic' if k[1] else ''}": v
-                                                                for k, v in op.plan.summary().items()},
-                       "plan_levels": int(op.plan.level_num), "plan_search_s": round(t_plan, 2),
-                       "cost_model": op.plan.meta.get("cost_model"),
-                       "l2": "flushed between steps (256 MiB write, untimed)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic", "config": cfg,
             "e2e": {"value": e2e_val, "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
-                    "path": "HybridSpMMFunction forward + torch.autograd.grad, pinned host buffers; "
-                            "copies on two side streams (up: B, dC; down: C during the backward, then dvals, dB)"},
+                    "path": "HybridSpMMFunction forward of both layers + torch.autograd.grad, pinned host "
+                            "buffers; copies on two side streams (up: B_l, dC_l; down: C_l during the rest, "
+                            "then the value gradient and dB_l)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "forward SpMM (zero-rows + fused hybrid kernel)",
+                         "kernel": "layer-1 forward SpMM (N = 128)",
                          "algorithmic_bytes_per_launch": int(alg), "ms_per_launch": fwd_ms,
                          "peak_source": peak_kind},
             "step_roofline": {"algorithmic_bytes_per_step": int(step_bytes),
@@ -543,7 +701,10 @@ def run_gpu(args):
             "csr_baseline": {"value": plain_value, "unit": "GFLOP/s", "ms_per_step": plain_ms,
                              "speedup_hybrid_over_csr": value / plain_value},
             "accuracy": acc,
-            "learned_cost_model": learned,
+            "gcn_training_step": {"ms": train_ms, "what": "whole two-layer GCN step (X W1, Z1 W2 and their "
+                                                          "gradients in torch fp32 GEMMs, ReLU, the sparse "
+                                                          "products), X resident"},
+            "secondary": secondary,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
@@ -555,7 +716,7 @@ def run_gpu(args):
 
 
 # ---------------------------------------------------------------------------
-# the other configurations (one JSON line each; the headline is "graph")
+# the other configurations (one JSON line each; the headline is "gcn2")
 # ---------------------------------------------------------------------------
 def run_config(args):
     import torch
@@ -735,13 +896,14 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="stile", choices=["stile", "reference"])
-    ap.add_argument("--workload", default="graph",
-                    help="graph (the headline line) or one of the other configurations: plain, plain_min10, "
-                         "pruned, pruned_t, sddmm, gcn, gcn_41 (one JSON line of measurements each)")
+    ap.add_argument("--workload", default="gcn2",
+                    help="gcn2 (the headline line: the two-layer GCN step) or one of the configurations: "
+                         "plain, plain_min10, graph, pruned, pruned_t, sddmm, gcn, gcn_41 (one JSON line of "
+                         "measurements each)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload != "graph":
+    elif args.workload != "gcn2":
         run_config(args)
     else:
         run_gpu(args)

@@ -23,7 +23,8 @@
  *   stile_csr_spmm_run
  *       -- the plain CSR SpMM comparator (the reference times cuSPARSE CSR
  *          through torch.sparse_csr_tensor @ B, gen_formats_v2.py:3079-3106)
- *   stile_plan_free / stile_last_error / stile_plan_error_flag
+ *   stile_spmm_plan_free / stile_sddmm_plan_free / stile_last_error /
+ *   stile_spmm_plan_error_flag / stile_spmm_plan_set_wait_policy
  *       -- ownership and error reporting (the reference relies on TVM
  *          NDArray lifetimes and asserts)
  *
@@ -252,9 +253,10 @@ int stile_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t
  * compiled into the library: STILE_CSR_NOALLOC_MAX_GROUPS entries (1 MiB),
  * held by every GPU that loads the library until the process exits, so
  * nnz <= STILE_CSR_NOALLOC_MAX_GROUPS * stile_csr_group_nnz() (16,777,216);
- * larger inputs are rejected with STILE_E_INVALID.  The first call on each
- * device looks up the array's device address (with that device current);
- * make that first call before any stream capture.  All calls on a device
+ * larger inputs are rejected with STILE_E_INVALID.  Every call looks up
+ * the array's address on the current device (cudaGetSymbolAddress, which
+ * allocates nothing); the first call on a device loads the library's module
+ * there, so make that first call before any stream capture.  All calls on a device
  * share the array: every entry a call reads it writes first, but calls that
  * overlap on the GPU (unordered streams) race on it. */
 #define STILE_CSR_NOALLOC_MAX_GROUPS (1 << 18)
@@ -271,6 +273,19 @@ int stile_spmm_plan_set_values(StileSpmmPlan* plan, const float* vals, void* str
 /* Device-side error flag of a plan's kernels (bounded waits that gave up):
  * synchronises the stream, returns the flag (0 = none) and clears it. */
 int stile_spmm_plan_error_flag(StileSpmmPlan* plan, void* stream, int32_t* flag);
+
+/* Wait policy of the plan's tensor-core kernel (failure detection; no
+ * counterpart in the reference).  Every pipeline wait of the kernel (on an
+ * operand slot or an accumulator) gives up after `polls` polls (polls <= 0:
+ * the default, 2^22), sets the plan's error flag and ends its role; the
+ * kernel's wait for its own MMAs before freeing tensor memory keeps the
+ * default.  stall_test != 0 (needs polls > 0) makes the MMA issuer first
+ * wait on a barrier that nothing arrives on, so that wait, and then the
+ * other roles' waits, run out: the run returns with the error flag set and
+ * its output undefined, and later runs with stall_test = 0 are unaffected.
+ * Not thread-safe against runs of the same plan in flight on other host
+ * threads. */
+int stile_spmm_plan_set_wait_policy(StileSpmmPlan* plan, int32_t polls, int32_t stall_test);
 
 /* Tensor-core layout self-check (no counterpart in the reference): runs one
  * tcgen05.mma (M=128, N=16; kind = 0: kind::f16, K=16; kind = 1:

@@ -13,6 +13,7 @@ nonzero of A, computed by walking the forward plan's own tiles.
 from __future__ import annotations
 
 import os
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -96,7 +97,12 @@ class SpmmOperator:
         self.device_layout = D.build_spmm_device(plan.tiles, self.A, N=self.N, tc_mode=self.cfg.tc_mode)
         self.handle = DeviceSpmmPlan(self.device_layout)
         self._transposed = None
-        self._values_version = None
+        # values last loaded with set_values (a device copy, CSR order); None
+        # while the plan still holds the values of A it was built from
+        self._vals = None
+        # (weak reference to the tensor, its version, its address) of the
+        # values HybridSpMMFunction loaded last
+        self._values_key = None
 
     def __call__(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         return self.handle.run(B, out)
@@ -111,13 +117,22 @@ class SpmmOperator:
         return self.handle.run_batched(self.handle.pack_values(vals), B, out)
 
     def set_values(self, vals: torch.Tensor):
+        """Load new values for A's pattern (``vals`` [nnz], CSR order) into
+        the plan, and into the transposed plan when it exists; a transposed
+        plan built later starts from these values too."""
+        vals = vals.detach().float().contiguous()
+        if vals.numel() != self.nnz:
+            raise ValueError("vals must have one entry per nonzero")
         self.handle.set_values(vals)
+        self._vals = vals.clone()
         if self._transposed is not None:
-            self._transposed[0].set_values(vals[self._transposed[1]])
+            self._transposed[0].set_values(self._vals[self._transposed[1]])
 
     @property
     def transposed(self):
-        """(operator of A^T, permutation: A^T nonzero -> A nonzero)."""
+        """(operator of A^T, permutation: A^T nonzero -> A nonzero).  Its
+        values are the ones this operator holds now: the last set_values,
+        else the values of A it was planned with."""
         if self._transposed is None:
             ids = sp.csr_matrix((np.arange(self.nnz, dtype=np.float64) + 1, self.A.indices, self.A.indptr),
                                 shape=self.shape)
@@ -129,7 +144,10 @@ class SpmmOperator:
             if self.shape[0] == self.shape[1] and pattern_key(AT) == pattern_key(self.A):
                 plan = self.plan        # symmetric pattern: same decomposition
             op = SpmmOperator(AT, self.N, self.cfg, plan=plan)
-            self._transposed = (op, torch.as_tensor(perm, device="cuda"))
+            perm_t = torch.as_tensor(perm, device="cuda")
+            if self._vals is not None:
+                op.set_values(self._vals[perm_t])
+            self._transposed = (op, perm_t)
         return self._transposed
 
     def stats(self):
@@ -227,18 +245,24 @@ class HybridSpMMFunction(torch.autograd.Function):
     """C = A(vals) @ B with A's pattern fixed by ``op`` (B fp32 or bf16; C,
     dvals fp32; dB in B's dtype).
 
-    forward : the fused hybrid kernel (values refreshed on device when
-              ``vals`` changed since the last call)
+    forward : the fused hybrid kernel.  The plan's values are reloaded from
+              ``vals`` unless ``vals`` is the very tensor loaded last time,
+              at the same address and version (in-place updates such as an
+              optimizer step bump the version).  Writes through ``vals.data``
+              bypass the version counter: call ``op.set_values`` after them.
     backward: dvals = SDDMM(dC, B) on A's pattern over the forward tiles;
-              dB = A^T @ dC with the cached transposed plan.
+              dB = A^T @ dC with the cached transposed plan, which holds the
+              same values as the forward.
     """
 
     @staticmethod
     def forward(ctx, vals, B, op: SpmmOperator):
-        key = (vals.data_ptr(), vals._version)
-        if op._values_version != key:
+        last = op._values_key
+        same = (last is not None and last[0]() is vals and last[1] == vals._version
+                and last[2] == vals.data_ptr())
+        if not same:
             op.set_values(vals.detach())
-            op._values_version = key
+            op._values_key = (weakref.ref(vals), vals._version, vals.data_ptr())
         C = op(B.detach())
         ctx.save_for_backward(B)
         ctx.op = op
@@ -248,7 +272,8 @@ class HybridSpMMFunction(torch.autograd.Function):
     def backward(ctx, dC):
         (B,) = ctx.saved_tensors
         op = ctx.op
-        dC = dC.contiguous()
+        # dC is passed as it is (a row stride that is a multiple of 4 and a
+        # 16-byte aligned base need no copy; ops.dense_operand copies others)
         dvals = dB = None
         if ctx.needs_input_grad[0]:
             dvals = op.dvals(dC, B)

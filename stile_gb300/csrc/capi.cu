@@ -701,6 +701,15 @@ int stile_spmm_plan_error_flag(StileSpmmPlan* plan, void* stream, int32_t* flag)
   return STILE_OK;
 }
 
+int stile_spmm_plan_set_wait_policy(StileSpmmPlan* plan, int32_t polls, int32_t stall_test) {
+  if (!plan) return fail(STILE_E_INVALID, "null plan");
+  if (stall_test && polls <= 0)
+    return fail(STILE_E_INVALID, "a stall test needs a poll limit (the default wait lasts seconds)");
+  plan->args.poll_limit = polls > 0 ? (uint32_t)polls : 0u;
+  plan->args.stall_test = stall_test ? 1 : 0;
+  return STILE_OK;
+}
+
 int stile_csr_row_softmax(int32_t M, const int32_t* indptr, int64_t nnz, const float* x, float* out, float scale,
                           int32_t batch, void* stream) {
   if (M < 0 || nnz < 0 || batch < 0) return fail(STILE_E_INVALID, "bad shape");

@@ -228,12 +228,13 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t byt
       : "memory");
 }
 
-// Bounded wait: gives up after ~2^22 polls (each try_wait suspends for a
-// bounded, implementation-defined time) and reports failure to the caller.
-// After a few failed polls the thread sleeps between polls, so that waiting
-// warps leave the issue slots to the warps doing the work.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-  for (uint32_t i = 0; i < (1u << 22); ++i) {
+// Bounded wait: gives up after `polls` polls (default 2^22; each try_wait
+// suspends for a bounded, implementation-defined time) and reports failure
+// to the caller.  After a few failed polls the thread sleeps between polls,
+// so that waiting warps leave the issue slots to the warps doing the work.
+constexpr uint32_t kDefaultPolls = 1u << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint32_t polls = kDefaultPolls) {
+  for (uint32_t i = 0; i < polls; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     if (i >= 4) __nanosleep(32);
   }

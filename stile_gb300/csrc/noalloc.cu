@@ -18,7 +18,6 @@
 // other's map and race.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/stile_gb300.h"
@@ -46,24 +45,17 @@ __global__ void csr_group_rows_kernel(int M, const int* __restrict__ indptr, int
   group_rows[g] = lo;
 }
 
-// Device address of the scratch array, looked up once per device (with that
-// device current) by the first call on it.
-static std::mutex g_scratch_mu;
-static void* g_scratch_ptr[256] = {};
-
+// Device address of the scratch array on the current device, looked up on
+// every call (cudaGetSymbolAddress allocates nothing and is cheap).  Not
+// caching it keeps the address right after a cudaDeviceReset, which reloads
+// the library's module at another address.  The first lookup on a device
+// loads the module there, which is why the first call should come before
+// any stream capture.
 static cudaError_t scratch_for_current_device(int** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_csr_group_rows);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_csr_group_rows);
-    if (e != cudaSuccess) return e;
-    g_scratch_ptr[dev] = p;
-  }
-  *out = static_cast<int*>(g_scratch_ptr[dev]);
+  *out = static_cast<int*>(p);
   return cudaSuccess;
 }
 

@@ -185,7 +185,8 @@ static cudaError_t launch_list_b16(long n, const int* rows, const int* cols, con
   const int lpr = F % 128 == 0 ? 16 : lpr_for_f8(F);
   const long groups = (n + kSddmmV - 1) / kSddmmV;
   long grid = (groups + (256 / lpr) - 1) / (256 / lpr);
-  if (grid > 152L * 32) grid = 152L * 32;
+  const long cap = (long)device_sm_count() * 32;  // persistent-style cap: 32 blocks per SM
+  if (grid > cap) grid = cap;
 #define STILE_SDDMM_B16(L)                                                                                      \
   launch_dependent(sddmm_list_kernel<L, kSddmmV, false, 2, kXb, kYb>, dim3((unsigned)grid), dim3(256), 0, st, n, \
                    rows, cols, outs, X, ldx, Y, ldy, out, F)
@@ -210,12 +211,13 @@ cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const in
   const int gpb = 256 / lpr;
   long groups = (n + kSddmmV - 1) / kSddmmV;
   long grid = (groups + gpb - 1) / gpb;
-  if (grid > 152L * 32) grid = 152L * 32;
+  const long cap = (long)device_sm_count() * 32;  // persistent-style cap: 32 blocks per SM
+  if (grid > cap) grid = cap;
   if (F % 128 == 0) {
     // 16-lane groups of 8 features per lane (two groups per warp)
     long groups2 = (n + kSddmmV - 1) / kSddmmV;
     long grid2 = (groups2 + 15) / 16;
-    if (grid2 > 152L * 32) grid2 = 152L * 32;
+    if (grid2 > cap) grid2 = cap;
     return launch_dependent(sddmm_list_kernel<16, kSddmmV, true, 2>, dim3((unsigned)grid2), dim3(256), 0, st, n, rows,
                             cols, outs, X, ldx, Y, ldy, out, F);
   }

@@ -270,6 +270,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
   const long T = (long)S * nf;  // this CTA's k-steps over its slices
   const int n_units = nc * nf;
   const int N = p.N;
+  const uint32_t polls = p.poll_limit ? p.poll_limit : kDefaultPolls;  // pipeline waits
   bool ok = true;
 
   if (warp < kProdWarps) {
@@ -339,12 +340,12 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
         if (gi < T) {
           const uint32_t par = (uint32_t)(g / kWsSlots) & 1u;
           bool got = true;
-          if (lane == 0) got = mbar_wait_bounded(empty0 + 8 * slot, par);
+          if (lane == 0) got = mbar_wait_bounded(empty0 + 8 * slot, par, polls);
           if (!__shfl_sync(0xffffffffu, got, 0)) {
             ok = false;
             break;
           }
-          if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par);  // completed: returns at once
+          if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par, polls);  // completed: returns at once
           issue16(cols_i, li, fi, slot);
           gi += kProdWarps;
           next_of(li, fi, li, fi);
@@ -379,12 +380,12 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
       if (g >= kWsSlots) {
         const uint32_t par = (uint32_t)((g - kWsSlots) / kWsSlots) & 1u;
         bool got = true;
-        if (lane == 0) got = mbar_wait_bounded(empty0 + 8 * slot, par);
+        if (lane == 0) got = mbar_wait_bounded(empty0 + 8 * slot, par, polls);
         if (!__shfl_sync(0xffffffffu, got, 0)) {
           ok = false;
           break;
         }
-        if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par);  // completed: returns at once
+        if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par, polls);  // completed: returns at once
       }
       const uint32_t sa = slots + W::a_off(slot);
 #pragma unroll
@@ -425,13 +426,16 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
                                                     : make_idesc(1, 1, 1, 0, 128, 16);
       long g = 0;
       int u = 0;  // accumulation groups issued so far (accumulator u % kAccBufs)
+      // failure-detection test: nothing arrives on `drain` before the
+      // commit below, so this wait runs out
+      if (p.stall_test && !mbar_wait_bounded(drain, 0u, polls)) ok = false;
 #pragma unroll 1
       for (int t = 0; t < n_units && ok; ++t) {
         const int n = __ldg(p.tc_chunk_nk + cb + t % nc);
 #pragma unroll 1
         for (int s0 = 0; s0 < n && ok; s0 += W::kGroup, ++u) {
           const int b = u % kAccBufs;
-          if (u >= kAccBufs && !mbar_wait_bounded(acce0 + 8 * b, (uint32_t)((u - kAccBufs) / kAccBufs) & 1u)) {
+          if (u >= kAccBufs && !mbar_wait_bounded(acce0 + 8 * b, (uint32_t)((u - kAccBufs) / kAccBufs) & 1u, polls)) {
             ok = false;
             break;
           }
@@ -441,7 +445,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
 #pragma unroll 1
           for (int s = s0; s < s1; ++s, ++g) {
             const int slot = (int)(g % kWsSlots);
-            if (!mbar_wait_bounded(full0 + 8 * slot, (uint32_t)(g / kWsSlots) & 1u)) {
+            if (!mbar_wait_bounded(full0 + 8 * slot, (uint32_t)(g / kWsSlots) & 1u, polls)) {
               ok = false;
               break;
             }
@@ -482,12 +486,12 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
         const int b = u % kAccBufs;
         const uint32_t par = (uint32_t)(u / kAccBufs) & 1u;
         bool got = true;
-        if (lane == 0) got = mbar_wait_bounded(accf0 + 8 * b, par);
+        if (lane == 0) got = mbar_wait_bounded(accf0 + 8 * b, par, polls);
         if (!__shfl_sync(0xffffffffu, got, 0)) {
           ok = false;
           break;
         }
-        if (lane != 0) mbar_wait_bounded(accf0 + 8 * b, par);  // completed: returns at once
+        if (lane != 0) mbar_wait_bounded(accf0 + 8 * b, par, polls);  // completed: returns at once
         tc_fence_after();
         uint32_t r[16];
         tmem_ld16(tmem + (uint32_t)(16 * b) + ((uint32_t)(32 * quarter) << 16), r);
@@ -958,6 +962,22 @@ cudaError_t launch_tc(const SpmmArgs& args, cudaStream_t st) {
   }
 }
 
+// Streaming multiprocessors of the current device (cached per device; 1 if
+// the query fails, which only shrinks grids).
+int device_sm_count() {
+  static std::mutex mu;
+  static std::map<int, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) return it->second;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+  cache[dev] = sms;
+  return sms;
+}
+
 // Blocks of the ELL kernels: x over groups; when that leaves the GPU short
 // of blocks (a wide B over few groups), y splits the feature passes, up to
 // about ten blocks per SM in all.
@@ -965,7 +985,7 @@ cudaError_t launch_tc(const SpmmArgs& args, cudaStream_t st) {
 static dim3 ell_grid(SpmmArgs& p, int groups_per_block, int pass) {
   const long gx = (p.ell_n_groups + groups_per_block - 1) / groups_per_block;
   const int n_pass = (p.N + pass - 1) / pass;
-  const long want = 152L * 10;
+  const long want = (long)device_sm_count() * 10;
   long gy = gx >= want ? 1 : (want + gx - 1) / gx;
   gy = std::max(1L, std::min<long>(gy, n_pass));
   const int per = (int)((n_pass + gy - 1) / gy);

@@ -67,6 +67,14 @@ struct SpmmArgs {
   const int* dv_id;
   // device error flag (bounded waits that gave up)
   int* err_flag;
+  // polls of every pipeline wait of the tensor-core kernel before it gives
+  // up (0: the default); the final wait for the kernel's own MMAs always
+  // uses the default, so TMEM is freed only after they completed
+  uint32_t poll_limit;
+  // failure-detection test: the MMA thread first waits on a barrier that
+  // nothing arrives on, so that wait and then every other role's wait runs
+  // out and the kernel returns with the error flag set
+  int stall_test;
 };
 
 cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const float* vals,
@@ -85,6 +93,8 @@ void note_launches(int n);
 // CTAs of the persistent tensor-core kernel resident on the current device
 // (0 on error)
 int tc_persistent_ctas(int mode);
+// streaming multiprocessors of the current device (cached; 1 on error)
+int device_sm_count();
 cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st);
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st);
 constexpr int kChunkSteps = 32;

@@ -78,6 +78,88 @@ class PackedValues:
         self.ptr = buf.data_ptr() + off
 
 
+def spmm_plan_host(dev: SpmmDevice):
+    """(StileSpmmPlanHost over the arrays of ``dev``, the arrays it points
+    into): the host side of stile_spmm_plan_upload.  The arrays must stay
+    alive until the upload returns."""
+    h = _lib.SpmmPlanHost()
+    h.M, h.K, h.nnz = dev.M, dev.K, dev.nnz
+    h.tc_mode = dev.tc_mode
+    h.tc_n_items = len(dev.tc_item_flags)
+    h.tc_n_ksteps = len(dev.tc_cols) // 16
+    keep = [dev.tc_item_kbeg, dev.tc_item_flags, dev.tc_out_rows, dev.tc_cols, dev.tc_vals,
+            dev.tc_nnz_id, dev.ell_item_row0, dev.ell_item_K, dev.ell_item_slot0,
+            dev.ell_item_flags, dev.ell_out_row, dev.ell_row_len, dev.ell_vals, dev.ell_kidx,
+            dev.ell_nnz_id, dev.zero_rows]
+    h.tc_item_kbeg = _ptr(dev.tc_item_kbeg)
+    h.tc_item_flags = _ptr(dev.tc_item_flags)
+    h.tc_out_rows = _ptr(dev.tc_out_rows)
+    h.tc_cols = _ptr(dev.tc_cols)
+    h.tc_vals = dev.tc_vals.ctypes.data if dev.tc_vals.size else None
+    h.tc_kstep_bytes = dev.tc_kstep_bytes
+    h.tc_nnz_id = _ptr(dev.tc_nnz_id)
+    h.ell_n_items = len(dev.ell_item_K)
+    h.ell_n_rows = len(dev.ell_out_row)
+    h.ell_n_slots = len(dev.ell_kidx)
+    h.ell_item_row0 = _ptr(dev.ell_item_row0)
+    h.ell_item_K = _ptr(dev.ell_item_K)
+    h.ell_item_slot0 = _ptr(dev.ell_item_slot0)
+    h.ell_item_flags = _ptr(dev.ell_item_flags)
+    h.ell_out_row = _ptr(dev.ell_out_row)
+    h.ell_row_len = _ptr(dev.ell_row_len)
+    h.ell_vals = _ptr(dev.ell_vals, ctypes.c_float)
+    h.ell_kidx = _ptr(dev.ell_kidx)
+    h.ell_nnz_id = _ptr(dev.ell_nnz_id)
+    h.n_zero_rows = len(dev.zero_rows)
+    h.zero_rows = _ptr(dev.zero_rows)
+    return h, keep
+
+
+def sddmm_plan_host(dev: SddmmDevice):
+    """(StileSddmmPlanHost over the arrays of ``dev``, the arrays)."""
+    h = _lib.SddmmPlanHost()
+    h.M, h.K, h.nnz = dev.M, dev.K, dev.nnz
+    h.n_1d = len(dev.mid_idx)
+    h.mid_idx, h.j_idx, h.remap = _ptr(dev.mid_idx), _ptr(dev.j_idx), _ptr(dev.remap)
+    h.n_blk = len(dev.blk_indptr) - 1
+    h.bm, h.bn = dev.bm, dev.bn
+    h.n_blk_nnz = len(dev.blk_out)
+    h.blk_i, h.blk_j = _ptr(dev.blk_i), _ptr(dev.blk_j)
+    h.blk_indptr = _ptr(dev.blk_indptr)
+    h.blk_dense_pos, h.blk_out = _ptr(dev.blk_dense_pos), _ptr(dev.blk_out)
+    keep = [dev.mid_idx, dev.j_idx, dev.remap, dev.blk_i, dev.blk_j, dev.blk_indptr, dev.blk_dense_pos, dev.blk_out]
+    return h, keep
+
+
+def _tiles_cover_every_nonzero(dev: SpmmDevice) -> bool:
+    """True when the written tile entries (tensor-core rows with an output
+    row, live ELL slots of rows with an output row) hold every nonzero id
+    exactly once: the value gradient then writes all of dvals."""
+    ids = []
+    if len(dev.tc_cols):
+        nks = len(dev.tc_cols) // 16
+        item = np.repeat(np.arange(len(dev.tc_item_flags)), np.diff(dev.tc_item_kbeg))
+        rows_ok = dev.tc_out_rows.reshape(-1, 16)[item] >= 0              # [nks, 16]
+        nid = dev.tc_nnz_id.reshape(nks, 16, 16)
+        ids.append(nid[rows_ok[:, :, None] & (nid >= 0)])
+    if len(dev.ell_kidx):
+        K = dev.ell_item_K
+        nrows = np.diff(dev.ell_item_row0)
+        row_k = np.repeat(K, nrows)
+        row_s0 = np.repeat(dev.ell_item_slot0, nrows) + (np.arange(len(row_k)) - np.repeat(dev.ell_item_row0[:-1],
+                                                                                            nrows)) * row_k
+        live = (dev.ell_out_row >= 0) & (dev.ell_row_len > 0)
+        lens = dev.ell_row_len[live].astype(np.int64)
+        starts = row_s0[live].astype(np.int64)
+        slot = np.repeat(starts - np.concatenate([[0], np.cumsum(lens)[:-1]]), lens) + np.arange(lens.sum())
+        nid = dev.ell_nnz_id[slot]
+        ids.append(nid[nid >= 0])
+    if not ids:
+        return dev.nnz == 0
+    ids = np.concatenate(ids).astype(np.int64)
+    return len(ids) == dev.nnz and bool(np.all(np.bincount(ids, minlength=dev.nnz) == 1))
+
+
 class DeviceSpmmPlan:
     """A packed SpMM plan resident on the current CUDA device."""
 
@@ -85,41 +167,12 @@ class DeviceSpmmPlan:
         self.lib = _lib.load()
         self.dev = dev
         self.M, self.K, self.nnz = dev.M, dev.K, dev.nnz
-        h = _lib.SpmmPlanHost()
-        h.M, h.K, h.nnz = dev.M, dev.K, dev.nnz
-        h.tc_mode = dev.tc_mode
-        h.tc_n_items = len(dev.tc_item_flags)
-        h.tc_n_ksteps = len(dev.tc_cols) // 16
-        self._keep = [dev.tc_item_kbeg, dev.tc_item_flags, dev.tc_out_rows, dev.tc_cols, dev.tc_vals,
-                      dev.tc_nnz_id, dev.ell_item_row0, dev.ell_item_K, dev.ell_item_slot0,
-                      dev.ell_item_flags, dev.ell_out_row, dev.ell_row_len, dev.ell_vals, dev.ell_kidx,
-                      dev.ell_nnz_id, dev.zero_rows]
-        h.tc_item_kbeg = _ptr(dev.tc_item_kbeg)
-        h.tc_item_flags = _ptr(dev.tc_item_flags)
-        h.tc_out_rows = _ptr(dev.tc_out_rows)
-        h.tc_cols = _ptr(dev.tc_cols)
-        h.tc_vals = dev.tc_vals.ctypes.data if dev.tc_vals.size else None
-        h.tc_kstep_bytes = dev.tc_kstep_bytes
-        h.tc_scales = None
-        h.tc_nnz_id = _ptr(dev.tc_nnz_id)
-        h.ell_n_items = len(dev.ell_item_K)
-        h.ell_n_rows = len(dev.ell_out_row)
-        h.ell_n_slots = len(dev.ell_kidx)
-        h.ell_item_row0 = _ptr(dev.ell_item_row0)
-        h.ell_item_K = _ptr(dev.ell_item_K)
-        h.ell_item_slot0 = _ptr(dev.ell_item_slot0)
-        h.ell_item_flags = _ptr(dev.ell_item_flags)
-        h.ell_out_row = _ptr(dev.ell_out_row)
-        h.ell_row_len = _ptr(dev.ell_row_len)
-        h.ell_vals = _ptr(dev.ell_vals, ctypes.c_float)
-        h.ell_kidx = _ptr(dev.ell_kidx)
-        h.ell_nnz_id = _ptr(dev.ell_nnz_id)
-        h.n_zero_rows = len(dev.zero_rows)
-        h.zero_rows = _ptr(dev.zero_rows)
+        h, self._keep = spmm_plan_host(dev)
         handle = ctypes.c_void_p()
         _lib.check(self.lib.stile_spmm_plan_upload(ctypes.byref(h), ctypes.byref(handle)),
                    "stile_spmm_plan_upload")
         self.handle = handle
+        self._dvals_cover_all = _tiles_cover_every_nonzero(dev)
 
     def run(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """C = A @ B in fp32; B is fp32 or bf16 (a bf16 B is read as is:
@@ -181,7 +234,9 @@ class DeviceSpmmPlan:
         dY, lddy = dense_operand(dY, "dY")
         bf16 = B.dtype == torch.bfloat16
         B, ldb = dense_operand_bf16(B, "B") if bf16 else dense_operand(B, "B")
-        out = torch.zeros(self.nnz, dtype=torch.float32, device=B.device)
+        # the value gradient writes every nonzero the tiles hold
+        alloc = torch.empty if self._dvals_cover_all else torch.zeros
+        out = alloc(self.nnz, dtype=torch.float32, device=B.device)
         fn = self.lib.stile_spmm_dvals_bf16 if bf16 else self.lib.stile_spmm_dvals
         _lib.check(fn(self.handle, dY.data_ptr(), lddy, B.data_ptr(), ldb, out.data_ptr(), B.shape[1], _stream()),
                    "stile_spmm_dvals_bf16" if bf16 else "stile_spmm_dvals")
@@ -194,6 +249,13 @@ class DeviceSpmmPlan:
             raise ValueError("vals must have one entry per nonzero")
         _lib.check(self.lib.stile_spmm_plan_set_values(self.handle, vals.data_ptr(), _stream()),
                    "stile_spmm_plan_set_values")
+
+    def set_wait_policy(self, polls: int = 0, stall_test: bool = False):
+        """Poll limit of the tensor-core kernel's pipeline waits (0: the
+        default) and the failure-detection stall test
+        (stile_spmm_plan_set_wait_policy)."""
+        _lib.check(self.lib.stile_spmm_plan_set_wait_policy(self.handle, int(polls), 1 if stall_test else 0),
+                   "stile_spmm_plan_set_wait_policy")
 
     def error_flag(self) -> int:
         f = ctypes.c_int32(0)
@@ -218,18 +280,7 @@ class DeviceSddmmPlan:
         self.lib = _lib.load()
         self.dev = dev
         self.M, self.K, self.nnz = dev.M, dev.K, dev.nnz
-        h = _lib.SddmmPlanHost()
-        h.M, h.K, h.nnz = dev.M, dev.K, dev.nnz
-        h.n_1d = len(dev.mid_idx)
-        h.mid_idx, h.j_idx, h.remap = _ptr(dev.mid_idx), _ptr(dev.j_idx), _ptr(dev.remap)
-        h.n_blk = len(dev.blk_indptr) - 1
-        h.bm, h.bn = dev.bm, dev.bn
-        h.n_blk_nnz = len(dev.blk_out)
-        h.blk_i, h.blk_j = _ptr(dev.blk_i), _ptr(dev.blk_j)
-        h.blk_indptr = _ptr(dev.blk_indptr)
-        h.blk_dense_pos, h.blk_out = _ptr(dev.blk_dense_pos), _ptr(dev.blk_out)
-        self._keep = [dev.mid_idx, dev.j_idx, dev.remap, dev.blk_i, dev.blk_j, dev.blk_indptr,
-                      dev.blk_dense_pos, dev.blk_out]
+        h, self._keep = sddmm_plan_host(dev)
         handle = ctypes.c_void_p()
         _lib.check(self.lib.stile_sddmm_plan_upload(ctypes.byref(h), ctypes.byref(handle)),
                    "stile_sddmm_plan_upload")

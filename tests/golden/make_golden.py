@@ -469,7 +469,7 @@ def serialise(mods, case_name, case, op, A, mbs, selected, TC_row_costs, reverse
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="root of the STile project checkout")
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
     mods = import_reference(args.ref)

@@ -71,20 +71,9 @@ def random_values(A, seed=0, dist="uniform"):
     return A
 
 
-# kind::tf32 probe images.  MN-major variant of A [128 (m) x 8 (k)] fp32:
-# 128B-swizzle, atoms of 32 features (LBO 1024 B).  B [16 (n) x 8 (k)] fp32,
-# K-major no swizzle, core matrices 8 rows x 16 B, LBO 128 B (k), SBO 256 B.
-TF32_DESC = (1024, 2048, 2, 128, 256, 0)
-
-
-def a_image_tf32(A, lbo=1024):
-    img = np.zeros(2048, dtype=np.uint32)
-    bits = np.ascontiguousarray(A, dtype=np.float32).view(np.uint32)
-    for m in range(128):
-        for k in range(8):
-            off = (m // 32) * lbo + k * 128 + ((((m % 32) // 4) ^ k) << 4) + (m % 4) * 4
-            img[off // 4] = bits[m, k]
-    return img
+# kind::tf32 probe images: A [128 (m) x 8 (k)] and B [16 (n) x 8 (k)] fp32,
+# both K-major without swizzle (core matrices 8 rows x 16 B, LBO 128 B along
+# k, SBO 256 B between 8-row groups).
 
 
 def b_image_tf32(Bm, lbo=128, sbo=256):
@@ -109,18 +98,18 @@ def a_image_tf32_kmajor(A, lbo=128, sbo=256):
     return img
 
 
-def run_probe_tf32(A, Bm, desc6=TF32_DESC, a_kmajor=False):
+def run_probe_tf32(A, Bm, desc6=(128, 256, 0, 128, 256, 0), a_kmajor=True):
     import torch
     from stile_gb300 import _lib
     lib = _lib.load()
-    aimg = a_image_tf32_kmajor(A, desc6[0], desc6[1]) if a_kmajor else a_image_tf32(A, desc6[0])
+    assert a_kmajor, "the kernels use K-major tf32 operands only"
+    aimg = a_image_tf32_kmajor(A, desc6[0], desc6[1])
     ai = torch.as_tensor(aimg.view(np.int32).copy(), device="cuda")
     bi = torch.as_tensor(b_image_tf32(Bm, desc6[3], desc6[4]).view(np.int32).copy(), device="cuda")
     out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     d = (ctypes.c_uint32 * 6)(*desc6)
-    a_mn = 0 if a_kmajor else 1
-    idesc = (1 << 4) | (2 << 7) | (2 << 10) | (a_mn << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
+    idesc = (1 << 4) | (2 << 7) | (2 << 10) | (0 << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
     rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, 1, out.data_ptr(), err.data_ptr(),
                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     _lib.check(rc, "probe")

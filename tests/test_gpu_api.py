@@ -53,6 +53,63 @@ def test_autograd_follows_new_values():
     assert S.rel_fro(C, S.spmm_fp64(A2, B)) <= 1e-5
 
 
+def test_autograd_first_backward_uses_new_values():
+    """Plan on A's values, then call the function with other values: the
+    first backward builds the transposed plan, and its dB must use the new
+    values, not the ones the plan was built from; a second step with yet
+    other values (the transposed plan now exists) must follow them too."""
+    A = _graph(seed=11)
+    N = 64
+    op = plan_spmm(A, N, PlanConfig(tc_mode=D.TC_SPLIT_BF16))
+    rng = np.random.default_rng(12)
+    B = rng.standard_normal((A.shape[1], N)).astype(np.float32)
+    dC = rng.standard_normal((A.shape[0], N)).astype(np.float32)
+    Bt = torch.as_tensor(B, device="cuda").requires_grad_(True)
+    dCt = torch.as_tensor(dC, device="cuda")
+    for step in range(2):
+        new = rng.uniform(-1, 1, A.nnz)
+        A2 = sp.csr_matrix((new, A.indices, A.indptr), shape=A.shape)
+        vals = torch.as_tensor(new.astype(np.float32), device="cuda").requires_grad_(True)
+        C = HybridSpMMFunction.apply(vals, Bt, op)
+        gv, gB = torch.autograd.grad(C, [vals, Bt], grad_outputs=dCt)
+        assert S.rel_fro(C.detach().cpu().numpy(), S.spmm_fp64(A2, B)) <= 1e-5, step
+        assert S.rel_fro(gB.cpu().numpy(), S.spmm_fp64(A2.T.tocsr(), dC)) <= 1e-5, step
+        assert S.rel_fro(gv.cpu().numpy(), S.sddmm_fp64(A2, dC, B)) <= 1e-5, step
+
+
+def test_autograd_reloads_values_of_a_new_tensor_and_after_inplace_update():
+    """A values tensor freed and a new one allocated (the caching allocator
+    hands back the same block, version 0), and an in-place update of the
+    values (an optimizer step): each forward and backward uses the values
+    the tensor holds."""
+    A = _graph(seed=13)
+    N = 32
+    op = plan_spmm(A, N, PlanConfig(tc_mode=D.TC_SPLIT_BF16))
+    rng = np.random.default_rng(14)
+    B = rng.standard_normal((A.shape[1], N)).astype(np.float32)
+    dC = rng.standard_normal((A.shape[0], N)).astype(np.float32)
+    Bt = torch.as_tensor(B, device="cuda").requires_grad_(True)
+    dCt = torch.as_tensor(dC, device="cuda")
+
+    def check(vals, ref_vals):
+        C = HybridSpMMFunction.apply(vals, Bt, op)
+        (gB,) = torch.autograd.grad(C, [Bt], grad_outputs=dCt)
+        Ar = sp.csr_matrix((ref_vals, A.indices, A.indptr), shape=A.shape)
+        assert S.rel_fro(C.detach().cpu().numpy(), S.spmm_fp64(Ar, B)) <= 1e-5
+        assert S.rel_fro(gB.cpu().numpy(), S.spmm_fp64(Ar.T.tocsr(), dC)) <= 1e-5
+
+    v1 = rng.uniform(-1, 1, A.nnz).astype(np.float32)
+    vals1 = torch.as_tensor(v1, device="cuda")
+    check(vals1, v1.astype(np.float64))
+    del vals1
+    v2 = rng.uniform(-1, 1, A.nnz).astype(np.float32)
+    vals2 = torch.as_tensor(v2, device="cuda")
+    check(vals2, v2.astype(np.float64))
+    with torch.no_grad():
+        vals2.mul_(-2.0)
+    check(vals2, -2.0 * v2.astype(np.float64))
+
+
 def test_gradcheck_induced_subgraph_fp64_central_differences():
     """512-node induced subgraph of the GCN-style graph: the analytic
     gradient of L = <dC, A(vals) @ B> from the GPU backward equals FP64

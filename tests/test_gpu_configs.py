@@ -99,9 +99,118 @@ def test_config4_sddmm_mask_bf16(sddmm_config):
     assert S.rel_fro(out, ref) <= 1e-5
 
 
-def test_config5_gcn_layer_full_graph():
+def test_config2_hybrid_graph():
+    """The bench graph (169,343 nodes, 1.17M nonzeros, N = 128): forward and
+    dB within the bf16 tolerance, dvals (fp32) on every nonzero."""
+    w = W.graph()
+    op, C, dB, dv = _spmm_products(w, D.TC_BF16)
+    A = op.A
+    assert S.rel_fro(C, S.spmm_fp64(A, w.dense["B"])) <= 1e-2
+    assert S.rel_fro(dB, S.spmm_fp64(A.T.tocsr(), w.dense["dC"])) <= 1e-2
+    assert S.rel_fro(dv, S.sddmm_fp64(A, w.dense["dC"], w.dense["B"])) <= 1e-5
+    assert op.device_layout.stats()["tc_ksteps"] > 0 and op.device_layout.stats()["ell_slots"] > 0
+
+
+@pytest.fixture(scope="module")
+def gcn_graph_ops():
+    """The GCN graph (232,965 nodes, ~11.4M nonzeros) and its operators for
+    the two layer widths, 128 and 41 (one plan each)."""
     w = W.gcn(128)
     assert w.A.nnz > 11_000_000
-    op = _check_spmm(w, D.TC_BF16, 1e-2)
+    op128 = SpmmOperator(w.A, 128, PlanConfig(tc_mode=D.TC_BF16))
+    op41 = SpmmOperator(w.A, 41, PlanConfig(tc_mode=D.TC_BF16))
+    return w, op128, op41
+
+
+def _check_op(op, B_np, dC_np, tol):
+    B = torch.as_tensor(B_np, device="cuda")
+    dC = torch.as_tensor(dC_np, device="cuda")
+    C = op(B).cpu().numpy()
+    opT, _ = op.transposed
+    dB = opT(dC).cpu().numpy()
+    dv = op.dvals(dC, B).cpu().numpy()
+    torch.cuda.synchronize()
+    assert op.handle.error_flag() == 0 and opT.handle.error_flag() == 0
+    A = op.A
+    assert S.rel_fro(C, S.spmm_fp64(A, B_np)) <= tol
+    assert S.rel_fro(dB, S.spmm_fp64(A.T.tocsr(), dC_np)) <= tol
+    ids, ref = W.sddmm_fp64_sample(A, dC_np, B_np)
+    assert S.rel_fro(dv[ids], ref) <= 1e-5
+
+
+def test_config5_gcn_layer_full_graph(gcn_graph_ops):
+    w, op128, _ = gcn_graph_ops
+    _check_op(op128, w.dense["B"], w.dense["dC"], 1e-2)
     # symmetric pattern: the transposed operator reuses the forward plan
-    assert op.transposed[0].plan is op.plan
+    assert op128.transposed[0].plan is op128.plan
+
+
+def test_config5_gcn_layer2_N41(gcn_graph_ops):
+    """The second layer's width, 41 features (not a multiple of the 128-feature
+    tensor-core slice nor of the 16-byte vector): operands with a padded
+    row stride of 44."""
+    w, _, op41 = gcn_graph_ops
+    rng = np.random.default_rng(41)
+    n = w.A.shape[0]
+    B = rng.standard_normal((n, 41)).astype(np.float32)
+    dC = rng.standard_normal((n, 41)).astype(np.float32)
+    _check_op(op41, B, dC, 1e-2)
+
+
+def _gcn2_fp64(A, X, W1, W2, G):
+    """float64 forward and gradients of L = <G, A relu(A X W1) W2> with respect
+    to W1, W2 and A's values (one value set shared by both layers)."""
+    A = A.astype(np.float64)
+    XW1 = X @ W1
+    H1 = A @ XW1
+    Z1 = np.maximum(H1, 0.0)
+    XW2 = Z1 @ W2
+    H2 = A @ XW2
+    AT = A.T.tocsr()
+    dXW2 = AT @ G
+    dW2 = Z1.T @ dXW2
+    dH1 = (dXW2 @ W2.T) * (H1 > 0)
+    dXW1 = AT @ dH1
+    dW1 = X.T @ dXW1
+    rows = np.repeat(np.arange(A.shape[0]), np.diff(A.indptr))
+    dvals = (np.einsum("ij,ij->i", G[rows], XW2[A.indices]) + np.einsum("ij,ij->i", dH1[rows], XW1[A.indices]))
+    return H2, dW1, dW2, dvals
+
+
+@pytest.mark.parametrize("where", ["induced_512", "full_graph"])
+def test_config5_two_layer_gcn_step(gcn_graph_ops, where):
+    """The two-layer GCN step, 602 -> 128 -> 41, through HybridSpMMFunction:
+    the output and the gradients of W1, W2 and of the shared edge values
+    against float64, on the 512-node induced subgraph (fp32 path, 1e-5) and
+    on the full graph (bf16 tensor tiles, 1e-2)."""
+    from stile_gb300.gcn import TwoLayerGCN
+    w, op128, op41 = gcn_graph_ops
+    if where == "induced_512":
+        # 512 consecutive nodes: their planted 16x16 communities stay inside
+        # the induced subgraph (920 edges), random nodes keep almost none
+        nodes = np.arange(100_000, 100_512)
+        A = w.A[nodes][:, nodes].tocsr()
+        A.sort_indices()
+        assert A.nnz > 0
+        cfg = PlanConfig(tc_mode=D.TC_SPLIT_BF16)
+        ops, tol = None, 1e-5
+    else:
+        A, cfg, ops, tol = op128.A, None, (op128, op41), 1e-2
+    n = A.shape[0]
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((n, 602)).astype(np.float32)
+    W1 = (rng.standard_normal((602, 128)) / np.sqrt(602)).astype(np.float32)
+    W2 = (rng.standard_normal((128, 41)) / np.sqrt(128)).astype(np.float32)
+    G = rng.standard_normal((n, 41)).astype(np.float32)
+    model = TwoLayerGCN(A, torch.as_tensor(W1, device="cuda"), torch.as_tensor(W2, device="cuda"), cfg, ops=ops)
+    Xt = torch.as_tensor(X, device="cuda")
+    H2 = model(Xt)
+    gW1, gW2, gv = torch.autograd.grad(H2, [model.lin1.weight, model.lin2.weight, model.vals],
+                                       grad_outputs=torch.as_tensor(G, device="cuda"))
+    torch.cuda.synchronize()
+    rH2, rW1, rW2, rdv = _gcn2_fp64(A, X.astype(np.float64), W1.astype(np.float64), W2.astype(np.float64),
+                                    G.astype(np.float64))
+    assert S.rel_fro(H2.detach().cpu().numpy(), rH2) <= tol
+    assert S.rel_fro(gW2.cpu().numpy(), rW2) <= tol
+    assert S.rel_fro(gW1.cpu().numpy(), rW1) <= tol
+    assert S.rel_fro(gv.cpu().numpy(), rdv) <= tol
