@@ -358,13 +358,13 @@ class SparseStep:
     a symmetric pattern reuses the forward plan), device-resident operands
     and outputs, the plain CSR comparator."""
 
-    def __init__(self, A, layers, dev, tc_mode):
+    def __init__(self, A, layers, dev, tc_mode, cache_dir=None):
         from stile_gb300.api import PlanConfig, SpmmOperator
         self.A, self.dev = A, dev
         t0 = time.time()
         self.ops = []
         for B, _ in layers:
-            op = SpmmOperator(A, B.shape[1], PlanConfig(tc_mode=tc_mode))
+            op = SpmmOperator(A, B.shape[1], PlanConfig(tc_mode=tc_mode, cache_dir=cache_dir))
             op.transposed
             self.ops.append(op)
         self.plan_s = time.time() - t0
@@ -459,14 +459,14 @@ def make_timer(flush):
     return timed
 
 
-def run_secondary_graph(dev, tc_mode, steps, timed, peak):
+def run_secondary_graph(dev, tc_mode, steps, timed, peak, cache_dir=None):
     """The 169,343-node graph (one layer, N = 128): step, forward and the
     plain CSR step, accuracy, forward roofline, and the plan of the learned
     cost model against the analytic one."""
     import oracle.semantics as S
     from stile_gb300.api import PlanConfig, SpmmOperator
     A, layers = make_graph_workload()
-    st = SparseStep(A, layers, dev, tc_mode)
+    st = SparseStep(A, layers, dev, tc_mode, cache_dir)
     st.step()
     import torch
     torch.cuda.synchronize()
@@ -492,7 +492,7 @@ def run_secondary_graph(dev, tc_mode, steps, timed, peak):
     # the learned cost model, measured by the forward time of the plan it chooses
     try:
         t0 = time.time()
-        op_l = SpmmOperator(A, layers[0][0].shape[1], PlanConfig(tc_mode=tc_mode, learned=True))
+        op_l = SpmmOperator(A, layers[0][0].shape[1], PlanConfig(tc_mode=tc_mode, learned=True, cache_dir=cache_dir))
         t_l = time.time() - t0
         Cl = torch.empty_like(st.C[0])
         op = st.ops[0]
@@ -561,7 +561,7 @@ def run_gpu(args):
     A, layers = make_gcn_workload()
     log(f"[bench] workload {A.shape} nnz={A.nnz} ({time.time() - t0:.1f}s)")
     tc_mode = D.TC_BF16
-    st = SparseStep(A, layers, dev, tc_mode)
+    st = SparseStep(A, layers, dev, tc_mode, args.plan_cache)
     log(f"[bench] plans {st.plan_summary()} ({st.plan_s:.1f}s)")
     flops = st.flops
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -670,7 +670,7 @@ def run_gpu(args):
     d2h = sum(A.shape[0] * B.shape[1] * 4 + A.shape[1] * B.shape[1] * 4 for B, _ in layers) + A.nnz * 4
 
     train_ms = gcn_training_step_ms(st, dev, timed, args.steps)
-    secondary = run_secondary_graph(dev, tc_mode, args.steps, timed, peak) if rank == 0 else None
+    secondary = run_secondary_graph(dev, tc_mode, args.steps, timed, peak, args.plan_cache) if rank == 0 else None
 
     cpu = run_cpu_baseline(A, layers, flops) if (rank == 0 and world == 1) else None
 
@@ -900,6 +900,9 @@ def main():
                     help="gcn2 (the headline line: the two-layer GCN step) or one of the configurations: "
                          "plain, plain_min10, graph, pruned, pruned_t, sddmm, gcn, gcn_41 (one JSON line of "
                          "measurements each)")
+    ap.add_argument("--plan-cache", default=None,
+                    help="directory of the on-disk plan cache (searched plans are stored and reloaded); "
+                         "default: search every run")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
