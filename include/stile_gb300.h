@@ -52,12 +52,10 @@ extern "C" {
 #define STILE_F32 0
 #define STILE_BF16 1
 #define STILE_F16 2
-#define STILE_FP8E4M3 3
 /* tensor-tile precision modes */
 #define STILE_TC_BF16 1        /* A, B rounded to bf16, fp32 accumulate */
 #define STILE_TC_F16 2         /* A, B rounded to fp16, fp32 accumulate */
 #define STILE_TC_SPLIT_BF16 4  /* hi+lo bf16 split of A and B, 4 products */
-#define STILE_TC_FP8 3         /* A e4m3 with per-tile scale, B e4m3, fp32 acc. */
 
 
 /*
@@ -89,7 +87,6 @@ typedef struct StileSpmmPlanHost {
   const int32_t* tc_cols;        /* [tc_n_ksteps * 16] */
   const void* tc_vals;           /* [tc_n_ksteps * tc_kstep_bytes] */
   int32_t tc_kstep_bytes;        /* 512 (bf16/fp16), 1024 (split) */
-  const float* tc_scales;        /* [tc_n_ksteps] fp8 per-tile scale, else NULL */
   const int32_t* tc_nnz_id;      /* [tc_n_ksteps * 256] row-major (n,k); -1: empty */
   int32_t ell_n_items, ell_n_rows, ell_n_slots;
   const int32_t* ell_item_row0;  /* [ell_n_items + 1] */

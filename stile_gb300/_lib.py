@@ -82,7 +82,7 @@ class SpmmPlanHost(ctypes.Structure):
         ("tc_n_items", ctypes.c_int32), ("tc_n_ksteps", ctypes.c_int32),
         ("tc_item_kbeg", c_i32p), ("tc_item_flags", c_i32p), ("tc_out_rows", c_i32p),
         ("tc_cols", c_i32p), ("tc_vals", ctypes.c_void_p), ("tc_kstep_bytes", ctypes.c_int32),
-        ("tc_scales", c_f32p), ("tc_nnz_id", c_i32p),
+        ("tc_nnz_id", c_i32p),
         ("ell_n_items", ctypes.c_int32), ("ell_n_rows", ctypes.c_int32), ("ell_n_slots", ctypes.c_int32),
         ("ell_item_row0", c_i32p), ("ell_item_K", c_i32p), ("ell_item_slot0", c_i32p),
         ("ell_item_flags", c_i32p), ("ell_out_row", c_i32p), ("ell_row_len", c_i32p),

@@ -458,7 +458,6 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   a.tc_out_rows = (const int*)P(i_orows);
   a.tc_cols = (const int*)P(i_cols);
   a.tc_vals = P(i_vals);
-  a.tc_scales = nullptr;
   a.tc_nnz_id = h->tc_nnz_id ? (const int*)P(i_tnid) : nullptr;
   a.ell_n_groups = (int)e_gptr.size() - 1;
   a.ell_n_pos = n_pos;

@@ -157,15 +157,6 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes)
                : "memory");
 }
-// Bulk asynchronous global -> shared copy (no tensor map): both addresses
-// 16-byte aligned, bytes a multiple of 16; completion is signalled as
-// transaction bytes on the mbarrier at `bar`.
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-      "l"(src), "r"(bytes), "r"(bar)
-      : "memory");
-}
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;" ::: "memory");
 }
@@ -286,17 +277,6 @@ __device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t adesc, uint6
       : "memory");
 }
 
-// D[tmem] (+)= A * B, kind::f8f6f4 (e4m3 inputs, fp32 accumulate)
-__device__ __forceinline__ void umma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
-                                        uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
 // arrive on an mbarrier once all previously issued tcgen05 ops of this thread finish
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile(
@@ -334,8 +314,8 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;
 }
 
-// Instruction descriptor for kind::f16 / kind::f8f6f4 with fp32 accumulate.
-// a_fmt/b_fmt: f16 kinds -> 0 = f16, 1 = bf16; f8f6f4 -> 0 = e4m3.
+// Instruction descriptor for kind::f16 / kind::tf32 with fp32 accumulate.
+// a_fmt/b_fmt: kind::f16 -> 0 = f16, 1 = bf16; kind::tf32 -> 2.
 // a_mn_major / b_mn_major: 1 = MN-major operand, 0 = K-major.
 __host__ __device__ constexpr uint32_t make_idesc(uint32_t a_fmt, uint32_t b_fmt,
                                                   uint32_t a_mn_major, uint32_t b_mn_major,

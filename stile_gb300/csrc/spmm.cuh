@@ -46,7 +46,6 @@ struct SpmmArgs {
   const int* tc_out_rows;
   const int* tc_cols;
   const void* tc_vals;
-  const float* tc_scales;
   const int* tc_nnz_id;
   // ELL tiles, compacted at upload into a stream of live entries in row
   // order, cut into groups of at most kSegNnz entries at row boundaries

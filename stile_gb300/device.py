@@ -30,7 +30,7 @@ import scipy.sparse as sp
 from .emit import emit_sddmm_reference, emit_spmm_reference
 from .plan import ELL, ONE_D, TC, TC_SDDMM
 
-TC_BF16, TC_F16, TC_FP8, TC_SPLIT_BF16 = 1, 2, 3, 4
+TC_BF16, TC_F16, TC_SPLIT_BF16 = 1, 2, 4
 
 
 class ValueIndex:

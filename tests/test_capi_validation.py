@@ -84,7 +84,7 @@ SPMM_CASES = [
     ("negative_shape", None, lambda h: setattr(h, "M", -1), INVALID, "negative shape"),
     ("negative_count", None, lambda h: setattr(h, "ell_n_slots", -3), INVALID, "negative count"),
     ("unknown_tc_mode", None, lambda h: setattr(h, "tc_mode", 99), UNSUPPORTED, "mode not supported"),
-    ("fp8_mode_without_build", None, lambda h: setattr(h, "tc_mode", 3), UNSUPPORTED, "mode not supported"),
+    ("mode_3_not_built", None, lambda h: setattr(h, "tc_mode", 3), UNSUPPORTED, "mode not supported"),
     ("kstep_bytes", None, lambda h: setattr(h, "tc_kstep_bytes", 1024), INVALID, "tc_kstep_bytes"),
     ("missing_tc_array", None, lambda h: setattr(h, "tc_cols", None), INVALID, "missing tensor-tile array"),
     ("tc_kbeg_span", _set("tc_item_kbeg", _poke(-1, 0)), None, INVALID, "does not span the k-steps"),
