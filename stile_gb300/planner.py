@@ -1027,8 +1027,19 @@ class SpmmPlanner:
                 if best_cost == float("inf"):
                     break
                 ts, poses, atomic = key
-                target = best_cost * (1 + self.max_avg_cost_diff)
+                # The reference widens by best * (1 + diff) here
+                # (my_branch_and_bound.py:300).  A whole-row option whose
+                # withdraw cost is negative (the row's earlier atomic tiles
+                # cost more than owning the row) then gets a window below
+                # the best itself, the local search returns nothing and the
+                # block never changes: the reference's loop does not end.
+                # The sign-aware window of its main loop (:1563-1568) keeps
+                # the best inside and changes no plan that terminates.
+                target = best_cost * (1 + self.max_avg_cost_diff) if best_cost >= 0 else \
+                    best_cost * (1 - self.max_avg_cost_diff)
                 good = self._local_tc_block(b, counts, ts, target, unit[ts][0], unit[ts][1], row_sel)
+                if not good:
+                    break  # nothing selected: the later passes cover the rest
                 if good and not good[0].atomic:
                     row_sel = good
                     ref = start_uncovered

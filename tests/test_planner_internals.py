@@ -52,3 +52,32 @@ def test_ell_folded_rows(seed, mbs):
     assert np.array_equal(np.sort(-rn[op.i_perm], kind="stable"), -rn[op.i_perm])
     for r in np.unique(rows):
         assert np.array_equal(op.cols[rows == r], np.sort(pat.indices[ids[pat.row_of[ids] == r]]))
+
+
+def test_block_pass_terminates_when_a_whole_row_costs_less_than_its_tiles():
+    """A 16-row block whose earlier atomic tiles cost more than owning the
+    whole row makes the whole-row option's (withdraw) cost negative.  The
+    reference's per-block window best * 1.2 then lies below the best and its
+    block loop never ends; the planner applies the sign-aware window of the
+    reference's main loop, so the search ends and covers every nonzero."""
+    import signal
+
+    from stile_gb300 import synthetic as syn
+    from stile_gb300.cost_model import gb300_model
+    from stile_gb300.planner import search_spmm
+
+    A = syn.community_graph(n=2048, target_nnz=30000, seed=13, max_deg=512)
+
+    def _timeout(*_):
+        raise TimeoutError("format search did not end")
+    old = signal.signal(signal.SIGALRM, _timeout)
+    signal.alarm(60)
+    try:
+        plan = search_spmm(A, 32, cost=gb300_model(), max_avg_cost_diff=0.2)
+    finally:
+        signal.alarm(0)
+        signal.signal(signal.SIGALRM, old)
+    from stile_gb300 import device as D
+    from stile_gb300.ops import _tiles_cover_every_nonzero
+    dev = D.build_spmm_device(plan.tiles, A, N=32, tc_mode=D.TC_SPLIT_BF16)
+    assert _tiles_cover_every_nonzero(dev)
