@@ -399,6 +399,16 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
       }
     }
   const long ndv = (long)dv_id.size();
+  // runs of one row, cut at kRunGroup entries (the row-run kernel's groups)
+  std::vector<int32_t> dv_gptr{0}, dv_grow;
+  for (long t = 0; t < ndv; ++t) {
+    const bool cut = t + 1 == ndv || dv_row[t + 1] != dv_row[t] || t + 1 - dv_gptr.back() == stile::kRunGroup;
+    if (cut) {
+      dv_grow.push_back(dv_row[t]);
+      dv_gptr.push_back((int32_t)(t + 1));
+    }
+  }
+  if (ndv > INT32_MAX) return fail(STILE_E_INVALID, "too many nonzeros for the value-gradient list");
 
   Arena ar;
   const long ti = h->tc_n_items, tk = h->tc_n_ksteps;
@@ -421,6 +431,8 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   size_t i_dvr = ar.add(dv_row.data(), (size_t)ndv * 4);
   size_t i_dvc = ar.add(dv_col.data(), (size_t)ndv * 4);
   size_t i_dvi = ar.add(dv_id.data(), (size_t)ndv * 4);
+  size_t i_dvgp = ar.add(dv_gptr.data(), dv_gptr.size() * 4);
+  size_t i_dvgr = ar.add(dv_grow.data(), dv_grow.size() * 4);
   size_t i_err = ar.add(nullptr, 16);
 
   auto* plan = new StileSpmmPlan();
@@ -476,6 +488,9 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   a.dv_row = (const int*)P(i_dvr);
   a.dv_col = (const int*)P(i_dvc);
   a.dv_id = (const int*)P(i_dvi);
+  a.dv_n_groups = (int)dv_grow.size();
+  a.dv_gptr = (const int*)P(i_dvgp);
+  a.dv_grow = (const int*)P(i_dvgr);
   a.tc_chunk_kbeg = (const int*)P(i_ckb);
   a.tc_chunk_nk = (const int*)P(i_ckn);
   a.tc_grid = tc_grid;

@@ -238,6 +238,168 @@ cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const in
   return e;
 }
 
+// Row-run SDDMM: the entries come in groups that share one row (runs of a
+// row-grouped list, cut at kRunGroup entries):
+//   out[outs[t]] = <X[grow[g]], Y[cols[t]]>  for t in [gptr[g], gptr[g+1]).
+// An LPR-lane group takes one run: it holds the run's X row in registers
+// (one pass: F <= 4 VEC LPR; longer rows reload their slice per batch, an
+// L1 hit) and streams the run's Y rows U at a time, each lane covering
+// 4 VEC features with VEC float4 (or one 16-byte bf16 load) per row.  The U
+// partial dot products are reduced with the transposing butterfly of the
+// entry-list kernel, so the lanes whose high bits spell an entry index hold
+// that entry's sum.  Few registers (no X gather per entry, no entry
+// records in flight) leave room for more warps per SM than the entry-list
+// kernel, and gathers grow with resident warps.
+constexpr int kRunU = 2;       // Y rows in flight per group
+constexpr int kRunBlocks = 6;  // resident 256-thread blocks per SM (register budget)
+
+// A float4 of features [f, f + 4) of a row whose stride is a multiple of 4
+// elements: loaded when f < F (the vector then lies inside the row's
+// storage), components at or past F set to zero by selects (padding may
+// hold anything, NaN included).
+__device__ __forceinline__ float4 ld4_live(const float* row, int f, int F) {
+  const int live = F - f;
+  float4 v = live > 0 ? ldg4(row + f) : make_float4(0.f, 0.f, 0.f, 0.f);
+  v.y = live > 1 ? v.y : 0.f;
+  v.z = live > 2 ? v.z : 0.f;
+  v.w = live > 3 ? v.w : 0.f;
+  return v;
+}
+
+// kOne: F <= 4 VEC LPR (one pass; the X row stays in registers).
+// kFull: F == 4 VEC LPR exactly (no masking at all).
+template <int LPR, int VEC, int U, int MINB, bool kYb, bool kOne, bool kFull>
+__global__ void __launch_bounds__(256, MINB) sddmm_run_kernel(int n_groups, const int* __restrict__ gptr,
+                                                                const int* __restrict__ grow,
+                                                                const int* __restrict__ cols,
+                                                                const int* __restrict__ outs,
+                                                                const float* __restrict__ X, long ldx,
+                                                                const void* __restrict__ Yv, long ldy,
+                                                                float* __restrict__ out, int F) {
+  static_assert(U <= LPR && (U & (U - 1)) == 0, "U must be a power of two no larger than the group");
+  static_assert(!kYb || VEC == 2, "a bf16 load covers 8 features");
+  static_assert(!kFull || kOne, "a full pass is one pass");
+  // launched dependent on the previous kernel: wait for its results (X may
+  // be one of them), then let the next dependent kernel launch
+  griddep_wait();
+  griddep_launch_dependents();
+  using TY = typename std::conditional<kYb, uint16_t, float>::type;
+  const TY* __restrict__ Y = static_cast<const TY*>(Yv);
+  const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
+  const unsigned gmask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
+  const long g = ((long)blockIdx.x * blockDim.x + threadIdx.x) / LPR;
+  if (g >= n_groups) return;  // the whole group leaves together
+  const int p0 = __ldg(gptr + g), p1 = __ldg(gptr + g + 1);
+  const float* __restrict__ xr = X + (long)__ldg(grow + g) * ldx;
+  constexpr int FP = 4 * VEC * LPR;  // features per pass
+  const int f0 = 4 * VEC * sl;
+  auto load_y = [&](int c, int f, float4 (&y)[VEC]) {
+    const TY* row = Y + (long)c * ldy;
+    if constexpr (kYb) {
+      bf16x8_to_f32(kFull ? ldg_u4(row + f) : ld_row8_bf16(row, f, F), y[0], y[1]);
+    } else {
+#pragma unroll
+      for (int w = 0; w < VEC; ++w) y[w] = kFull ? ldg4(row + f + 4 * w) : ld4_live(row, f + 4 * w, F);
+    }
+  };
+  float4 x1[VEC];
+  if constexpr (kOne) {
+#pragma unroll
+    for (int w = 0; w < VEC; ++w) x1[w] = kFull ? ldg4(xr + f0 + 4 * w) : ld4_live(xr, f0 + 4 * w, F);
+  }
+#pragma unroll 1
+  for (int b0 = p0; b0 < p1; b0 += U) {
+    int c[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) c[u] = __ldg(cols + min(b0 + u, p1 - 1));  // past the run: a valid row, unused
+    float s[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) s[u] = 0.f;
+    if constexpr (kOne) {
+      float4 y[U][VEC];
+#pragma unroll
+      for (int u = 0; u < U; ++u) load_y(c[u], f0, y[u]);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+#pragma unroll
+        for (int w = 0; w < VEC; ++w) s[u] += dot4(x1[w], y[u][w]);
+      }
+    } else {
+#pragma unroll 1
+      for (int fc = 0; fc < F; fc += FP) {
+        const int f = fc + f0;
+        float4 xv[VEC];
+#pragma unroll
+        for (int w = 0; w < VEC; ++w) xv[w] = ld4_live(xr, f + 4 * w, F);
+        float4 y[U][VEC];
+#pragma unroll
+        for (int u = 0; u < U; ++u) load_y(c[u], f, y[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+          for (int w = 0; w < VEC; ++w) s[u] += dot4(xv[w], y[u][w]);
+        }
+      }
+    }
+    int e = 0;
+#pragma unroll
+    for (int m = U, hw = LPR / 2; m > 1; m >>= 1, hw >>= 1) {
+      const bool up = (sl & hw) != 0;
+#pragma unroll
+      for (int i = 0; i < m / 2; ++i) {
+        const float send = up ? s[i] : s[i + m / 2];
+        const float keep = up ? s[i + m / 2] : s[i];
+        s[i] = keep + __shfl_xor_sync(gmask, send, hw);
+      }
+      if (up) e += m / 2;
+    }
+#pragma unroll
+    for (int o = LPR / (2 * U); o > 0; o >>= 1) s[0] += __shfl_xor_sync(gmask, s[0], o);
+    if ((sl & (LPR / U - 1)) == 0 && b0 + e < p1) out[__ldg(outs + b0 + e)] = s[0];
+  }
+}
+
+template <int L, bool kYb>
+static cudaError_t launch_runs_t(int grid, bool one, bool full, cudaStream_t st, int n_groups, const int* gptr,
+                                 const int* grow, const int* cols, const int* outs, const float* X, long ldx,
+                                 const void* Y, long ldy, float* out, int F) {
+  if (full)
+    return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, true, true>, dim3((unsigned)grid),
+                            dim3(256), 0, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+  if (one)
+    return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, true, false>, dim3((unsigned)grid),
+                            dim3(256), 0, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+  return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, false, false>, dim3((unsigned)grid),
+                          dim3(256), 0, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+}
+
+cudaError_t launch_sddmm_runs(int n_groups, const int* gptr, const int* grow, const int* cols, const int* outs,
+                              const float* X, long ldx, const void* Y, bool y_bf16, long ldy, float* out, int F,
+                              cudaStream_t st) {
+  if (n_groups <= 0) return cudaSuccess;
+  // lanes per run: 8 features per lane (two float4, or one bf16 load);
+  // 128 features per pass at most (longer rows take several passes)
+  int lpr = 16;
+  if (F < 128) {
+    const int lanes = (F + 7) / 8;
+    lpr = 4;
+    while (lpr < lanes) lpr <<= 1;
+  }
+  const bool one = F <= 8 * lpr, full = F == 8 * lpr;
+  const int grid = (int)(((long)n_groups * lpr + 255) / 256);
+  switch (lpr) {
+    case 4:
+      return y_bf16 ? launch_runs_t<4, true>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F)
+                    : launch_runs_t<4, false>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+    case 8:
+      return y_bf16 ? launch_runs_t<8, true>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F)
+                    : launch_runs_t<8, false>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+    default:
+      return y_bf16 ? launch_runs_t<16, true>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F)
+                    : launch_runs_t<16, false>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+  }
+}
+
 constexpr int kChunk = 128;
 constexpr int kPadRow = kChunk + 4;
 

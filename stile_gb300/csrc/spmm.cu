@@ -1053,9 +1053,11 @@ cudaError_t launch_ell(const SpmmArgs& args, cudaStream_t st) {
   return dispatch_lpr<EllLaunch>(lpr_for(p.N), p, st);
 }
 
+// dvals[t] = <dY[row(t)], B[col(t)]> over the plan's entry list, as runs of
+// one row (the row-run SDDMM kernel holds the dY row and gathers B rows)
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {
-  return launch_sddmm_list(p.dv_n, p.dv_row, p.dv_col, p.dv_id, dY, false, lddy, p.B, p.b_bf16 != 0, p.ldb, dvals,
-                           p.N, st);
+  return launch_sddmm_runs(p.dv_n_groups, p.dv_gptr, p.dv_grow, p.dv_col, p.dv_id, dY, lddy, p.B, p.b_bf16 != 0,
+                           p.ldb, dvals, p.N, st);
 }
 
 }  // namespace stile

@@ -64,6 +64,11 @@ struct SpmmArgs {
   const int* dv_row;
   const int* dv_col;
   const int* dv_id;
+  // the same list cut into runs of one row (at most kRunGroup entries):
+  // run g is entries [dv_gptr[g], dv_gptr[g + 1]) of row dv_grow[g]
+  int dv_n_groups;
+  const int* dv_gptr;
+  const int* dv_grow;
   // device error flag (bounded waits that gave up)
   int* err_flag;
   // polls of every pipeline wait of the tensor-core kernel before it gives
@@ -126,6 +131,11 @@ cudaError_t launch_csr_row_softmax(int M, const int* indptr, long nnz, const flo
                                    int batch, cudaStream_t st);
 cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const int* outs, const void* X, bool x_bf16,
                               long ldx, const void* Y, bool y_bf16, long ldy, float* out, int F, cudaStream_t st);
+// row-run SDDMM: group g is entries [gptr[g], gptr[g+1]) of row grow[g]
+constexpr int kRunGroup = 64;  // entries per run group at most
+cudaError_t launch_sddmm_runs(int n_groups, const int* gptr, const int* grow, const int* cols, const int* outs,
+                              const float* X, long ldx, const void* Y, bool y_bf16, long ldy, float* out, int F,
+                              cudaStream_t st);
 
 cudaError_t launch_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
                               uint32_t idesc, uint32_t kind, float* out, int* err, cudaStream_t st);
