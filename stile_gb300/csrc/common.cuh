@@ -32,6 +32,19 @@ __device__ __forceinline__ float4 ld_row4(const float* row, int f, int N) {
   return v;
 }
 
+// A float4 of features [f, f + 4) of a row whose stride is a multiple of 4
+// elements: loaded when f < N (the vector then lies inside the row's
+// storage), components at or past N set to zero by selects (padding may
+// hold anything, NaN included).
+__device__ __forceinline__ float4 ld4_live(const float* row, int f, int N) {
+  const int live = N - f;
+  float4 v = live > 0 ? ldg4(row + f) : make_float4(0.f, 0.f, 0.f, 0.f);
+  v.y = live > 1 ? v.y : 0.f;
+  v.z = live > 2 ? v.z : 0.f;
+  v.w = live > 3 ? v.w : 0.f;
+  return v;
+}
+
 __device__ __forceinline__ void st_row4(float* row, int f, int N, float4 v) {
   if (f + 3 < N) {
     *reinterpret_cast<float4*>(row + f) = v;

@@ -253,19 +253,6 @@ cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const in
 constexpr int kRunU = 2;       // Y rows in flight per group
 constexpr int kRunBlocks = 6;  // resident 256-thread blocks per SM (register budget)
 
-// A float4 of features [f, f + 4) of a row whose stride is a multiple of 4
-// elements: loaded when f < F (the vector then lies inside the row's
-// storage), components at or past F set to zero by selects (padding may
-// hold anything, NaN included).
-__device__ __forceinline__ float4 ld4_live(const float* row, int f, int F) {
-  const int live = F - f;
-  float4 v = live > 0 ? ldg4(row + f) : make_float4(0.f, 0.f, 0.f, 0.f);
-  v.y = live > 1 ? v.y : 0.f;
-  v.z = live > 2 ? v.z : 0.f;
-  v.w = live > 3 ? v.w : 0.f;
-  return v;
-}
-
 // kOne: F <= 4 VEC LPR (one pass; the X row stays in registers).
 // kFull: F == 4 VEC LPR exactly (no masking at all).
 template <int LPR, int VEC, int U, int MINB, bool kYb, bool kOne, bool kFull>

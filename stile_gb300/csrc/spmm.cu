@@ -537,7 +537,8 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
 // VEC = 2 two sub-groups share every warp-wide shuffle and branch, so the
 // instructions per gathered byte halve; no gather waits on a metadata load,
 // and few registers leave room for many warps per SM.
-// kFull: N % (4 * VEC * LPR) == 0, every lane's features are in range.
+// kFull: N % (4 * VEC * LPR) == 0, every lane's features are in range
+// (otherwise each float4 is masked by the row's width N).
 // kOff32: every B row offset col * ldb fits in 32 bits.
 // kSpanY: blockIdx.y takes features [y span, (y + 1) span) (a wide B over
 // few groups; span = p.ell_fc_span, a multiple of the pass width).
@@ -545,7 +546,6 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
 template <int LPR, int VEC, bool kFull, bool kOff32, bool kSpanY = false, bool kHeads = false>
 __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   constexpr int kBatch = 4 / VEC;  // entries per batch: 4 float4 in flight per lane
-  static_assert(VEC == 1 || kFull, "wide lanes need full feature slices");
   // Launched dependent on the previous kernel.  When that is the zero-rows
   // kernel (p.ell_lazy_wait), only the atomic adds (into rows it zeroes)
   // wait for it, and every thread waits before it exits, so that this
@@ -591,8 +591,10 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
 #pragma unroll
             for (int w = 0; w < VEC; ++w) bv[u][w] = ldg4(row + 4 * w);
           } else {
-            bv[u][0] = b0 + u < n ? ld_row4(p.B + head * p.b_head_stride + (long)c * p.ldb, f, N)
-                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+            // features past N (row padding, any bits) read as zero
+            const float* row = p.B + head * p.b_head_stride + (long)c * p.ldb;
+#pragma unroll
+            for (int w = 0; w < VEC; ++w) bv[u][w] = ld4_live(row, f + 4 * w, N);
           }
         }
 #pragma unroll
@@ -1007,6 +1009,25 @@ struct EllLaunch {
   }
 };
 
+// Narrow fp32 B (N < 128): LPR-lane sub-groups of 8 features per lane (two
+// float4), LPR the power of two covering N, so a 41-wide row takes 6 of 8
+// lanes instead of 11 of 16 single-float4 lanes.
+template <int LPR>
+struct EllNarrowLaunch {
+  static cudaError_t run(SpmmArgs p, cudaStream_t st) {
+    const dim3 grid = ell_grid(p, 256 / LPR, 8 * LPR);
+    const bool full = p.N % (8 * LPR) == 0;
+    if (grid.z > 1)
+      return full ? launch_dependent(spmm_ell_seg_kernel<LPR, 2, true, false, true, true>, grid, dim3(256), 0, st, p)
+                  : launch_dependent(spmm_ell_seg_kernel<LPR, 2, false, false, true, true>, grid, dim3(256), 0, st, p);
+    if (grid.y > 1)
+      return full ? launch_dependent(spmm_ell_seg_kernel<LPR, 2, true, false, true>, grid, dim3(256), 0, st, p)
+                  : launch_dependent(spmm_ell_seg_kernel<LPR, 2, false, false, true>, grid, dim3(256), 0, st, p);
+    return full ? launch_dependent(spmm_ell_seg_kernel<LPR, 2, true, false>, grid, dim3(256), 0, st, p)
+                : launch_dependent(spmm_ell_seg_kernel<LPR, 2, false, false>, grid, dim3(256), 0, st, p);
+  }
+};
+
 template <int LPR>
 struct EllBf16Launch {
   static cudaError_t run(SpmmArgs p, cudaStream_t st) {
@@ -1049,6 +1070,11 @@ cudaError_t launch_ell(const SpmmArgs& args, cudaStream_t st) {
       return launch_dependent(spmm_ell_seg_kernel<16, 2, true, false, true>, grid, dim3(256), 0, st, p);
     else if (off32) return launch_dependent(spmm_ell_seg_kernel<16, 2, true, true>, grid, dim3(256), 0, st, p);
     return launch_dependent(spmm_ell_seg_kernel<16, 2, true, false>, grid, dim3(256), 0, st, p);
+  }
+  if (p.N < 128) {
+    int lpr = 4;
+    while (lpr < (p.N + 7) / 8) lpr <<= 1;
+    return dispatch_lpr<EllNarrowLaunch>(lpr, p, st);
   }
   return dispatch_lpr<EllLaunch>(lpr_for(p.N), p, st);
 }

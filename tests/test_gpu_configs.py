@@ -11,7 +11,7 @@ import torch
 import oracle.semantics as S
 from stile_gb300 import device as D
 from stile_gb300 import workloads as W
-from stile_gb300.api import PlanConfig, SddmmOperator, SpmmOperator
+from stile_gb300.api import HybridSpMMFunction, PlanConfig, SddmmOperator, SpmmOperator
 
 pytestmark = pytest.mark.gpu
 
@@ -157,19 +157,22 @@ def test_config5_gcn_layer2_N41(gcn_graph_ops):
     _check_op(op41, B, dC, 1e-2)
 
 
-def _gcn2_fp64(A, X, W1, W2, G):
+def _gcn2_fp64(A, X, W1, W2, G, mask):
     """float64 forward and gradients of L = <G, A relu(A X W1) W2> with respect
-    to W1, W2 and A's values (one value set shared by both layers)."""
+    to W1, W2 and A's values (one value set shared by both layers).  The ReLU
+    mask is given (the GPU's H1 > 0): an entry of H1 within rounding of zero
+    may change sign, and its gradient then differs by the whole value, which
+    says nothing about the products' accuracy."""
     A = A.astype(np.float64)
     XW1 = X @ W1
     H1 = A @ XW1
-    Z1 = np.maximum(H1, 0.0)
+    Z1 = np.where(mask, H1, 0.0)
     XW2 = Z1 @ W2
     H2 = A @ XW2
     AT = A.T.tocsr()
     dXW2 = AT @ G
     dW2 = Z1.T @ dXW2
-    dH1 = (dXW2 @ W2.T) * (H1 > 0)
+    dH1 = (dXW2 @ W2.T) * mask
     dXW1 = AT @ dH1
     dW1 = X.T @ dXW1
     rows = np.repeat(np.arange(A.shape[0]), np.diff(A.indptr))
@@ -204,12 +207,15 @@ def test_config5_two_layer_gcn_step(gcn_graph_ops, where):
     G = rng.standard_normal((n, 41)).astype(np.float32)
     model = TwoLayerGCN(A, torch.as_tensor(W1, device="cuda"), torch.as_tensor(W2, device="cuda"), cfg, ops=ops)
     Xt = torch.as_tensor(X, device="cuda")
-    H2 = model(Xt)
+    # the model's forward, step by step so that H1 (its ReLU mask) is seen
+    H1 = HybridSpMMFunction.apply(model.vals, model.lin1(Xt), model.op1)
+    H2 = HybridSpMMFunction.apply(model.vals, model.lin2(torch.relu(H1)), model.op2)
     gW1, gW2, gv = torch.autograd.grad(H2, [model.lin1.weight, model.lin2.weight, model.vals],
                                        grad_outputs=torch.as_tensor(G, device="cuda"))
     torch.cuda.synchronize()
+    mask = H1.detach().cpu().numpy() > 0
     rH2, rW1, rW2, rdv = _gcn2_fp64(A, X.astype(np.float64), W1.astype(np.float64), W2.astype(np.float64),
-                                    G.astype(np.float64))
+                                    G.astype(np.float64), mask)
     assert S.rel_fro(H2.detach().cpu().numpy(), rH2) <= tol
     assert S.rel_fro(gW2.cpu().numpy(), rW2) <= tol
     assert S.rel_fro(gW1.cpu().numpy(), rW1) <= tol
