@@ -6,8 +6,8 @@ exponent 1.9, ~11.4M nonzeros, planted 16x16 communities, values 1/deg) and
 the sparse products of a two-layer graph convolution, 602 -> 128 -> 41, with
 the dense operands synthetic N(0,1):
     layer 1  C1 = A @ B1 (N = 128)          layer 2  C2 = A @ B2 (N = 41)
-    backward dvals_l = <dC_l[row], B_l[col]> over the forward tiles
-             dB_l = A^T @ dC_l (transposed plan)      for l = 2, 1
+    backward dB_l = A^T @ dC_l (transposed plan) and, from the same dC rows,
+             dvals_l = <dC_l[row], B_l[col]>           for l = 2, 1
 FLOPs per step = 3 * 2 * nnz * (128 + 41).  The dense GEMMs of the GCN
 (X W1, Z1 W2) are cuBLAS work outside the metric; the line times the whole
 training step of the model for context (``gcn_training_step``).  The
@@ -384,10 +384,9 @@ class SparseStep:
                 ev[1].record()
 
     def backward(self):
+        # dB_l and dvals_l from one pass over the transposed plan's tiles
         for i in reversed(range(len(self.ops))):
-            op = self.ops[i]
-            self.dv[i] = op.dvals(self.dC[i], self.B[i])
-            op.transposed[0](self.dC[i], out=self.dB[i])
+            _, self.dv[i] = self.ops[i].backward(self.dC[i], self.B[i], self.dB[i])
 
     def step(self, ev=None):
         self.forward(ev)
@@ -772,12 +771,10 @@ def run_config(args):
 
         def step():
             op(B, out=C)
-            op.dvals(dC, B)
-            opT(dC, out=dB)
+            op.backward(dC, B, dB)   # dB and dvals from one pass over A^T's tiles
 
         op(B, out=C)
-        opT(dC, out=dB)
-        dv = op.dvals(dC, B)
+        _, dv = op.backward(dC, B, dB)
         torch.cuda.synchronize()
         ids, ref = W.sddmm_fp64_sample(A, dC_np, B_np)
         out["accuracy"] = {**errors("C", C.cpu().numpy(), S.spmm_fp64(A, B_np)),

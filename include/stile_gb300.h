@@ -262,6 +262,24 @@ int stile_csr_spmm_run_noalloc(int32_t M, int64_t nnz, const int32_t* indptr,
                                const float* B, int64_t ldb, float* C, int64_t ldc,
                                int32_t N, void* stream);
 
+/*
+ * Fused backward of C = A @ B (no counterpart in the reference, like
+ * stile_spmm_dvals).  planT is the plan of A^T (its own pattern and tiles);
+ * stile_spmm_plan_set_transpose_ids tells it, once, the forward's numbering:
+ * perm[t] (device, nnz entries) is the nonzero of A that nonzero t of A^T
+ * (CSR order of A^T) is.  Then
+ *   dB[K, N]  = A^T @ dC[M, N]             (fp32, fully written)
+ *   dvals[s]  = <dC[row(s)], B[col(s)]>    for every nonzero s of A
+ * in one pass over A^T's row tiles: each dC row gathered for dB also gives
+ * the value gradients of its entries (B's row is held per row run); the
+ * tensor-tile nonzeros take a second, row-run pass.  N > 128 runs the
+ * product and the gradient pass one after the other.  dvals is fully
+ * written when A^T's tiles hold every nonzero. */
+int stile_spmm_plan_set_transpose_ids(StileSpmmPlan* planT, const int32_t* perm, int64_t nnz, void* stream);
+int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t lddc,
+                        const float* B, int64_t ldb, float* dB, int64_t lddb,
+                        float* dvals, int32_t N, void* stream);
+
 /* Refresh the tile values of a plan from vals[nnz] (device, CSR order of the
  * pattern the plan was built for); the pattern and index arrays are kept.
  * Used when A's values change between calls (training the values). */

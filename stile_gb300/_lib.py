@@ -144,6 +144,11 @@ EXPORTS = {
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                                   ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),
     "stile_spmm_plan_set_values": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "stile_spmm_plan_set_transpose_ids": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                                         ctypes.c_void_p]),
+    "stile_spmm_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                           ctypes.c_int32, ctypes.c_void_p]),
     "stile_spmm_plan_set_wait_policy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     "stile_spmm_plan_error_flag": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, c_i32p]),
     "stile_debug_umma_probe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,

@@ -8,7 +8,10 @@
 
 The backward of the SpMM is hand-written: dB = A^T @ dC with a plan built
 once for the transposed pattern, and dvals = <dC[row], B[col]> for every
-nonzero of A, computed by walking the forward plan's own tiles.
+nonzero of A.  With an fp32 B both come from one pass over the transposed
+plan's row tiles (each dC row gathered for dB also gives its entries' value
+gradients) plus a row-run pass for its tensor tiles; otherwise dvals walks
+the forward plan's own tiles.
 """
 from __future__ import annotations
 
@@ -110,6 +113,11 @@ class SpmmOperator:
     def dvals(self, dC: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
         return self.handle.dvals(dC, B)
 
+    def backward(self, dC: torch.Tensor, B: torch.Tensor, dB: torch.Tensor | None = None):
+        """(dB = A^T @ dC, dvals = <dC[row], B[col]> on A's pattern) in one
+        pass over the transposed plan's row tiles (fp32 dC and B)."""
+        return self.transposed[0].handle.backward(dC, B, dB)
+
     def batched(self, vals: torch.Tensor, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """C[h] = A(vals[h]) @ B[h] for H value sets on A's pattern (vals
         [H, nnz] in CSR order, B [H, K, N]): the multi-head SpMM, one launch
@@ -147,6 +155,7 @@ class SpmmOperator:
             perm_t = torch.as_tensor(perm, device="cuda")
             if self._vals is not None:
                 op.set_values(self._vals[perm_t])
+            op.handle.set_transpose_ids(perm_t)
             self._transposed = (op, perm_t)
         return self._transposed
 
@@ -275,6 +284,10 @@ class HybridSpMMFunction(torch.autograd.Function):
         # dC is passed as it is (a row stride that is a multiple of 4 and a
         # 16-byte aligned base need no copy; ops.dense_operand copies others)
         dvals = dB = None
+        if ctx.needs_input_grad[0] and ctx.needs_input_grad[1] and B.dtype == torch.float32:
+            # both gradients from one pass over the transposed plan's tiles
+            dB, dvals = op.backward(dC, B)
+            return dvals, dB, None
         if ctx.needs_input_grad[0]:
             dvals = op.dvals(dC, B)
         if ctx.needs_input_grad[1]:

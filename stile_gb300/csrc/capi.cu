@@ -51,6 +51,7 @@ bool in_range(const T* a, long n, long lo, long hi) {
 
 struct StileSpmmPlan {
   void* arena = nullptr;
+  void* tid_buf = nullptr;  // ids in the forward operator's numbering (set_transpose_ids)
   int* err_flag = nullptr;
   stile::SpmmArgs args{};
   int M = 0, K = 0;
@@ -368,6 +369,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
 
   // value-gradient entry list from the tiles (needs the nonzero ids)
   std::vector<int32_t> dv_row, dv_col, dv_id;
+  long n_tc_dv = 0;  // the list's tensor-core entries come first
   if (h->tc_nnz_id)
     for (int i = 0; i < h->tc_n_items; ++i)
       for (int r = 0; r < 16; ++r) {
@@ -382,6 +384,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
             dv_id.push_back(id);
           }
       }
+  n_tc_dv = (long)dv_id.size();
   if (h->ell_nnz_id)
     for (int i = 0; i < h->ell_n_items; ++i) {
       const int K = h->ell_item_K[i];
@@ -399,10 +402,15 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
       }
     }
   const long ndv = (long)dv_id.size();
-  // runs of one row, cut at kRunGroup entries (the row-run kernel's groups)
+  // runs of one row, cut at kRunGroup entries and where the tensor-core
+  // entries end (the row-run kernel's groups; the tensor-core prefix alone
+  // serves the fused backward)
   std::vector<int32_t> dv_gptr{0}, dv_grow;
+  int dv_groups_tc = 0;
   for (long t = 0; t < ndv; ++t) {
-    const bool cut = t + 1 == ndv || dv_row[t + 1] != dv_row[t] || t + 1 - dv_gptr.back() == stile::kRunGroup;
+    const bool cut = t + 1 == ndv || dv_row[t + 1] != dv_row[t] || t + 1 - dv_gptr.back() == stile::kRunGroup ||
+                     t + 1 == n_tc_dv;
+    if (t + 1 == n_tc_dv) dv_groups_tc = (int)dv_grow.size() + 1;
     if (cut) {
       dv_grow.push_back(dv_row[t]);
       dv_gptr.push_back((int32_t)(t + 1));
@@ -489,6 +497,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   a.dv_col = (const int*)P(i_dvc);
   a.dv_id = (const int*)P(i_dvi);
   a.dv_n_groups = (int)dv_grow.size();
+  a.dv_n_groups_tc = dv_groups_tc;
   a.dv_gptr = (const int*)P(i_dvgp);
   a.dv_grow = (const int*)P(i_dvgr);
   a.tc_chunk_kbeg = (const int*)P(i_ckb);
@@ -504,6 +513,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
 
 int stile_spmm_plan_free(StileSpmmPlan* plan) {
   if (!plan) return STILE_OK;
+  if (plan->tid_buf) cudaFree(plan->tid_buf);
   cudaError_t e = cudaFree(plan->arena);
   delete plan;
   if (e != cudaSuccess) return cuda_fail(e, "cudaFree(plan)");
@@ -689,6 +699,90 @@ int stile_spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, c
 int stile_spmm_dvals_bf16(const StileSpmmPlan* plan, const float* dY, int64_t lddy, const uint16_t* B, int64_t ldb,
                           float* dvals, int32_t N, void* stream) {
   return spmm_dvals(plan, dY, lddy, B, true, ldb, dvals, N, stream);
+}
+
+int stile_spmm_plan_set_transpose_ids(StileSpmmPlan* plan, const int32_t* perm, int64_t nnz, void* stream) {
+  if (!plan || !perm) return fail(STILE_E_INVALID, "null argument");
+  if (nnz != plan->nnz) return fail(STILE_E_INVALID, "perm must have one entry per nonzero of the plan");
+  if ((plan->args.tc_n_items && !plan->args.tc_nnz_id) || (plan->args.ell_n_groups && !plan->args.ell_nnz_id))
+    return fail(STILE_E_INVALID, "plan was uploaded without nonzero ids");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const long n_ell = plan->args.ell_n_groups ? plan->ell_n_slots : 0, n_dv = plan->args.dv_n;
+  if (!plan->tid_buf) {
+    cudaError_t e = cudaMalloc(&plan->tid_buf, (size_t)(n_ell + n_dv + 1) * 4);
+    if (e != cudaSuccess) {
+      plan->tid_buf = nullptr;
+      return cuda_fail(e, "cudaMalloc(transpose ids)");
+    }
+  }
+  int* ids = static_cast<int*>(plan->tid_buf);
+  cudaError_t e = stile::launch_permute_ids(plan->args.ell_nnz_id, n_ell, perm, ids, st);
+  if (e == cudaSuccess) e = stile::launch_permute_ids(plan->args.dv_id, n_dv, perm, ids + n_ell, st);
+  if (e != cudaSuccess) return cuda_fail(e, "id permutation launch");
+  g_launches += (n_ell > 0) + (n_dv > 0);
+  plan->args.ell_dvp_id = ids;
+  plan->args.dvp_id = ids + n_ell;
+  return STILE_OK;
+}
+
+int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t lddc, const float* B, int64_t ldb,
+                        float* dB, int64_t lddb, float* dvals, int32_t N, void* stream) {
+  if (!planT) return fail(STILE_E_INVALID, "null plan");
+  if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
+  if (!dvals) return fail(STILE_E_INVALID, "null dvals");
+  if (!planT->args.dvp_id || (planT->args.ell_n_groups && !planT->args.ell_dvp_id))
+    return fail(STILE_E_INVALID, "call stile_spmm_plan_set_transpose_ids first");
+  int rc;
+  if ((rc = check_dense(lddc, N, dC, "dC")) != 0) return rc;
+  if ((rc = check_dense(ldb, N, B, "B")) != 0) return rc;
+  if ((rc = check_dense(lddb, N, dB, "dB")) != 0) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  stile::SpmmArgs a = planT->args;
+  a.B = dC;
+  a.b_bf16 = 0;
+  a.ldb = lddc;
+  a.C = dB;
+  a.ldc = lddb;
+  a.N = N;
+  a.n_fchunks = (N + 127) / 128;
+  a.dvx = B;
+  a.dvx_ld = ldb;
+  a.dv_out = dvals;
+  if (N > 128 || !planT->args.ell_n_groups) {
+    // wider than one feature pass (or no row tiles): the transposed product,
+    // then the gradient of every nonzero from the run list
+    if ((rc = spmm_run(planT, dC, false, lddc, dB, lddb, N, stream)) != 0) return rc;
+    e = stile::launch_sddmm_runs(a.dv_n_groups, a.dv_gptr, a.dv_grow, a.dv_col, a.dvp_id, B, ldb, dC, false, lddc,
+                                 dvals, N, st);
+    if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
+    g_launches += (a.dv_n_groups > 0);
+    return STILE_OK;
+  }
+  bool zero_kernel = false;
+  if (2L * planT->n_zero_rows >= planT->M) {
+    e = cudaMemset2DAsync(dB, (size_t)lddb * 4, 0, (size_t)N * 4, (size_t)planT->M, st);
+    if (e != cudaSuccess) return cuda_fail(e, "zeroing dB");
+  } else {
+    e = stile::launch_zero_rows(planT->zero_rows, planT->n_zero_rows, dB, lddb, N, st);
+    if (e != cudaSuccess) return cuda_fail(e, "zero_rows launch");
+    if (planT->n_zero_rows) g_launches++;
+    zero_kernel = planT->n_zero_rows > 0;
+  }
+  a.ell_lazy_wait = zero_kernel ? 1 : 0;
+  e = stile::launch_ell_bwd(a, st);
+  if (e != cudaSuccess) return cuda_fail(e, "fused backward ELL launch");
+  g_launches++;
+  e = stile::launch_tc(a, st);
+  if (e != cudaSuccess) return cuda_fail(e, "tensor-core SpMM launch");
+  if (a.tc_n_chunks) g_launches++;
+  // the tensor-core nonzeros' gradients: the run list's tensor-core prefix
+  // (rows of A^T hold B's rows, columns dC's)
+  e = stile::launch_sddmm_runs(a.dv_n_groups_tc, a.dv_gptr, a.dv_grow, a.dv_col, a.dvp_id, B, ldb, dC, false, lddc,
+                               dvals, N, st);
+  if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
+  g_launches += (a.dv_n_groups_tc > 0);
+  return STILE_OK;
 }
 
 int stile_spmm_plan_set_values(StileSpmmPlan* plan, const float* vals, void* stream) {

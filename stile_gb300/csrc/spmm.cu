@@ -627,6 +627,116 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   if (p.ell_lazy_wait) griddep_wait();
 }
 
+// The fused backward's ELL pass, run over the transposed operator's tiles
+// with B = dC: the stream kernel above for VEC = 2 in one feature pass
+// (N <= 8 LPR), and for every entry (row r, column c) of A^T also
+//   dv_out[ell_dvp_id[s]] = <dC[c], dvx[r]>,
+// the value gradient of the forward's nonzero (c, r).  The dC row it
+// gathers for the product is the one the gradient needs; dvx[r] (the
+// forward's dense operand) is loaded once per row run and kept in registers.
+// The two entries of a batch reduce their dot products together with the
+// transposing butterfly (lanes whose high bit spells the entry hold its
+// sum).  kFull: N == 8 LPR.
+template <int LPR, bool kFull>
+__global__ void __launch_bounds__(256, 4) spmm_ell_bwd_kernel(SpmmArgs p) {
+  constexpr int kBatch = 2;
+  static_assert(LPR >= 2, "two entries per batch");
+  if (!p.ell_lazy_wait) griddep_wait();
+  griddep_launch_dependents();
+  const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR;
+  const unsigned mask = (LPR == 32) ? 0xffffffffu : (((1u << LPR) - 1u) << (sub * LPR));
+  const int g = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (kWarp / LPR) + sub;
+  if (g >= p.ell_n_groups) {  // the whole sub-group leaves together
+    if (p.ell_lazy_wait) griddep_wait();
+    return;
+  }
+  const int p0 = __ldg(p.ell_group_ptr + g);
+  const int n = __ldg(p.ell_group_ptr + g + 1) - p0;
+  const int4* __restrict__ ent = p.ell_entry + p0;
+  const int N = p.N;
+  const int f = 8 * sl;
+  auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, 0); };
+  auto row_of = [](int ce) { const int code = ce >> 1; return code >= 0 ? code : -code - 1; };
+  float4 acc[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+  float4 xr[2];
+  int xrow = -1;
+  int4 mcur = rec(sl);
+#pragma unroll 1
+  for (int c0 = 0; c0 < n; c0 += LPR) {
+    const int4 mnext = rec(c0 + LPR + sl);
+#pragma unroll 1
+    for (int b0 = c0; b0 < min(n, c0 + LPR); b0 += kBatch) {
+      float4 bv[kBatch][2];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int c = __shfl_sync(mask, mcur.x, b0 - c0 + u, LPR);  // records past n: row 0, value 0
+        const float* row = p.B + (long)c * p.ldb;
+#pragma unroll
+        for (int w = 0; w < 2; ++w) bv[u][w] = kFull ? ldg4(row + f + 4 * w) : ld4_live(row, f + 4 * w, N);
+      }
+      float s[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const float v = __int_as_float(__shfl_sync(mask, mcur.y, b0 - c0 + u, LPR));
+        const int ce = __shfl_sync(mask, mcur.z, b0 - c0 + u, LPR);
+        const int r = row_of(ce);
+        if (r != xrow) {  // a new row run: its dvx row (uniform over the sub-group)
+          const float* xp = p.dvx + (long)r * p.dvx_ld;
+#pragma unroll
+          for (int w = 0; w < 2; ++w) xr[w] = kFull ? ldg4(xp + f + 4 * w) : ld4_live(xp, f + 4 * w, N);
+          xrow = r;
+        }
+        s[u] = dot4(xr[0], bv[u][0]) + dot4(xr[1], bv[u][1]);
+#pragma unroll
+        for (int w = 0; w < 2; ++w) fma4(acc[w], v, bv[u][w]);
+        if (ce & 1) {
+          const int code = ce >> 1;
+          float* crow = p.C + (long)r * p.ldc;
+          if (code < 0 && p.ell_lazy_wait) griddep_wait();
+#pragma unroll
+          for (int w = 0; w < 2; ++w) {
+            const int fw = f + 4 * w;
+            if (kFull) {
+              if (code >= 0) *reinterpret_cast<float4*>(crow + fw) = acc[w];
+              else atomicAdd(reinterpret_cast<float4*>(crow + fw), acc[w]);
+            } else {
+              if (code >= 0) st_row4(crow, fw, N, acc[w]); else red_row4(crow, fw, N, acc[w]);
+            }
+            acc[w] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
+      }
+      // transposing butterfly over the batch: lanes with bit LPR/2 set keep
+      // entry 1, the others entry 0, then the halves reduce on their own
+      const bool up = (sl & (LPR / 2)) != 0;
+      float t = (up ? s[1] : s[0]) + __shfl_xor_sync(mask, up ? s[0] : s[1], LPR / 2);
+#pragma unroll
+      for (int o = LPR / 4; o > 0; o >>= 1) t += __shfl_xor_sync(mask, t, o);
+      const int e = up ? 1 : 0;
+      if ((sl & (LPR / 2 - 1)) == 0 && b0 + e < n) {
+        const int id = __ldg(p.ell_dvp_id + p0 + b0 + e);
+        if (id >= 0) p.dv_out[id] = t;
+      }
+    }
+    mcur = mnext;
+  }
+  if (p.ell_lazy_wait) griddep_wait();
+}
+
+__global__ void permute_ids_kernel(const int* __restrict__ in, long n, const int* __restrict__ perm,
+                                   int* __restrict__ out) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int v = in[i];
+  out[i] = v >= 0 ? perm[v] : -1;
+}
+
+cudaError_t launch_permute_ids(const int* in, long n, const int* perm, int* out, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  permute_ids_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, n, perm, out);
+  return cudaGetLastError();
+}
+
 // The same entry stream over a bf16 B: each lane covers 8 features with one
 // 16-byte load (half the gathered bytes of fp32 rows), converts them to
 // fp32 and accumulates in fp32; 4 entries' rows in flight per lane.
@@ -1081,6 +1191,26 @@ cudaError_t launch_ell(const SpmmArgs& args, cudaStream_t st) {
 
 // dvals[t] = <dY[row(t)], B[col(t)]> over the plan's entry list, as runs of
 // one row (the row-run SDDMM kernel holds the dY row and gathers B rows)
+template <int LPR>
+static cudaError_t launch_ell_bwd_t(SpmmArgs p, cudaStream_t st) {
+  const long gx = (p.ell_n_groups + (256 / LPR) - 1) / (256 / LPR);
+  const dim3 grid((unsigned)gx, 1, 1);
+  return p.N == 8 * LPR ? launch_dependent(spmm_ell_bwd_kernel<LPR, true>, grid, dim3(256), 0, st, p)
+                        : launch_dependent(spmm_ell_bwd_kernel<LPR, false>, grid, dim3(256), 0, st, p);
+}
+
+cudaError_t launch_ell_bwd(const SpmmArgs& p, cudaStream_t st) {
+  if (p.ell_n_groups == 0) return cudaSuccess;
+  if (p.N > 128 || p.b_bf16 || p.heads > 1) return cudaErrorNotSupported;
+  int lpr = 4;
+  while (8 * lpr < p.N) lpr <<= 1;
+  switch (lpr) {
+    case 4: return launch_ell_bwd_t<4>(p, st);
+    case 8: return launch_ell_bwd_t<8>(p, st);
+    default: return launch_ell_bwd_t<16>(p, st);
+  }
+}
+
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {
   return launch_sddmm_runs(p.dv_n_groups, p.dv_gptr, p.dv_grow, p.dv_col, p.dv_id, dY, lddy, p.B, p.b_bf16 != 0,
                            p.ldb, dvals, p.N, st);

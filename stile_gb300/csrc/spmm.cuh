@@ -79,6 +79,17 @@ struct SpmmArgs {
   // nothing arrives on, so that wait and then every other role's wait runs
   // out and the kernel returns with the error flag set
   int stall_test;
+  // fused backward (this plan is the transposed operator's): the ELL pass
+  // that computes dB = A^T dC also writes dvals[ell_dvp_id[s]] =
+  // <dC[col], dvx[row]> for its entries (dvx: the forward's dense operand),
+  // and the run list's tensor-core prefix (dv_n_groups_tc groups) gives the
+  // rest with ids dvp_id; ids in the forward operator's nonzero numbering
+  const float* dvx;
+  long dvx_ld;
+  float* dv_out;
+  const int* ell_dvp_id;
+  const int* dvp_id;
+  int dv_n_groups_tc;
 };
 
 cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const float* vals,
@@ -100,6 +111,10 @@ int tc_persistent_ctas(int mode);
 // streaming multiprocessors of the current device (cached; 1 on error)
 int device_sm_count();
 cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st);
+// the ELL pass of the fused backward (fp32, N <= 128, one head)
+cudaError_t launch_ell_bwd(const SpmmArgs& p, cudaStream_t st);
+// out[i] = in[i] >= 0 ? perm[in[i]] : -1
+cudaError_t launch_permute_ids(const int* in, long n, const int* perm, int* out, cudaStream_t st);
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st);
 constexpr int kChunkSteps = 32;
 cudaError_t launch_pack_values(const SpmmArgs& p, const float* vals, long nnz, int heads, void* ell_out,

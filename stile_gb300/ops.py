@@ -242,6 +242,34 @@ class DeviceSpmmPlan:
                    "stile_spmm_dvals_bf16" if bf16 else "stile_spmm_dvals")
         return out
 
+    def set_transpose_ids(self, perm: torch.Tensor):
+        """This plan is the transposed operator of a forward plan: perm[t] is
+        the forward's nonzero that this plan's nonzero t is (device int32)."""
+        perm = perm.to(torch.int32).contiguous()
+        if perm.numel() != self.nnz:
+            raise ValueError("perm must have one entry per nonzero")
+        self._perm = perm
+        _lib.check(self.lib.stile_spmm_plan_set_transpose_ids(self.handle, perm.data_ptr(), self.nnz, _stream()),
+                   "stile_spmm_plan_set_transpose_ids")
+
+    def backward(self, dC: torch.Tensor, B: torch.Tensor, dB: torch.Tensor | None = None):
+        """(dB, dvals) of the forward C = A @ B whose transposed plan this is:
+        dB = A^T @ dC and dvals = <dC[row], B[col]> over A's nonzeros (forward
+        numbering), from one pass over this plan's row tiles
+        (stile_spmm_backward); fp32 operands."""
+        dC, lddc = dense_operand(dC, "dC")
+        B, ldb = dense_operand(B, "B")
+        N = dC.shape[1]
+        if dB is None:
+            dB, lddb = new_output(self.M, N, dC.device)
+        else:
+            lddb = dB.stride(0)
+        alloc = torch.empty if self._dvals_cover_all else torch.zeros
+        dvals = alloc(self.nnz, dtype=torch.float32, device=dC.device)
+        _lib.check(self.lib.stile_spmm_backward(self.handle, dC.data_ptr(), lddc, B.data_ptr(), ldb, dB.data_ptr(),
+                                                lddb, dvals.data_ptr(), N, _stream()), "stile_spmm_backward")
+        return dB, dvals
+
     def set_values(self, vals: torch.Tensor):
         _require_cuda(vals, "vals")
         vals = vals.float().contiguous()

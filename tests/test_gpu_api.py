@@ -246,3 +246,34 @@ def test_batched_heads_match_one_head_at_a_time(N, mode, knots):
         one = op(B[h]).cpu().numpy()
         assert np.allclose(C[h], one, rtol=1e-5, atol=1e-5)
     assert op.handle.error_flag() == 0
+
+
+@pytest.mark.parametrize("N", [128, 41, 64, 200])
+@pytest.mark.parametrize("mode", [D.TC_BF16, D.TC_SPLIT_BF16], ids=["bf16", "split"])
+@pytest.mark.parametrize("pattern", ["graph", "rect"])
+def test_fused_backward_matches_separate_passes_and_fp64(N, mode, pattern):
+    """stile_spmm_backward: dB = A^T dC and dvals from one pass over the
+    transposed plan's row tiles (plus a row-run pass for its tensor tiles)
+    equal the separate transposed product and value-gradient pass, and
+    float64; on a symmetric community graph (the transposed plan reuses the
+    forward's) and a rectangular power-law matrix (its own plan)."""
+    if pattern == "graph":
+        A = _graph(seed=15)
+    else:
+        A = syn.power_law_rows(3000, 2200, min_len=2, max_len=300, seed=16)
+    op = plan_spmm(A, N, PlanConfig(tc_mode=mode))
+    rng = np.random.default_rng(17)
+    B = rng.standard_normal((A.shape[1], N)).astype(np.float32)
+    dC = rng.standard_normal((A.shape[0], N)).astype(np.float32)
+    Bt, dCt = torch.as_tensor(B, device="cuda"), torch.as_tensor(dC, device="cuda")
+    dB, dv = op.backward(dCt, Bt)
+    dv_sep = op.dvals(dCt, Bt)
+    opT, _ = op.transposed
+    dB_sep = opT(dCt)
+    torch.cuda.synchronize()
+    assert op.handle.error_flag() == 0 and opT.handle.error_flag() == 0
+    assert torch.allclose(dv, dv_sep, rtol=1e-5, atol=1e-5)
+    assert torch.allclose(dB, dB_sep, rtol=1e-5, atol=1e-5)
+    tol = 1e-2 if mode == D.TC_BF16 else 1e-5
+    assert S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC, B)) <= 1e-5
+    assert S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(op.A.T.tocsr(), dC)) <= tol
