@@ -224,6 +224,26 @@ int stile_csr_row_softmax(int32_t M, const int32_t* indptr, int64_t nnz,
                           const float* x, float* out, float scale,
                           int32_t batch, void* stream);
 
+/*
+ * Fused sparse attention, every head in one launch (no counterpart kernel in
+ * the reference, which runs the three steps as separate operators):
+ *   out[h][r] = sum_t p_t V[h][c_t],  p = softmax over row r's stored
+ *   entries c_t of scale * <Q[h][r], K[h][c_t]> (the others count as -inf)
+ * for the CSR pattern (indptr[n_rows + 1], indices: column ids < the rows of
+ * K and V, not checked).  One pass per row with an online softmax: neither
+ * the scores nor the probabilities are stored.  fp32; 1 <= F, Fv <= 128;
+ * row strides multiples of 4 elements, 16-byte aligned rows; head h's
+ * operands start h * stride elements further.  A row without entries gives
+ * zeros.  It replaces the chain SDDMM -> stile_csr_row_softmax -> batched
+ * SpMM of the LogSparse / Strided attention operators
+ * (MY_sparse/gen_formats_v2.py:2926-3003).
+ */
+int stile_sparse_attention(int32_t n_rows, const int32_t* indptr, const int32_t* indices, const float* Q,
+                           const float* K, const float* V, int64_t ldq, int64_t ldk, int64_t ldv,
+                           int64_t q_head_stride, int64_t k_head_stride, int64_t v_head_stride, float* out,
+                           int64_t ldo, int64_t out_head_stride, int32_t F, int32_t Fv, float scale, int32_t heads,
+                           void* stream);
+
 /* Learned tile cost model (replaces get_MLP_pred / PyTorchMLP,
  * my_cost_model.py:1010-1093, and its trainer MLP_train_cost_model.py:81-204):
  * a STILE_MLP_FEATURES -> 64 -> 32 -> 1 ReLU network over standardised tile

@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD, "libstile_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["spmm.cu", "sddmm.cu", "probe.cu", "capi.cu", "noalloc.cu", "mlp.cu"]
+SOURCES = ["spmm.cu", "sddmm.cu", "attention.cu", "probe.cu", "capi.cu", "noalloc.cu", "mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -130,6 +130,11 @@ EXPORTS = {
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                           ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p]),
     "stile_csr_group_nnz": (ctypes.c_int32, []),
+    "stile_sparse_attention": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                              ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                              ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+                                              ctypes.c_int32, ctypes.c_float, ctypes.c_int32, ctypes.c_void_p]),
     "stile_csr_row_softmax": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                              ctypes.c_void_p, ctypes.c_float, ctypes.c_int32, ctypes.c_void_p]),
     "stile_mlp_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,

@@ -187,20 +187,24 @@ class SddmmOperator:
 
 
 class SparseAttention:
-    """softmax(scale * Q K^T on a sparse pattern) @ V for every head: the
-    SDDMM of the scores over the pattern, a row softmax over each row's
-    entries (``stile_csr_row_softmax``, all heads in one launch), then the
-    batched hybrid SpMM with each head's probabilities as its values (one
-    launch of each kernel for all heads).  The sparse-attention
-    pipeline the reference's LogSparse / Strided operators come from
-    (MY_sparse/gen_formats_v2.py:2926-3003); both plans are searched once
-    per pattern (and cached with ``cfg.cache_dir``).
+    """softmax(scale * Q K^T on a sparse pattern) @ V for every head, the
+    sparse-attention pipeline the reference's LogSparse / Strided operators
+    come from (MY_sparse/gen_formats_v2.py:2926-3003).
+
+    ``fused=True`` (default; fp32, F and Fv <= 128): one launch for all
+    heads (``stile_sparse_attention``) that walks each row once with an
+    online softmax, so the scores and probabilities never reach memory.
+    ``fused=False``: the SDDMM of the scores over the pattern (hybrid plan),
+    a row softmax over each row's entries (``stile_csr_row_softmax``, all
+    heads in one launch), then the batched hybrid SpMM with each head's
+    probabilities as its values; both plans are searched once per pattern
+    (and cached with ``cfg.cache_dir``).
 
     Q, K: [H, n, F] (or [n, F]); V: [H, n, Fv]; the result is fp32
     [H, n, Fv].
     """
 
-    def __init__(self, pattern, F, Fv=None, cfg: PlanConfig | None = None, scale=None):
+    def __init__(self, pattern, F, Fv=None, cfg: PlanConfig | None = None, scale=None, fused=True):
         from . import _lib
         A = _csr(pattern)
         A.data[:] = 1.0
@@ -209,13 +213,42 @@ class SparseAttention:
         self.F = int(F)
         self.Fv = int(Fv or F)
         self.scale = float(scale if scale is not None else 1.0 / np.sqrt(self.F))
-        cfg = cfg or PlanConfig()
-        kw = dict(cfg.__dict__)
-        kw["max_bucket_size"] = kw["max_bucket_size"] or 32
-        self.scores = SddmmOperator(A, self.F, PlanConfig(**kw))
-        self.product = SpmmOperator(A, self.Fv, cfg)
+        self.fused = bool(fused) and self.F <= 128 and self.Fv <= 128
+        if not self.fused:
+            cfg = cfg or PlanConfig()
+            kw = dict(cfg.__dict__)
+            kw["max_bucket_size"] = kw["max_bucket_size"] or 32
+            self.scores = SddmmOperator(A, self.F, PlanConfig(**kw))
+            self.product = SpmmOperator(A, self.Fv, cfg)
         self.indptr = torch.as_tensor(A.indptr.astype(np.int32), device="cuda")
+        self.indices = torch.as_tensor(A.indices.astype(np.int32), device="cuda")
         self.lib = _lib.load()
+
+    def _fused(self, Q, K, V):
+        from . import _lib
+        from .ops import _stream
+
+        def heads_operand(x, name):
+            x = x.float()
+            H, n, f = x.shape
+            ld = (f + 3) // 4 * 4
+            if x.stride() != (n * ld, ld, 1) or x.data_ptr() % 16:
+                buf = torch.zeros((H, n, ld), dtype=torch.float32, device=x.device)
+                buf[:, :, :f] = x
+                x = buf
+            return x, ld
+        Q, ldq = heads_operand(Q, "Q")
+        K, ldk = heads_operand(K, "K")
+        V, ldv = heads_operand(V, "V")
+        H, n = Q.shape[0], self.n
+        ldo = (self.Fv + 3) // 4 * 4
+        out = torch.empty((H, n, ldo), dtype=torch.float32, device=Q.device)
+        _lib.check(self.lib.stile_sparse_attention(n, self.indptr.data_ptr(), self.indices.data_ptr(), Q.data_ptr(),
+                                                   K.data_ptr(), V.data_ptr(), ldq, ldk, ldv, Q.stride(0),
+                                                   K.stride(0), V.stride(0), out.data_ptr(), ldo, out.stride(0),
+                                                   self.F, self.Fv, self.scale, H, _stream()),
+                   "stile_sparse_attention")
+        return out[:, :, :self.Fv]
 
     def __call__(self, Q, K, V):
         from . import _lib
@@ -223,6 +256,9 @@ class SparseAttention:
         single = Q.dim() == 2
         if single:
             Q, K, V = Q[None], K[None], V[None]
+        if self.fused:
+            out = self._fused(Q, K, V)
+            return out[0] if single else out
         H = Q.shape[0]
         nnz = self.A.nnz
         S = torch.empty((H, nnz), dtype=torch.float32, device=Q.device)

@@ -818,6 +818,32 @@ int stile_spmm_plan_set_wait_policy(StileSpmmPlan* plan, int32_t polls, int32_t 
   return STILE_OK;
 }
 
+int stile_sparse_attention(int32_t n_rows, const int32_t* indptr, const int32_t* indices, const float* Q,
+                           const float* K, const float* V, int64_t ldq, int64_t ldk, int64_t ldv,
+                           int64_t q_head_stride, int64_t k_head_stride, int64_t v_head_stride, float* out,
+                           int64_t ldo, int64_t out_head_stride, int32_t F, int32_t Fv, float scale, int32_t heads,
+                           void* stream) {
+  if (n_rows < 0 || heads < 0) return fail(STILE_E_INVALID, "bad shape");
+  if (F <= 0 || Fv <= 0 || F > 128 || Fv > 128)
+    return fail(STILE_E_UNSUPPORTED, "fused attention takes 1..128 features for Q/K and for V");
+  if (n_rows == 0 || heads == 0) return STILE_OK;
+  if (!indptr || !indices) return fail(STILE_E_INVALID, "null pattern");
+  int rc;
+  if ((rc = check_dense(ldq, F, Q, "Q")) != 0) return rc;
+  if ((rc = check_dense(ldk, F, K, "K")) != 0) return rc;
+  if ((rc = check_dense(ldv, Fv, V, "V")) != 0) return rc;
+  if ((rc = check_dense(ldo, Fv, out, "out")) != 0) return rc;
+  if (heads > 1 && ((q_head_stride % 4) || (k_head_stride % 4) || (v_head_stride % 4) || (out_head_stride % 4)))
+    return fail(STILE_E_INVALID, "head strides must be multiples of 4 elements");
+  if (heads > 1 && out_head_stride < (int64_t)n_rows * ldo) return fail(STILE_E_INVALID, "output heads overlap");
+  cudaError_t e = stile::launch_sparse_attention(n_rows, indptr, indices, Q, K, V, ldq, ldk, ldv, q_head_stride,
+                                                 k_head_stride, v_head_stride, out, ldo, out_head_stride, F, Fv,
+                                                 scale, heads, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "sparse attention launch");
+  g_launches++;
+  return STILE_OK;
+}
+
 int stile_csr_row_softmax(int32_t M, const int32_t* indptr, int64_t nnz, const float* x, float* out, float scale,
                           int32_t batch, void* stream) {
   if (M < 0 || nnz < 0 || batch < 0) return fail(STILE_E_INVALID, "bad shape");

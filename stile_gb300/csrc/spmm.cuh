@@ -152,6 +152,11 @@ cudaError_t launch_sddmm_runs(int n_groups, const int* gptr, const int* grow, co
                               const float* X, long ldx, const void* Y, bool y_bf16, long ldy, float* out, int F,
                               cudaStream_t st);
 
+cudaError_t launch_sparse_attention(int n_rows, const int* indptr, const int* indices, const float* Q,
+                                    const float* K, const float* V, long ldq, long ldk, long ldv, long q_head,
+                                    long k_head, long v_head, float* out, long ldo, long o_head, int F, int Fv,
+                                    float scale, int heads, cudaStream_t st);
+
 cudaError_t launch_umma_probe(const void* a_img, const void* b_img, const uint32_t* desc6,
                               uint32_t idesc, uint32_t kind, float* out, int* err, cudaStream_t st);
 

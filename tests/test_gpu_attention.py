@@ -1,5 +1,7 @@
-"""Sparse attention on the GPU (SDDMM -> row softmax -> hybrid SpMM) against
-the float64 restatement, on the reference's LogSparse and Strided masks."""
+"""Sparse attention on the GPU against the float64 restatement, on the
+reference's LogSparse and Strided masks: the fused one-pass kernel (online
+softmax, all heads in one launch) and the three-step path (SDDMM -> row
+softmax -> hybrid SpMM)."""
 import numpy as np
 import pytest
 import torch
@@ -40,7 +42,31 @@ def test_sparse_attention_matches_fp64(kind, mode, tol):
     A = syn.logsparse_pattern(n) if kind == "logsparse" else syn.strided_pattern(n)
     rng = np.random.default_rng(2)
     Q, K, V = (rng.standard_normal((H, n, F)).astype(np.float32) for _ in range(3))
-    att = SparseAttention(A, F, cfg=PlanConfig(tc_mode=mode))
+    att = SparseAttention(A, F, cfg=PlanConfig(tc_mode=mode), fused=False)
     out = att(*(torch.as_tensor(x, device="cuda") for x in (Q, K, V))).cpu().numpy()
     ref = OA.attention_fp64(A, Q, K, V, 1.0 / np.sqrt(F))
     assert S.rel_fro(out, ref) <= tol
+
+
+@pytest.mark.parametrize("kind", ["logsparse", "strided"])
+@pytest.mark.parametrize("F,Fv,H", [(64, 64, 2), (128, 128, 3), (41, 24, 1), (16, 100, 2)])
+def test_fused_sparse_attention_matches_fp64(kind, F, Fv, H):
+    """The fused kernel (fp32 throughout, online softmax) within 1e-5 of
+    float64 on widths that fill 128-feature groups and on ragged ones, and a
+    row without entries gives zeros."""
+    n = 1500
+    A = syn.logsparse_pattern(n) if kind == "logsparse" else syn.strided_pattern(n)
+    A = A.tolil()
+    A[7, :] = 0          # an empty row
+    A = A.tocsr()
+    A.eliminate_zeros()
+    rng = np.random.default_rng(3)
+    Q = rng.standard_normal((H, n, F)).astype(np.float32)
+    K = rng.standard_normal((H, n, F)).astype(np.float32)
+    V = rng.standard_normal((H, n, Fv)).astype(np.float32)
+    att = SparseAttention(A, F, Fv)
+    assert att.fused
+    out = att(*(torch.as_tensor(x, device="cuda") for x in (Q, K, V))).cpu().numpy()
+    ref = OA.attention_fp64(A, Q, K, V, 1.0 / np.sqrt(F))
+    assert np.all(out[:, 7] == 0)
+    assert S.rel_fro(out, ref) <= 1e-5
