@@ -717,6 +717,56 @@ def run_gpu(args):
 # ---------------------------------------------------------------------------
 # the other configurations (one JSON line each; the headline is "gcn2")
 # ---------------------------------------------------------------------------
+def run_attention(args):
+    """Sparse attention on the reference's LogSparse and Strided patterns
+    (n = 4096, 8 heads, F = Fv = 64): the fused one-pass kernel against the
+    three-launch path (hybrid SDDMM, row softmax, batched hybrid SpMM), both
+    against float64 on the first two heads."""
+    import torch
+    import oracle.attention as OA
+    import oracle.semantics as S
+    from stile_gb300 import synthetic as syn
+    from stile_gb300.api import SparseAttention
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    n, H, F = 4096, 8, 64
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        ts = []
+        for _ in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            fn()
+            e.record()
+            e.synchronize()
+            ts.append(s.elapsed_time(e))
+        return float(np.median(ts))
+
+    out = {"workload": "sparse_attention", "n": n, "heads": H, "F": F, "Fv": F, "steps": args.steps,
+           "l2": "flushed between iterations (256 MiB write)"}
+    rng = np.random.default_rng(0)
+    Q, K, V = (torch.as_tensor(rng.standard_normal((H, n, F)).astype(np.float32), device=dev) for _ in range(3))
+    for kind in ("logsparse", "strided"):
+        A = syn.logsparse_pattern(n) if kind == "logsparse" else syn.strided_pattern(n)
+        fused = SparseAttention(A, F)
+        three = SparseAttention(A, F, fused=False)
+        ref = OA.attention_fp64(A, Q[:2].cpu().numpy(), K[:2].cpu().numpy(), V[:2].cpu().numpy(), 1.0 / np.sqrt(F))
+        r = {"nnz": int(A.nnz)}
+        for name, att in (("fused", fused), ("three_launches", three)):
+            o = att(Q, K, V)
+            torch.cuda.synchronize()
+            r[name] = {"ms": timed(lambda: att(Q, K, V)),
+                       "rel_fro_first_two_heads": S.rel_fro(o[:2].cpu().numpy(), ref)}
+        r["speedup_fused"] = r["three_launches"]["ms"] / r["fused"]["ms"]
+        out[kind] = r
+    print(json.dumps(out), flush=True)
+
+
 def run_config(args):
     import torch
     import oracle.semantics as S
@@ -895,14 +945,16 @@ def main():
     ap.add_argument("--impl", default="stile", choices=["stile", "reference"])
     ap.add_argument("--workload", default="gcn2",
                     help="gcn2 (the headline line: the two-layer GCN step) or one of the configurations: "
-                         "plain, plain_min10, graph, pruned, pruned_t, sddmm, gcn, gcn_41 (one JSON line of "
-                         "measurements each)")
+                         "plain, plain_min10, graph, pruned, pruned_t, sddmm, gcn, gcn_41, attention (one JSON "
+                         "line of measurements each)")
     ap.add_argument("--plan-cache", default=None,
                     help="directory of the on-disk plan cache (searched plans are stored and reloaded); "
                          "default: search every run")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "attention":
+        run_attention(args)
     elif args.workload != "gcn2":
         run_config(args)
     else:
