@@ -84,6 +84,21 @@ def algorithmic_bytes_spmm(A, N, s_a=4, s_b=4, s_c=4):
     return (M + 1) * 4 + A.nnz * (4 + s_a) + k_touched * N * s_b + M * N * s_c
 
 
+# Random 512-byte fp32 row gathers from L2 measured on this GPU (16-lane
+# groups of 128-bit loads, two rows in flight per group, 8 blocks of 256
+# threads per SM, 119 MB matrix): the rate the row gathers of a SpMM can
+# reach, whatever the HBM roofline says.
+GATHER_PEAK_GBS = 16340.0
+
+
+def gathered_bytes_spmm(op, N, s_b=4):
+    """Bytes of B rows one forward of ``op`` gathers: one row per live ELL
+    entry and 16 rows per tensor-core k-step (a row of N elements each)."""
+    dev = op.device_layout
+    n_ell = int((dev.ell_nnz_id >= 0).sum()) if len(dev.ell_nnz_id) else int(np.count_nonzero(dev.ell_row_len))
+    return (n_ell + len(dev.tc_cols)) * N * s_b
+
+
 def algorithmic_bytes_sddmm(A, F, s=4):
     m_t = int(np.count_nonzero(np.diff(A.indptr)))
     n_t = int(np.count_nonzero(np.bincount(A.indices, minlength=A.shape[1])))
@@ -600,6 +615,7 @@ def run_gpu(args):
     fwd_ms = float(np.mean(fwd_times))
     alg = algorithmic_bytes_spmm(A, WIDTHS[0])
     achieved = alg / (fwd_ms * 1e-3) / 1e9
+    gathered = gathered_bytes_spmm(st.ops[0], WIDTHS[0])
     traffic = profile_traffic("fused_spmm_gcn.md")
     step_bytes = sum(2 * algorithmic_bytes_spmm(A, B.shape[1]) + algorithmic_bytes_sddmm(A, B.shape[1])
                      for B, _ in layers)
@@ -693,7 +709,13 @@ def run_gpu(args):
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "layer-1 forward SpMM (N = 128)",
                          "algorithmic_bytes_per_launch": int(alg), "ms_per_launch": fwd_ms,
-                         "peak_source": peak_kind},
+                         "peak_source": peak_kind,
+                         "gather": {"bytes_per_launch": int(gathered),
+                                    "achieved_gbs": gathered / (fwd_ms * 1e-3) / 1e9,
+                                    "peak_gbs": GATHER_PEAK_GBS,
+                                    "frac": gathered / (fwd_ms * 1e-3) / 1e9 / GATHER_PEAK_GBS,
+                                    "what": "B rows gathered from L2 (one per row-tile entry, 16 per tensor-core "
+                                            "k-step) against the measured random-row gather rate"}},
             "step_roofline": {"algorithmic_bytes_per_step": int(step_bytes),
                               "achieved_gbs": step_bytes / (ms * 1e-3) / 1e9,
                               "frac": step_bytes / (ms * 1e-3) / 1e9 / peak},

@@ -716,11 +716,14 @@ int stile_spmm_plan_set_transpose_ids(StileSpmmPlan* plan, const int32_t* perm, 
     }
   }
   int* ids = static_cast<int*>(plan->tid_buf);
-  cudaError_t e = stile::launch_permute_ids(plan->args.ell_nnz_id, n_ell, perm, ids, st);
+  // the ELL records carry their id in their fourth word; the run list gets
+  // a permuted copy
+  cudaError_t e = stile::launch_record_ids(const_cast<int4*>(plan->args.ell_entry), plan->args.ell_nnz_id, n_ell,
+                                           perm, st);
   if (e == cudaSuccess) e = stile::launch_permute_ids(plan->args.dv_id, n_dv, perm, ids + n_ell, st);
   if (e != cudaSuccess) return cuda_fail(e, "id permutation launch");
   g_launches += (n_ell > 0) + (n_dv > 0);
-  plan->args.ell_dvp_id = ids;
+  plan->args.ell_ids_set = 1;
   plan->args.dvp_id = ids + n_ell;
   return STILE_OK;
 }
@@ -730,7 +733,7 @@ int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t ldd
   if (!planT) return fail(STILE_E_INVALID, "null plan");
   if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
   if (!dvals) return fail(STILE_E_INVALID, "null dvals");
-  if (!planT->args.dvp_id || (planT->args.ell_n_groups && !planT->args.ell_dvp_id))
+  if (!planT->args.dvp_id || (planT->args.ell_n_groups && !planT->args.ell_ids_set))
     return fail(STILE_E_INVALID, "call stile_spmm_plan_set_transpose_ids first");
   int rc;
   if ((rc = check_dense(lddc, N, dC, "dC")) != 0) return rc;

@@ -630,16 +630,17 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
 // The fused backward's ELL pass, run over the transposed operator's tiles
 // with B = dC: the stream kernel above for VEC = 2 in one feature pass
 // (N <= 8 LPR), and for every entry (row r, column c) of A^T also
-//   dv_out[ell_dvp_id[s]] = <dC[c], dvx[r]>,
-// the value gradient of the forward's nonzero (c, r).  The dC row it
-// gathers for the product is the one the gradient needs; dvx[r] (the
-// forward's dense operand) is loaded once per row run and kept in registers.
-// The two entries of a batch reduce their dot products together with the
-// transposing butterfly (lanes whose high bit spells the entry hold its
-// sum).  kFull: N == 8 LPR.
+//   dv_out[id] = <dC[c], dvx[r]>,
+// the value gradient of the forward's nonzero (c, r); id, in the forward's
+// numbering, rides in the entry record's fourth word.  The dC row gathered
+// for the product is the one the gradient needs; dvx[r] (the forward's
+// dense operand) is loaded where a row run starts, for both entries of a
+// batch before either is used, so those loads overlap the dC gathers.  The
+// two entries reduce their dot products together with the transposing
+// butterfly (lanes whose high bit spells the entry hold its sum).
+// kFull: N == 8 LPR.
 template <int LPR, bool kFull>
 __global__ void __launch_bounds__(256, 4) spmm_ell_bwd_kernel(SpmmArgs p) {
-  constexpr int kBatch = 2;
   static_assert(LPR >= 2, "two entries per batch");
   if (!p.ell_lazy_wait) griddep_wait();
   griddep_launch_dependents();
@@ -655,72 +656,99 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_bwd_kernel(SpmmArgs p) {
   const int4* __restrict__ ent = p.ell_entry + p0;
   const int N = p.N;
   const int f = 8 * sl;
-  auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, 0); };
+  auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, -1); };
   auto row_of = [](int ce) { const int code = ce >> 1; return code >= 0 ? code : -code - 1; };
-  float4 acc[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
-  float4 xr[2];
+  auto ld8 = [&](const float* row, float4& a, float4& b) {
+    a = kFull ? ldg4(row + f) : ld4_live(row, f, N);
+    b = kFull ? ldg4(row + f + 4) : ld4_live(row, f + 4, N);
+  };
+  float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
+  float4 xa0 = acc0, xa1 = acc0;  // dvx row of the last entry handled
   int xrow = -1;
   int4 mcur = rec(sl);
 #pragma unroll 1
   for (int c0 = 0; c0 < n; c0 += LPR) {
-    const int4 mnext = rec(c0 + LPR + sl);
 #pragma unroll 1
-    for (int b0 = c0; b0 < min(n, c0 + LPR); b0 += kBatch) {
-      float4 bv[kBatch][2];
+    for (int b0 = c0; b0 < min(n, c0 + LPR); b0 += 2) {
+      const int j = b0 - c0;
+      const int col0 = __shfl_sync(mask, mcur.x, j, LPR), col1 = __shfl_sync(mask, mcur.x, j + 1, LPR);
+      const int ce0 = __shfl_sync(mask, mcur.z, j, LPR), ce1 = __shfl_sync(mask, mcur.z, j + 1, LPR);
+      const float v0 = __int_as_float(__shfl_sync(mask, mcur.y, j, LPR));
+      const float v1 = __int_as_float(__shfl_sync(mask, mcur.y, j + 1, LPR));
+      const int id0 = __shfl_sync(mask, mcur.w, j, LPR), id1 = __shfl_sync(mask, mcur.w, j + 1, LPR);
+      const int r0 = row_of(ce0), r1 = row_of(ce1);
+      // records past n: row 0, column 0, value 0, no run end, id -1
+      float4 b00, b01, b10, b11;
+      ld8(p.B + (long)col0 * p.ldb, b00, b01);
+      ld8(p.B + (long)col1 * p.ldb, b10, b11);
+      float4 x00 = xa0, x01 = xa1;
+      if (r0 != xrow) ld8(p.dvx + (long)r0 * p.dvx_ld, x00, x01);
+      float4 x10 = x00, x11 = x01;
+      if (r1 != r0) ld8(p.dvx + (long)r1 * p.dvx_ld, x10, x11);
+      xa0 = x10;
+      xa1 = x11;
+      xrow = r1;
+      const float s0 = dot4(x00, b00) + dot4(x01, b01);
+      const float s1 = dot4(x10, b10) + dot4(x11, b11);
+      fma4(acc0, v0, b00);
+      fma4(acc1, v0, b01);
 #pragma unroll
-      for (int u = 0; u < kBatch; ++u) {
-        const int c = __shfl_sync(mask, mcur.x, b0 - c0 + u, LPR);  // records past n: row 0, value 0
-        const float* row = p.B + (long)c * p.ldb;
-#pragma unroll
-        for (int w = 0; w < 2; ++w) bv[u][w] = kFull ? ldg4(row + f + 4 * w) : ld4_live(row, f + 4 * w, N);
-      }
-      float s[kBatch];
-#pragma unroll
-      for (int u = 0; u < kBatch; ++u) {
-        const float v = __int_as_float(__shfl_sync(mask, mcur.y, b0 - c0 + u, LPR));
-        const int ce = __shfl_sync(mask, mcur.z, b0 - c0 + u, LPR);
-        const int r = row_of(ce);
-        if (r != xrow) {  // a new row run: its dvx row (uniform over the sub-group)
-          const float* xp = p.dvx + (long)r * p.dvx_ld;
-#pragma unroll
-          for (int w = 0; w < 2; ++w) xr[w] = kFull ? ldg4(xp + f + 4 * w) : ld4_live(xp, f + 4 * w, N);
-          xrow = r;
+      for (int u = 0; u < 2; ++u) {
+        const int ce = u ? ce1 : ce0;
+        if (u) {
+          fma4(acc0, v1, b10);
+          fma4(acc1, v1, b11);
         }
-        s[u] = dot4(xr[0], bv[u][0]) + dot4(xr[1], bv[u][1]);
-#pragma unroll
-        for (int w = 0; w < 2; ++w) fma4(acc[w], v, bv[u][w]);
         if (ce & 1) {
           const int code = ce >> 1;
-          float* crow = p.C + (long)r * p.ldc;
+          float* crow = p.C + (long)(u ? r1 : r0) * p.ldc;
           if (code < 0 && p.ell_lazy_wait) griddep_wait();
-#pragma unroll
-          for (int w = 0; w < 2; ++w) {
-            const int fw = f + 4 * w;
-            if (kFull) {
-              if (code >= 0) *reinterpret_cast<float4*>(crow + fw) = acc[w];
-              else atomicAdd(reinterpret_cast<float4*>(crow + fw), acc[w]);
+          if (kFull) {
+            if (code >= 0) {
+              *reinterpret_cast<float4*>(crow + f) = acc0;
+              *reinterpret_cast<float4*>(crow + f + 4) = acc1;
             } else {
-              if (code >= 0) st_row4(crow, fw, N, acc[w]); else red_row4(crow, fw, N, acc[w]);
+              atomicAdd(reinterpret_cast<float4*>(crow + f), acc0);
+              atomicAdd(reinterpret_cast<float4*>(crow + f + 4), acc1);
             }
-            acc[w] = make_float4(0.f, 0.f, 0.f, 0.f);
+          } else if (code >= 0) {
+            st_row4(crow, f, N, acc0);
+            st_row4(crow, f + 4, N, acc1);
+          } else {
+            red_row4(crow, f, N, acc0);
+            red_row4(crow, f + 4, N, acc1);
           }
+          acc0 = make_float4(0.f, 0.f, 0.f, 0.f);
+          acc1 = acc0;
         }
       }
-      // transposing butterfly over the batch: lanes with bit LPR/2 set keep
-      // entry 1, the others entry 0, then the halves reduce on their own
+      // transposing butterfly over the pair: the upper half keeps entry 1
       const bool up = (sl & (LPR / 2)) != 0;
-      float t = (up ? s[1] : s[0]) + __shfl_xor_sync(mask, up ? s[0] : s[1], LPR / 2);
+      float t = (up ? s1 : s0) + __shfl_xor_sync(mask, up ? s0 : s1, LPR / 2);
 #pragma unroll
       for (int o = LPR / 4; o > 0; o >>= 1) t += __shfl_xor_sync(mask, t, o);
-      const int e = up ? 1 : 0;
-      if ((sl & (LPR / 2 - 1)) == 0 && b0 + e < n) {
-        const int id = __ldg(p.ell_dvp_id + p0 + b0 + e);
-        if (id >= 0) p.dv_out[id] = t;
-      }
+      const int id = up ? id1 : id0;
+      if ((sl & (LPR / 2 - 1)) == 0 && id >= 0) p.dv_out[id] = t;
     }
-    mcur = mnext;
+    if (c0 + LPR < n) mcur = rec(c0 + LPR + sl);
   }
   if (p.ell_lazy_wait) griddep_wait();
+}
+
+// fourth word of every ELL record := the forward operator's id of its
+// nonzero (perm of the record's own id), -1 for padding
+__global__ void record_ids_kernel(int4* __restrict__ ent, const int* __restrict__ ids, long n,
+                                  const int* __restrict__ perm) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int v = ids[i];
+  ent[i].w = v >= 0 ? perm[v] : -1;
+}
+
+cudaError_t launch_record_ids(int4* ent, const int* ids, long n, const int* perm, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  record_ids_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ent, ids, n, perm);
+  return cudaGetLastError();
 }
 
 __global__ void permute_ids_kernel(const int* __restrict__ in, long n, const int* __restrict__ perm,

@@ -80,14 +80,15 @@ struct SpmmArgs {
   // out and the kernel returns with the error flag set
   int stall_test;
   // fused backward (this plan is the transposed operator's): the ELL pass
-  // that computes dB = A^T dC also writes dvals[ell_dvp_id[s]] =
-  // <dC[col], dvx[row]> for its entries (dvx: the forward's dense operand),
-  // and the run list's tensor-core prefix (dv_n_groups_tc groups) gives the
-  // rest with ids dvp_id; ids in the forward operator's nonzero numbering
+  // that computes dB = A^T dC also writes dvals[id] = <dC[col], dvx[row]>
+  // for its entries, id in the fourth word of each record (dvx: the
+  // forward's dense operand), and the run list's tensor-core prefix
+  // (dv_n_groups_tc groups) gives the rest with ids dvp_id; ids in the
+  // forward operator's nonzero numbering (set by set_transpose_ids)
   const float* dvx;
   long dvx_ld;
   float* dv_out;
-  const int* ell_dvp_id;
+  int ell_ids_set;
   const int* dvp_id;
   int dv_n_groups_tc;
 };
@@ -115,6 +116,8 @@ cudaError_t launch_ell(const SpmmArgs& p, cudaStream_t st);
 cudaError_t launch_ell_bwd(const SpmmArgs& p, cudaStream_t st);
 // out[i] = in[i] >= 0 ? perm[in[i]] : -1
 cudaError_t launch_permute_ids(const int* in, long n, const int* perm, int* out, cudaStream_t st);
+// ent[i].w = ids[i] >= 0 ? perm[ids[i]] : -1
+cudaError_t launch_record_ids(int4* ent, const int* ids, long n, const int* perm, cudaStream_t st);
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st);
 constexpr int kChunkSteps = 32;
 cudaError_t launch_pack_values(const SpmmArgs& p, const float* vals, long nnz, int heads, void* ell_out,
