@@ -55,6 +55,12 @@ class PlanConfig:
     # count-sorted tensor-core columns (the reference's reorder_k_by_nnz);
     # False: non-empty columns first, in column order
     reorder_k_by_nnz: bool = True
+    # the backward of an fp32 SpMM: "fused" (dB and the value gradients from
+    # one pass over the transposed plan's row tiles), "separate" (the
+    # transposed product, then the value-gradient pass over the forward
+    # tiles) or "auto" (the first backward of each width times both on its
+    # own operands and keeps the faster)
+    backward: str = "auto"
 
     def search_kwargs(self):
         cost = self.cost_model
@@ -106,6 +112,8 @@ class SpmmOperator:
         # (weak reference to the tensor, its version, its address) of the
         # values HybridSpMMFunction loaded last
         self._values_key = None
+        # backward variant chosen per dense width ("fused" / "separate")
+        self._bwd_choice = {}
 
     def __call__(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         return self.handle.run(B, out)
@@ -114,9 +122,46 @@ class SpmmOperator:
         return self.handle.dvals(dC, B)
 
     def backward(self, dC: torch.Tensor, B: torch.Tensor, dB: torch.Tensor | None = None):
-        """(dB = A^T @ dC, dvals = <dC[row], B[col]> on A's pattern) in one
-        pass over the transposed plan's row tiles (fp32 dC and B)."""
-        return self.transposed[0].handle.backward(dC, B, dB)
+        """(dB = A^T @ dC, dvals = <dC[row], B[col]> on A's pattern), fp32 dC
+        and B: fused (one pass over the transposed plan's row tiles) or
+        separate (transposed product, then the value-gradient pass), as
+        ``cfg.backward`` says; "auto" times both once per width."""
+        opT, _ = self.transposed
+        choice = self.cfg.backward
+        if choice == "auto":
+            choice = self._bwd_choice.get(int(B.shape[1]))
+            if choice is None:
+                choice = self._tune_backward(opT, dC, B)
+                self._bwd_choice[int(B.shape[1])] = choice
+        if choice == "fused":
+            return opT.handle.backward(dC, B, dB)
+        dvals = self.handle.dvals(dC, B)
+        return opT.handle.run(dC, dB), dvals
+
+    def _tune_backward(self, opT, dC, B, reps=3):
+        """The faster backward variant on these operands: each runs once to
+        warm up, then ``reps`` times between CUDA events; the median wins."""
+        import statistics
+
+        def fused():
+            opT.handle.backward(dC, B)
+
+        def separate():
+            self.handle.dvals(dC, B)
+            opT.handle.run(dC)
+        times = {}
+        for name, fn in (("fused", fused), ("separate", separate)):
+            fn()
+            ts = []
+            for _ in range(reps):
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record()
+                fn()
+                e.record()
+                e.synchronize()
+                ts.append(s.elapsed_time(e))
+            times[name] = statistics.median(ts)
+        return min(times, key=times.get)
 
     def batched(self, vals: torch.Tensor, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """C[h] = A(vals[h]) @ B[h] for H value sets on A's pattern (vals
@@ -321,7 +366,7 @@ class HybridSpMMFunction(torch.autograd.Function):
         # 16-byte aligned base need no copy; ops.dense_operand copies others)
         dvals = dB = None
         if ctx.needs_input_grad[0] and ctx.needs_input_grad[1] and B.dtype == torch.float32:
-            # both gradients from one pass over the transposed plan's tiles
+            # both gradients (fused or separate, as the operator chose)
             dB, dvals = op.backward(dC, B)
             return dvals, dB, None
         if ctx.needs_input_grad[0]:

@@ -261,7 +261,7 @@ def test_fused_backward_matches_separate_passes_and_fp64(N, mode, pattern):
         A = _graph(seed=15)
     else:
         A = syn.power_law_rows(3000, 2200, min_len=2, max_len=300, seed=16)
-    op = plan_spmm(A, N, PlanConfig(tc_mode=mode))
+    op = plan_spmm(A, N, PlanConfig(tc_mode=mode, backward="fused"))
     rng = np.random.default_rng(17)
     B = rng.standard_normal((A.shape[1], N)).astype(np.float32)
     dC = rng.standard_normal((A.shape[0], N)).astype(np.float32)
@@ -277,3 +277,21 @@ def test_fused_backward_matches_separate_passes_and_fp64(N, mode, pattern):
     tol = 1e-2 if mode == D.TC_BF16 else 1e-5
     assert S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC, B)) <= 1e-5
     assert S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(op.A.T.tocsr(), dC)) <= tol
+
+
+def test_backward_auto_choice_is_timed_once_per_width_and_correct():
+    """backward="auto": the first backward of a width times the fused and the
+    separate variant on its operands, keeps the faster for later calls, and
+    the result matches float64 either way."""
+    A = _graph(seed=18)
+    op = plan_spmm(A, 64, PlanConfig(tc_mode=D.TC_SPLIT_BF16))
+    rng = np.random.default_rng(19)
+    B = rng.standard_normal((A.shape[1], 64)).astype(np.float32)
+    dC = rng.standard_normal((A.shape[0], 64)).astype(np.float32)
+    Bt, dCt = torch.as_tensor(B, device="cuda"), torch.as_tensor(dC, device="cuda")
+    for _ in range(2):
+        dB, dv = op.backward(dCt, Bt)
+        assert op._bwd_choice[64] in ("fused", "separate")
+        assert S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC, B)) <= 1e-5
+        assert S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(op.A.T.tocsr(), dC)) <= 1e-5
+    assert list(op._bwd_choice) == [64]
