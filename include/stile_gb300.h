@@ -56,6 +56,8 @@ extern "C" {
 #define STILE_TC_BF16 1        /* A, B rounded to bf16, fp32 accumulate */
 #define STILE_TC_F16 2         /* A, B rounded to fp16, fp32 accumulate */
 #define STILE_TC_SPLIT_BF16 4  /* hi+lo bf16 split of A and B, 4 products */
+#define STILE_TC_FP8 3         /* A e4m3 (per-tensor scale), B e4m3 (per tile-row
+                                  scale), fp32 accumulate; fp32 B operands */
 
 
 /*
@@ -67,7 +69,10 @@ extern "C" {
  * image of one tcgen05.mma B operand (K-major, no swizzle):
  *   element (row n, col k) at byte (n/8)*256 + (k/8)*128 + (n%8)*16 + (k%8)*2
  * for 16-bit modes (bf16 / fp16); STILE_TC_SPLIT_BF16 stores the hi image
- * followed by the lo image (1024 B per k-step).
+ * followed by the lo image (1024 B per k-step).  STILE_TC_FP8 stores, per
+ * k-step, the e4m3 bytes of value / tc_row_scale[item * 16 + n] as a K = 32
+ * operand whose upper 16 k are zero: byte (n/8)*256 + (k/16)*128 +
+ * (n%8)*16 + k%16 (512 B per k-step).
  *
  * ELL items: one per row-bucket tile; rows [ell_item_row0[i],
  * ell_item_row0[i+1]), every row with ell_item_K[i] slots starting at
@@ -101,6 +106,8 @@ typedef struct StileSpmmPlanHost {
   int32_t n_zero_rows;
   const int32_t* zero_rows;      /* [n_zero_rows] */
   int64_t nnz;                   /* nonzeros of the pattern (dvals length) */
+  const float* tc_row_scale;     /* [tc_n_items * 16] STILE_TC_FP8: scale of every
+                                    tensor-tile row (its largest |value| / 448); else NULL */
 } StileSpmmPlanHost;
 
 /*
@@ -324,7 +331,7 @@ int stile_spmm_plan_set_wait_policy(StileSpmmPlan* plan, int32_t polls, int32_t 
 
 /* Tensor-core layout self-check (no counterpart in the reference): runs one
  * tcgen05.mma (M=128, N=16; kind = 0: kind::f16, K=16; kind = 1:
- * kind::tf32, K=8; fp32 accumulate) on two 8 KB shared-memory images copied
+ * kind::tf32, K=8; kind = 2: kind::f8f6f4, K=32; fp32 accumulate) on two 8 KB shared-memory images copied
  * verbatim from a_img / b_img, with descriptor fields desc6 = {a_lbo, a_sbo,
  * a_layout, b_lbo, b_sbo, b_layout} (bytes, multiples of 16, <= 2048) and
  * instruction descriptor idesc; writes the 128x16 fp32 accumulator row-major

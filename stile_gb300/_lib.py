@@ -89,6 +89,7 @@ class SpmmPlanHost(ctypes.Structure):
         ("ell_vals", c_f32p), ("ell_kidx", c_i32p), ("ell_nnz_id", c_i32p),
         ("n_zero_rows", ctypes.c_int32), ("zero_rows", c_i32p),
         ("nnz", ctypes.c_int64),
+        ("tc_row_scale", c_f32p),
     ]
 
 

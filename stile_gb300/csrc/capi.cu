@@ -88,8 +88,14 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
     return fail(STILE_E_INVALID, "negative count");
   const int mode = h->tc_mode;
   if (h->tc_n_items > 0) {
-    if (mode != STILE_TC_BF16 && mode != STILE_TC_F16 && mode != STILE_TC_SPLIT_BF16)
+    if (mode != STILE_TC_BF16 && mode != STILE_TC_F16 && mode != STILE_TC_SPLIT_BF16 && mode != STILE_TC_FP8)
       return fail(STILE_E_UNSUPPORTED, "tensor-tile mode not supported by this build");
+    if (mode == STILE_TC_FP8) {
+      if (!h->tc_row_scale) return fail(STILE_E_INVALID, "fp8 tensor tiles need tc_row_scale");
+      for (long i = 0; i < (long)h->tc_n_items * 16; ++i)
+        if (!(h->tc_row_scale[i] > 0.f) || !(h->tc_row_scale[i] < 3.0e38f))
+          return fail(STILE_E_INVALID, "tc_row_scale must be positive and finite");
+    }
     const int want = (mode == STILE_TC_SPLIT_BF16) ? 1024 : 512;
     if (h->tc_kstep_bytes != want) return fail(STILE_E_INVALID, "tc_kstep_bytes does not match mode");
     if (!h->tc_item_kbeg || !h->tc_item_flags || !h->tc_out_rows || !h->tc_cols || !h->tc_vals)
@@ -442,6 +448,9 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   size_t i_dvgp = ar.add(dv_gptr.data(), dv_gptr.size() * 4);
   size_t i_dvgr = ar.add(dv_grow.data(), dv_grow.size() * 4);
   size_t i_err = ar.add(nullptr, 16);
+  const bool fp8 = mode == STILE_TC_FP8 && h->tc_n_items > 0;
+  size_t i_rsc = ar.add(fp8 ? h->tc_row_scale : nullptr, fp8 ? (size_t)h->tc_n_items * 16 * 4 : 0);
+  size_t i_amax = ar.add(nullptr, 16);
 
   auto* plan = new StileSpmmPlan();
   cudaError_t e = cudaMalloc(&plan->arena, ar.total ? ar.total : 256);
@@ -485,6 +494,8 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   a.ell_entry = (const int4*)P(i_eent);
   a.ell_nnz_id = h->ell_nnz_id ? (const int*)P(i_enid) : nullptr;
   a.err_flag = plan->err_flag;
+  a.tc_row_scale = fp8 ? (const float*)P(i_rsc) : nullptr;
+  a.tc_xamax = (unsigned*)(base + ar.offs[i_amax]);
   plan->M = h->M;
   plan->K = h->K;
   plan->nnz = h->nnz;
@@ -572,6 +583,17 @@ static int spmm_run(const StileSpmmPlan* plan, const void* B, bool b_bf16, int64
   if ((rc = check_dense(ldc, N, C, "C")) != 0) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e;
+  const bool fp8 = plan->args.tc_n_chunks && plan->args.tc_mode == STILE_TC_FP8;
+  if (fp8) {
+    if (hd.n > 0) return fail(STILE_E_UNSUPPORTED, "fp8 tensor tiles take one value set");
+    // B's e4m3 scale: max |B| over the run's operand, by an ordinary launch
+    // that every later kernel of the run starts after
+    e = cudaMemsetAsync(plan->args.tc_xamax, 0, 4, st);
+    if (e == cudaSuccess)
+      e = stile::launch_amax(static_cast<const float*>(B), ldb, plan->K, N, plan->args.tc_xamax, st);
+    if (e != cudaSuccess) return cuda_fail(e, "amax launch");
+    g_launches++;
+  }
   // rows without an owned writer start at zero; when they are the majority,
   // one strided memset of C is cheaper than the row list (owned rows are
   // overwritten by their writer anyway)
@@ -638,6 +660,8 @@ int64_t stile_spmm_values_bytes(const StileSpmmPlan* plan, int32_t heads) {
 
 int stile_spmm_values_pack(const StileSpmmPlan* plan, const float* vals, int32_t heads, void* packed, void* stream) {
   if (!plan || heads < 0) return fail(STILE_E_INVALID, "bad arguments");
+  if (plan->args.tc_n_chunks && plan->args.tc_mode == STILE_TC_FP8)
+    return fail(STILE_E_UNSUPPORTED, "fp8 tensor tiles take one value set (their scales come with the plan)");
   if (heads == 0) return STILE_OK;
   if (!vals || !packed) return fail(STILE_E_INVALID, "null argument");
   if ((reinterpret_cast<uintptr_t>(packed) & 255) != 0) return fail(STILE_E_INVALID, "packed: must be 256-byte aligned");
@@ -790,6 +814,8 @@ int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t ldd
 
 int stile_spmm_plan_set_values(StileSpmmPlan* plan, const float* vals, void* stream) {
   if (!plan || !vals) return fail(STILE_E_INVALID, "null argument");
+  if (plan->args.tc_n_chunks && plan->args.tc_mode == STILE_TC_FP8)
+    return fail(STILE_E_UNSUPPORTED, "fp8 tensor tiles: new values need a new upload (their row scales change)");
   if ((plan->args.tc_n_items && !plan->args.tc_nnz_id) ||
       (plan->args.ell_n_groups && !plan->args.ell_nnz_id))
     return fail(STILE_E_INVALID, "plan was uploaded without nonzero ids");
@@ -1002,7 +1028,8 @@ int stile_debug_umma_probe(const void* a_img, const void* b_img, const uint32_t*
       return fail(STILE_E_INVALID, "probe strides must be multiples of 16 and <= 2048");
     if (lay != 0 && lay != 2 && lay != 4 && lay != 6) return fail(STILE_E_INVALID, "bad layout type");
   }
-  if (kind != 0 && kind != 1) return fail(STILE_E_INVALID, "kind must be 0 (f16) or 1 (tf32)");
+  if (kind != 0 && kind != 1 && kind != 2)
+    return fail(STILE_E_INVALID, "kind must be 0 (f16), 1 (tf32) or 2 (f8f6f4)");
   cudaError_t e = stile::launch_umma_probe(a_img, b_img, desc6, idesc, (uint32_t)kind, out, err,
                                            static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "probe launch");

@@ -290,6 +290,18 @@ __device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t adesc, uint6
       : "memory");
 }
 
+// D[tmem] (+)= A[smem] * B[smem], kind::f8f6f4 (e4m3 inputs here, fp32
+// accumulate); K = 32 per instruction
+__device__ __forceinline__ void umma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                        uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 // arrive on an mbarrier once all previously issued tcgen05 ops of this thread finish
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile(
@@ -327,8 +339,9 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;
 }
 
-// Instruction descriptor for kind::f16 / kind::tf32 with fp32 accumulate.
-// a_fmt/b_fmt: kind::f16 -> 0 = f16, 1 = bf16; kind::tf32 -> 2.
+// Instruction descriptor for kind::f16 / kind::tf32 / kind::f8f6f4 with fp32
+// accumulate.  a_fmt/b_fmt: kind::f16 -> 0 = f16, 1 = bf16; kind::tf32 -> 2;
+// kind::f8f6f4 -> 0 = e4m3.
 // a_mn_major / b_mn_major: 1 = MN-major operand, 0 = K-major.
 __host__ __device__ constexpr uint32_t make_idesc(uint32_t a_fmt, uint32_t b_fmt,
                                                   uint32_t a_mn_major, uint32_t b_mn_major,
@@ -342,6 +355,14 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<uint32_t*>(&v);
 }
+// two floats -> two e4m3 bytes (round to nearest even, saturated to +-448),
+// lo in the low byte
+__device__ __forceinline__ uint32_t pack_e4m3x2(float lo, float hi) {
+  unsigned short d;
+  asm("cvt.rn.satfinite.e4m3x2.f32 %0, %1, %2;" : "=h"(d) : "f"(hi), "f"(lo));
+  return (uint32_t)d;
+}
+
 __device__ __forceinline__ uint32_t pack_f16x2(float lo, float hi) {
   __half2 v = __floats2half2_rn(lo, hi);
   return *reinterpret_cast<uint32_t*>(&v);

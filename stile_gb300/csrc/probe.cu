@@ -1,6 +1,7 @@
 // Layout self-check for the tensor-core path: one CTA copies two operand
 // images verbatim into shared memory, issues one tcgen05.mma (M=128, N=16;
-// kind::f16 with K=16 or kind::tf32 with K=8; fp32 accumulate) with
+// kind::f16 with K=16, kind::tf32 with K=8 or kind::f8f6f4 with K=32; fp32
+// accumulate) with
 // caller-chosen descriptor fields and
 // writes the 128x16 accumulator to global memory.  Every descriptor the
 // caller can pass stays inside the CTA's shared memory: each operand gets a
@@ -50,7 +51,9 @@ __global__ void __launch_bounds__(128) umma_probe_kernel(const uint4* __restrict
   asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(slot) : "memory");
   if (tid == 0) {
     const uint64_t ad = smem_desc(sa, a_lbo, a_sbo, a_layout), bd = smem_desc(sb, b_lbo, b_sbo, b_layout);
-    if (kind == 1) umma_tf32(tmem, ad, bd, idesc, 0u); else umma_f16(tmem, ad, bd, idesc, 0u);
+    if (kind == 1) umma_tf32(tmem, ad, bd, idesc, 0u);
+    else if (kind == 2) umma_f8(tmem, ad, bd, idesc, 0u);
+    else umma_f16(tmem, ad, bd, idesc, 0u);
     umma_commit(bar);
   }
   const bool done = __syncthreads_and(mbar_wait_bounded(bar, 0)) != 0;

@@ -150,6 +150,11 @@ constexpr uint32_t kBStage = 512;    // bytes of one B image (16-bit)
 constexpr uint32_t kALbo = 2048, kASbo = 1024;
 constexpr uint32_t kBLbo = 128, kBSbo = 256;
 constexpr uint32_t kRawRows = 8192;  // 16 rows x 128 fp32 per stage
+// fp8 operands (K = 32 bytes, K-major, no swizzle): core matrices of 8 rows
+// x 16 bytes, the two k halves 128 B apart (LBO), 8-row groups 256 B apart
+// (SBO); the A image is 4 KB, a k-step's value image 512 B
+constexpr uint32_t kF8Lbo = 128, kF8Sbo = 256;
+constexpr float kE4m3Max = 448.f;
 
 __device__ __forceinline__ uint32_t a_img_off(int m, int k) {
   // m: feature (0..127), k: column within the k-step (0..15)
@@ -246,6 +251,13 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
     }
     mbar_init(drain, 1);
     fence_mbar_init();
+  }
+  if constexpr (MODE == STILE_TC_FP8) {
+    // the A images' upper k halves stay zero (each k-step fills the lower
+    // half of a K = 32 operand); made visible to the tensor core's proxy
+    for (int i = tid; i < (int)(kWsSlots * W::kAImg / 16); i += kWsThreads)
+      st_shared_v4(slots + W::a_off(0) + 16 * i, make_uint4(0u, 0u, 0u, 0u));
+    fence_proxy_async_smem();
   }
   if (warp == 0) {
     __syncwarp();
@@ -353,6 +365,14 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
       }
       cp_async_wait<0>();
     } else {
+    // fp8: B's e4m3 scale comes from the run's amax pass, which finished
+    // before this kernel started (an ordinary launch never lets a dependent
+    // start early)
+    float xinv = 1.f;
+    if constexpr (MODE == STILE_TC_FP8) {
+      const float amax = __uint_as_float(*p.tc_xamax);
+      xinv = amax > 0.f ? kE4m3Max / amax : 0.f;
+    }
     auto issue = [&](int cols, int l, int ff) {
       const int f = ff + 4 * lane;
       const uint32_t bytes = kFull ? 16u : ((f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u));
@@ -388,8 +408,31 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
         if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par, polls);  // completed: returns at once
       }
       const uint32_t sa = slots + W::a_off(slot);
+      if constexpr (MODE == STILE_TC_FP8) {
+        // this lane's 4 features x the step's 16 rows -> four K-major
+        // 16-byte rows of the A image (feature m: the e4m3 bytes of x / s_x
+        // for k = 0..15), core matrices of 8 features x 16 bytes
+        uint32_t wd[4][4];
 #pragma unroll
-      for (int r = 0; r < 16; ++r) {
+        for (int r = 0; r < 16; r += 2) {
+          const uint4 ra = ld_shared_v4(stage + r * 512 + lane * 16);
+          const uint4 rb = ld_shared_v4(stage + (r + 1) * 512 + lane * 16);
+          const uint32_t ua[4] = {ra.x, ra.y, ra.z, ra.w}, ub[4] = {rb.x, rb.y, rb.z, rb.w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const uint32_t h = pack_e4m3x2(__uint_as_float(ua[j]) * xinv, __uint_as_float(ub[j]) * xinv);
+            if ((r & 2) == 0) wd[j][r >> 2] = h; else wd[j][r >> 2] |= h << 16;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int m = 4 * lane + j;
+          st_shared_v4(sa + (uint32_t)((m >> 3) * kF8Sbo + (m & 7) * 16),
+                       make_uint4(wd[j][0], wd[j][1], wd[j][2], wd[j][3]));
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < (MODE == STILE_TC_FP8 ? 0 : 16); ++r) {
         const uint4 raw = ld_shared_v4(stage + r * 512 + lane * 16);
         const float4 v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y), __uint_as_float(raw.z),
                                      __uint_as_float(raw.w));
@@ -422,8 +465,10 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
   } else if (warp == kProdWarps) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const uint32_t idesc = (MODE == STILE_TC_F16) ? make_idesc(0, 0, 1, 0, 128, 16)
-                                                    : make_idesc(1, 1, 1, 0, 128, 16);
+      // fp8: e4m3 x e4m3, both operands K-major
+      const uint32_t idesc = (MODE == STILE_TC_F16)   ? make_idesc(0, 0, 1, 0, 128, 16)
+                             : (MODE == STILE_TC_FP8) ? make_idesc(0, 0, 0, 0, 128, 16)
+                                                      : make_idesc(1, 1, 1, 0, 128, 16);
       long g = 0;
       int u = 0;  // accumulation groups issued so far (accumulator u % kAccBufs)
       // failure-detection test: nothing arrives on `drain` before the
@@ -453,7 +498,11 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
             const uint32_t sa = slots + W::a_off(slot), sv = slots + W::v_off(slot);
             const uint64_t a_hi = smem_desc(sa, kALbo, kASbo, kSwizzle128B);
             const uint64_t v_hi = smem_desc(sv, kBLbo, kBSbo, kSwizzleNone);
-            umma_f16(d, a_hi, v_hi, idesc, s > s0 ? 1u : 0u);
+            if constexpr (MODE == STILE_TC_FP8)
+              umma_f8(d, smem_desc(sa, kF8Lbo, kF8Sbo, kSwizzleNone), smem_desc(sv, kF8Lbo, kF8Sbo, kSwizzleNone),
+                      idesc, s > s0 ? 1u : 0u);
+            else
+              umma_f16(d, a_hi, v_hi, idesc, s > s0 ? 1u : 0u);
             if (W::kSplit) {
               umma_f16(d, a_hi, smem_desc(sv + kBStage, kBLbo, kBSbo, kSwizzleNone), idesc, 1u);
               umma_f16(d, smem_desc(sa + kAStage, kALbo, kASbo, kSwizzle128B), v_hi, idesc, 1u);
@@ -509,6 +558,12 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
         const int item = __ldg(p.tc_chunk_item + c);
         const bool atomic = (__ldg(p.tc_chunk_flags + c) & 1) != 0;
         const int* orows = p.tc_out_rows + (long)item * 16;
+        if constexpr (MODE == STILE_TC_FP8) {
+          // undo the scales: B's (per tensor) and the tile row's
+          const float sx = __uint_as_float(*p.tc_xamax) / kE4m3Max;
+#pragma unroll
+          for (int i = 0; i < 16; ++i) acc[i] *= sx * __ldg(p.tc_row_scale + (long)item * 16 + i);
+        }
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           const int row = __ldg(orows + i);
@@ -928,6 +983,27 @@ __global__ void pack_values_kernel(SpmmArgs p, const float* __restrict__ vals, l
   }
 }
 
+// bits of max |B| over K rows x N features into *out (atomicMax on the bits
+// of non-negative floats, which order like the floats)
+__global__ void amax_kernel(const float* __restrict__ B, long ldb, int K, int N, unsigned* __restrict__ out) {
+  float m = 0.f;
+  const long total = (long)K * N;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(B[(i / N) * ldb + i % N]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(out, __float_as_uint(m));
+}
+
+cudaError_t launch_amax(const float* B, long ldb, int K, int N, unsigned* amax_bits, cudaStream_t st) {
+  const long total = (long)K * N;
+  if (total == 0) return cudaSuccess;
+  const long cap = (long)device_sm_count() * 8;
+  const long grid = std::min((total + 255) / 256, cap);
+  amax_kernel<<<(unsigned)grid, 256, 0, st>>>(B, ldb, K, N, amax_bits);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pack_values(const SpmmArgs& p, const float* vals, long nnz, int heads, void* ell_out,
                                void* tc_out, long n_ell, long tc_head_bytes, cudaStream_t st) {
   const long total = (long)p.tc_n_ksteps * 256 + n_ell;
@@ -1094,6 +1170,8 @@ cudaError_t launch_tc(const SpmmArgs& args, cudaStream_t st) {
   switch (p.tc_mode) {
     case STILE_TC_F16:
       return p.N % 128 == 0 ? launch_ws_t<STILE_TC_F16, true>(p, st) : launch_ws_t<STILE_TC_F16, false>(p, st);
+    case STILE_TC_FP8:
+      return p.N % 128 == 0 ? launch_ws_t<STILE_TC_FP8, true>(p, st) : launch_ws_t<STILE_TC_FP8, false>(p, st);
     case STILE_TC_SPLIT_BF16:
       return p.N % 128 == 0 ? launch_ws_t<STILE_TC_SPLIT_BF16, true>(p, st)
                             : launch_ws_t<STILE_TC_SPLIT_BF16, false>(p, st);

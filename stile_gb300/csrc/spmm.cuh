@@ -47,6 +47,11 @@ struct SpmmArgs {
   const int* tc_cols;
   const void* tc_vals;
   const int* tc_nnz_id;
+  // STILE_TC_FP8: scale of every (item, row) and the device word that holds
+  // the bits of max |B| of the run (written by an amax pass before the
+  // kernels; B's e4m3 scale is that / 448)
+  const float* tc_row_scale;
+  unsigned* tc_xamax;
   // ELL tiles, compacted at upload into a stream of live entries in row
   // order, cut into groups of at most kSegNnz entries at row boundaries
   // (rows longer than that are split into atomic pieces of their own)
@@ -123,6 +128,9 @@ constexpr int kChunkSteps = 32;
 cudaError_t launch_pack_values(const SpmmArgs& p, const float* vals, long nnz, int heads, void* ell_out,
                                void* tc_out, long n_ell, long tc_head_bytes, cudaStream_t st);
 cudaError_t launch_repack(const SpmmArgs& p, const float* vals, long n_ell_slots, cudaStream_t st);
+// *amax_bits = bits of max |B[r][f]| over K rows x N features (atomicMax on
+// the non-negative floats' bits; *amax_bits starts at 0); an ordinary launch
+cudaError_t launch_amax(const float* B, long ldb, int K, int N, unsigned* amax_bits, cudaStream_t st);
 
 struct SddmmArgs {
   const float* X;  // fp32, or bf16 bits when xy_bf16 (X and Y alike)

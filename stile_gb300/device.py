@@ -22,7 +22,7 @@ column) for every live entry; the reference plans on the 0/1 pattern.
 """
 from __future__ import annotations
 
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 import scipy.sparse as sp
@@ -30,7 +30,8 @@ import scipy.sparse as sp
 from .emit import emit_sddmm_reference, emit_spmm_reference
 from .plan import ELL, ONE_D, TC, TC_SDDMM
 
-TC_BF16, TC_F16, TC_SPLIT_BF16 = 1, 2, 4
+TC_BF16, TC_F16, TC_FP8, TC_SPLIT_BF16 = 1, 2, 3, 4
+E4M3_MAX = 448.0
 
 
 class ValueIndex:
@@ -88,6 +89,42 @@ def operand_image_16bit(vals16):
     return np.ascontiguousarray(v.reshape(nk, 256))
 
 
+def to_e4m3(x):
+    """float32 -> (e4m3 bytes, the e4m3 values as float32): round to nearest
+    even, saturated to +-448."""
+    import torch
+    t = torch.as_tensor(np.ascontiguousarray(x, np.float32)).clamp(-E4M3_MAX, E4M3_MAX).to(torch.float8_e4m3fn)
+    return t.view(torch.uint8).numpy(), t.to(torch.float32).numpy()
+
+
+def operand_image_e4m3(bytes16):
+    """[n_ksteps, 16 (n), 16 (k)] e4m3 bytes -> [n_ksteps, 512] K-major,
+    no-swizzle image of a K = 32 operand whose upper 16 k are zero: core
+    matrices of 8 rows x 16 bytes, element (n, k) at byte (n//8)*256 +
+    (k//16)*128 + (n%8)*16 + k%16."""
+    nk = bytes16.shape[0]
+    img = np.zeros((nk, 2, 2, 8, 16), dtype=np.uint8)     # (ks, n_grp, k_half, n_in, k_in)
+    img[:, :, 0] = bytes16.reshape(nk, 2, 8, 16)
+    return np.ascontiguousarray(img.reshape(nk, 512))
+
+
+def fp8_row_scales(vals_f, kbeg):
+    """Per (tensor-core item, row) scale: the largest |value| of the row over
+    the item's k-steps / 448 (1 for an empty row).  [n_items * 16] float32."""
+    n_items = len(kbeg) - 1
+    out = np.ones((n_items, 16), dtype=np.float32)
+    if n_items == 0 or len(vals_f) == 0:
+        return out.reshape(-1)
+    rowmax = np.abs(vals_f).max(axis=2)                  # [n_ks, 16]
+    starts = np.asarray(kbeg[:-1], dtype=np.int64)
+    nonempty = np.diff(kbeg) > 0
+    red = np.maximum.reduceat(rowmax, np.minimum(starts, len(rowmax) - 1), axis=0)
+    red[~nonempty] = 0.0
+    s = red / E4M3_MAX
+    out = np.where(s > 0, s, 1.0).astype(np.float32)
+    return out.reshape(-1)
+
+
 @dataclass
 class SpmmDevice:
     M: int
@@ -112,6 +149,8 @@ class SpmmDevice:
     ell_kidx: np.ndarray
     ell_nnz_id: np.ndarray
     zero_rows: np.ndarray
+    # fp8 tensor tiles: scale of every (item, row) (empty otherwise)
+    tc_row_scale: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
 
     def stats(self):
         return {"tc_items": int(len(self.tc_item_flags)), "tc_ksteps": int(len(self.tc_cols) // 16),
@@ -206,6 +245,13 @@ def build_spmm_device(tiles, A, N=32, tc_mode=TC_BF16, emitted=None):
         img = np.concatenate([operand_image_16bit(hi.reshape(n_ks, 16, 16)),
                               operand_image_16bit(lo.reshape(n_ks, 16, 16))], axis=1)
         tc_bytes = 1024
+    elif tc_mode == TC_FP8:
+        row_scale = fp8_row_scales(vals_f, np.asarray(kbeg, dtype=np.int64))
+        item_of = np.repeat(np.arange(len(kbeg) - 1), np.diff(np.asarray(kbeg, dtype=np.int64)))
+        s = row_scale.reshape(-1, 16)[item_of] if n_ks else np.ones((0, 16), np.float32)
+        b8, _ = to_e4m3(vals_f / s[:, :, None] if n_ks else vals_f)
+        img = operand_image_e4m3(b8.reshape(n_ks, 16, 16))
+        tc_bytes = 512
     else:
         raise ValueError(f"unsupported tensor-tile mode {tc_mode}")
     tc_vals = np.ascontiguousarray(img).view(np.uint8).reshape(-1)
@@ -287,7 +333,8 @@ def build_spmm_device(tiles, A, N=32, tc_mode=TC_BF16, emitted=None):
         ell_item_row0=np.asarray(row0, dtype=np.int32), ell_item_K=np.asarray(eK, dtype=np.int32),
         ell_item_slot0=np.asarray(eslot, dtype=np.int32), ell_item_flags=ell_flags,
         ell_out_row=ell_out, ell_row_len=cat(elen, np.int32), ell_vals=cat(evals, np.float32),
-        ell_kidx=cat(ekidx, np.int32), ell_nnz_id=cat(enid, np.int32), zero_rows=zero_rows)
+        ell_kidx=cat(ekidx, np.int32), ell_nnz_id=cat(enid, np.int32), zero_rows=zero_rows,
+        tc_row_scale=row_scale if tc_mode == TC_FP8 else np.zeros(0, np.float32))
 
 
 @dataclass

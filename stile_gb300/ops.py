@@ -112,6 +112,8 @@ def spmm_plan_host(dev: SpmmDevice):
     h.ell_nnz_id = _ptr(dev.ell_nnz_id)
     h.n_zero_rows = len(dev.zero_rows)
     h.zero_rows = _ptr(dev.zero_rows)
+    keep.append(dev.tc_row_scale)
+    h.tc_row_scale = _ptr(dev.tc_row_scale, ctypes.c_float)
     return h, keep
 
 

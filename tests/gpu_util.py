@@ -120,3 +120,41 @@ def run_probe_tf32(A, Bm, desc6=(128, 256, 0, 128, 256, 0), a_kmajor=True):
 def tf32_trunc(x):
     b = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32) & np.uint32(0xFFFFE000)
     return b.view(np.float32)
+
+
+def e4m3_round(x):
+    """float32 values rounded to the nearest e4m3 value (saturated to
+    +-448), kept as float32, and their e4m3 bytes."""
+    import torch
+    t = torch.as_tensor(np.asarray(x, np.float32)).clamp(-448.0, 448.0).to(torch.float8_e4m3fn)
+    return t.to(torch.float32).numpy(), t.view(torch.uint8).numpy()
+
+
+def kmajor_image_8bit(bytes_rk):
+    """[rows, 32 (k)] bytes -> K-major, no-swizzle tcgen05 operand image:
+    core matrices of 8 rows x 16 bytes, the two k halves 128 B apart (LBO),
+    8-row groups 256 B apart (SBO)."""
+    rows = bytes_rk.shape[0]
+    img = np.zeros(8192, dtype=np.uint8)
+    for r in range(rows):
+        for k in range(32):
+            img[(r // 8) * 256 + (k // 16) * 128 + (r % 8) * 16 + k % 16] = bytes_rk[r, k]
+    return img
+
+
+def run_probe_f8(Abytes, Bbytes):
+    """One kind::f8f6f4 MMA (e4m3 x e4m3, K = 32) on K-major images."""
+    import torch
+    from stile_gb300 import _lib
+    lib = _lib.load()
+    ai = torch.as_tensor(kmajor_image_8bit(Abytes), device="cuda")
+    bi = torch.as_tensor(kmajor_image_8bit(Bbytes), device="cuda")
+    out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    d = (ctypes.c_uint32 * 6)(128, 256, 0, 128, 256, 0)
+    idesc = (1 << 4) | (0 << 7) | (0 << 10) | (0 << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
+    rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, 2, out.data_ptr(), err.data_ptr(),
+                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc, "probe")
+    torch.cuda.synchronize()
+    return out.cpu().numpy().reshape(128, 16), int(err.item())

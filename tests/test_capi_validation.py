@@ -84,7 +84,9 @@ SPMM_CASES = [
     ("negative_shape", None, lambda h: setattr(h, "M", -1), INVALID, "negative shape"),
     ("negative_count", None, lambda h: setattr(h, "ell_n_slots", -3), INVALID, "negative count"),
     ("unknown_tc_mode", None, lambda h: setattr(h, "tc_mode", 99), UNSUPPORTED, "mode not supported"),
-    ("mode_3_not_built", None, lambda h: setattr(h, "tc_mode", 3), UNSUPPORTED, "mode not supported"),
+    ("fp8_without_row_scales", None, lambda h: setattr(h, "tc_mode", 3), INVALID, "need tc_row_scale"),
+    ("fp8_bad_row_scale", lambda d: dataclasses.replace(d, tc_mode=3, tc_row_scale=np.full(
+        len(d.tc_item_flags) * 16, -1.0, np.float32)), None, INVALID, "positive and finite"),
     ("kstep_bytes", None, lambda h: setattr(h, "tc_kstep_bytes", 1024), INVALID, "tc_kstep_bytes"),
     ("missing_tc_array", None, lambda h: setattr(h, "tc_cols", None), INVALID, "missing tensor-tile array"),
     ("tc_kbeg_span", _set("tc_item_kbeg", _poke(-1, 0)), None, INVALID, "does not span the k-steps"),

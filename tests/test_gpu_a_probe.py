@@ -30,3 +30,17 @@ def test_umma_tf32_kmajor_layout():
     ref = A.astype(np.float64) @ Bm.astype(np.float64).T
     D, err = run_probe_tf32(A, Bm, (128, 256, 0, 128, 256, 0), a_kmajor=True)
     assert err == 0 and float(np.abs(D - ref).max()) < 1e-3
+
+
+def test_umma_f8_kmajor_layout():
+    """kind::f8f6f4 with e4m3 operands, both K-major without swizzle (core
+    matrices 8 rows x 16 B, the two 16-byte k halves 128 B apart, 8-row
+    groups 256 B apart): the layout of the fp8 tensor tiles.  Products of
+    e4m3 values are exact in fp32, so the MMA equals float64 closely."""
+    from gpu_util import e4m3_round, run_probe_f8
+    rng = np.random.default_rng(8)
+    A, Ab = e4m3_round(rng.standard_normal((128, 32)) * 4)
+    Bm, Bb = e4m3_round(rng.standard_normal((16, 32)) * 4)
+    ref = A.astype(np.float64) @ Bm.astype(np.float64).T
+    D, err = run_probe_f8(Ab, Bb)
+    assert err == 0 and float(np.abs(D - ref).max()) < 1e-3 * max(1.0, float(np.abs(ref).max()))
