@@ -903,6 +903,15 @@ def run_config(args):
                                     "bf16_B_forward_ms": timed(lambda: op_b(B16, out=C16), args.steps),
                                     "C_rel_fro": S.rel_fro(Cb.cpu().numpy(), S.spmm_fp64(A, B_np))}
             op_b.handle.close()
+            # fp8 e4m3 tensor tiles (per tile-row weight scales, per-tensor
+            # activation scale), the same plan, fp32 activations
+            op_f8 = SpmmOperator(A, N, PlanConfig(tc_mode=D.TC_FP8), plan=op.plan)
+            C8 = torch.empty_like(C)
+            op_f8(B, out=C8)
+            torch.cuda.synchronize()
+            out["fp8_tiles"] = {"forward_ms": timed(lambda: op_f8(B, out=C8), args.steps),
+                                **errors("C", C8.cpu().numpy(), S.spmm_fp64(A, B_np))}
+            op_f8.handle.close()
             # context: the zero-filled weight as a dense bf16 GEMM (cuBLAS
             # through torch.matmul, bf16 output) on the same activations
             Wd = torch.as_tensor(A.toarray(), device=dev).to(torch.bfloat16)

@@ -45,9 +45,11 @@ __device__ __forceinline__ float4 ld4_live(const float* row, int f, int N) {
   return v;
 }
 
+// Output rows are written once and not read again by the writing kernel:
+// streaming (evict-first) stores leave L2 to the gathered operand rows.
 __device__ __forceinline__ void st_row4(float* row, int f, int N, float4 v) {
   if (f + 3 < N) {
-    *reinterpret_cast<float4*>(row + f) = v;
+    __stcs(reinterpret_cast<float4*>(row + f), v);
   } else if (f < N) {
     row[f] = v.x;
     if (f + 1 < N) row[f + 1] = v.y;

@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(256, MINB) sddmm_run_kernel(int n_groups, cons
     }
 #pragma unroll
     for (int o = LPR / (2 * U); o > 0; o >>= 1) s[0] += __shfl_xor_sync(gmask, s[0], o);
-    if ((sl & (LPR / U - 1)) == 0 && b0 + e < p1) out[__ldg(outs + b0 + e)] = s[0];
+    if ((sl & (LPR / U - 1)) == 0 && b0 + e < p1) __stcs(out + __ldg(outs + b0 + e), s[0]);  // evict first
   }
 }
 

@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
           const int row = __ldg(orows + i);
           if (row < 0) continue;
           float* dst = p.C + blockIdx.z * p.c_head_stride + (long)row * p.ldc + f;
-          if (atomic) atomicAdd(dst, acc[i]); else *dst = acc[i];
+          if (atomic) atomicAdd(dst, acc[i]); else __stcs(dst, acc[i]);  // C is not read again: evict first
         }
       }
     }
@@ -622,7 +622,8 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   const int4* __restrict__ ent = p.ell_entry + head * p.ell_n_pos + p0;
   const int N = p.N;
   const int ldb32 = (int)p.ldb;
-  auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, 0); };
+  // records are read once: streaming loads leave L2 to the B rows
+  auto rec = [&](int i) { return i < n ? __ldcs(ent + i) : make_int4(0, 0, 0, 0); };
   for (int fc = kSpanY ? blockIdx.y * p.ell_fc_span : 0;
        fc < (kSpanY ? min(N, (int)(blockIdx.y + 1) * p.ell_fc_span) : N); fc += 4 * VEC * LPR) {
     const int f = fc + 4 * VEC * sl;
@@ -666,7 +667,7 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
               const int fw = f + 4 * w;
               if (code < 0 && p.ell_lazy_wait) griddep_wait();
               if (kFull) {
-                if (code >= 0) *reinterpret_cast<float4*>(row + fw) = acc[w];
+                if (code >= 0) __stcs(reinterpret_cast<float4*>(row + fw), acc[w]);  // evict first
                 else atomicAdd(reinterpret_cast<float4*>(row + fw), acc[w]);
               } else {
                 if (code >= 0) st_row4(row, fw, N, acc[w]); else red_row4(row, fw, N, acc[w]);
@@ -711,7 +712,7 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_bwd_kernel(SpmmArgs p) {
   const int4* __restrict__ ent = p.ell_entry + p0;
   const int N = p.N;
   const int f = 8 * sl;
-  auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, -1); };
+  auto rec = [&](int i) { return i < n ? __ldcs(ent + i) : make_int4(0, 0, 0, -1); };
   auto row_of = [](int ce) { const int code = ce >> 1; return code >= 0 ? code : -code - 1; };
   auto ld8 = [&](const float* row, float4& a, float4& b) {
     a = kFull ? ldg4(row + f) : ld4_live(row, f, N);
@@ -760,8 +761,8 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_bwd_kernel(SpmmArgs p) {
           if (code < 0 && p.ell_lazy_wait) griddep_wait();
           if (kFull) {
             if (code >= 0) {
-              *reinterpret_cast<float4*>(crow + f) = acc0;
-              *reinterpret_cast<float4*>(crow + f + 4) = acc1;
+              __stcs(reinterpret_cast<float4*>(crow + f), acc0);
+              __stcs(reinterpret_cast<float4*>(crow + f + 4), acc1);
             } else {
               atomicAdd(reinterpret_cast<float4*>(crow + f), acc0);
               atomicAdd(reinterpret_cast<float4*>(crow + f + 4), acc1);
@@ -783,7 +784,7 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_bwd_kernel(SpmmArgs p) {
 #pragma unroll
       for (int o = LPR / 4; o > 0; o >>= 1) t += __shfl_xor_sync(mask, t, o);
       const int id = up ? id1 : id0;
-      if ((sl & (LPR / 2 - 1)) == 0 && id >= 0) p.dv_out[id] = t;
+      if ((sl & (LPR / 2 - 1)) == 0 && id >= 0) __stcs(p.dv_out + id, t);
     }
     if (c0 + LPR < n) mcur = rec(c0 + LPR + sl);
   }
@@ -849,7 +850,8 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_seg_bf16_kernel(SpmmArgs p) {
   float* __restrict__ Ch = p.C + blockIdx.z * p.c_head_stride;
   const int N = p.N;
   const int ldb32 = (int)p.ldb;
-  auto rec = [&](int i) { return i < n ? __ldg(ent + i) : make_int4(0, 0, 0, 0); };
+  // records are read once: streaming loads leave L2 to the B rows
+  auto rec = [&](int i) { return i < n ? __ldcs(ent + i) : make_int4(0, 0, 0, 0); };
   for (int fc = kSpanY ? blockIdx.y * p.ell_fc_span : 0;
        fc < (kSpanY ? min(N, (int)(blockIdx.y + 1) * p.ell_fc_span) : N); fc += 8 * LPR) {
     const int f = fc + 8 * sl;
@@ -882,8 +884,8 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_seg_bf16_kernel(SpmmArgs p) {
             if (code < 0 && p.ell_lazy_wait) griddep_wait();
             if (kFull) {
               if (code >= 0) {
-                *reinterpret_cast<float4*>(row + f) = acc0;
-                *reinterpret_cast<float4*>(row + f + 4) = acc1;
+                __stcs(reinterpret_cast<float4*>(row + f), acc0);
+                __stcs(reinterpret_cast<float4*>(row + f + 4), acc1);
               } else {
                 atomicAdd(reinterpret_cast<float4*>(row + f), acc0);
                 atomicAdd(reinterpret_cast<float4*>(row + f + 4), acc1);
