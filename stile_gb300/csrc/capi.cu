@@ -780,8 +780,8 @@ int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t ldd
     // wider than one feature pass (or no row tiles): the transposed product,
     // then the gradient of every nonzero from the run list
     if ((rc = spmm_run(planT, dC, false, lddc, dB, lddb, N, stream)) != 0) return rc;
-    e = stile::launch_sddmm_runs(a.dv_n_groups, a.dv_gptr, a.dv_grow, a.dv_col, a.dvp_id, B, ldb, dC, false, lddc,
-                                 dvals, N, st);
+    e = stile::launch_sddmm_runs(a.dv_n_groups, a.dv_gptr, a.dv_grow, a.dv_col, a.dvp_id, B, false, ldb, dC, false,
+                                 lddc, dvals, N, st);
     if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
     g_launches += (a.dv_n_groups > 0);
     return STILE_OK;
@@ -805,8 +805,8 @@ int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t ldd
   if (a.tc_n_chunks) g_launches++;
   // the tensor-core nonzeros' gradients: the run list's tensor-core prefix
   // (rows of A^T hold B's rows, columns dC's)
-  e = stile::launch_sddmm_runs(a.dv_n_groups_tc, a.dv_gptr, a.dv_grow, a.dv_col, a.dvp_id, B, ldb, dC, false, lddc,
-                               dvals, N, st);
+  e = stile::launch_sddmm_runs(a.dv_n_groups_tc, a.dv_gptr, a.dv_grow, a.dv_col, a.dvp_id, B, false, ldb, dC, false,
+                               lddc, dvals, N, st);
   if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
   g_launches += (a.dv_n_groups_tc > 0);
   return STILE_OK;
@@ -929,6 +929,14 @@ int stile_sddmm_plan_upload(const StileSddmmPlanHost* h, StileSddmmPlan** out) {
         !in_range(h->blk_out, h->n_blk_nnz, 0, h->nnz))
       return fail(STILE_E_INVALID, "block index out of range");
   }
+  // the 1D entries as runs of one row, cut at stile::kRunGroup entries
+  std::vector<int32_t> run_ptr{0}, run_row;
+  for (long t = 0; t < h->n_1d; ++t) {
+    if (t + 1 == h->n_1d || h->mid_idx[t + 1] != h->mid_idx[t] || t + 1 - run_ptr.back() == stile::kRunGroup) {
+      run_row.push_back(h->mid_idx[t]);
+      run_ptr.push_back((int32_t)(t + 1));
+    }
+  }
   Arena ar;
   size_t a0 = ar.add(h->mid_idx, (size_t)h->n_1d * 4);
   size_t a1 = ar.add(h->j_idx, (size_t)h->n_1d * 4);
@@ -938,6 +946,8 @@ int stile_sddmm_plan_upload(const StileSddmmPlanHost* h, StileSddmmPlan** out) {
   size_t a5 = ar.add(h->blk_indptr, h->n_blk ? (size_t)(h->n_blk + 1) * 4 : 0);
   size_t a6 = ar.add(h->blk_dense_pos, (size_t)h->n_blk_nnz * 4);
   size_t a7 = ar.add(h->blk_out, (size_t)h->n_blk_nnz * 4);
+  size_t a8 = ar.add(run_ptr.data(), run_ptr.size() * 4);
+  size_t a9 = ar.add(run_row.data(), run_row.size() * 4);
   auto* plan = new StileSddmmPlan();
   cudaError_t e = cudaMalloc(&plan->arena, ar.total ? ar.total : 256);
   if (e != cudaSuccess) {
@@ -969,6 +979,9 @@ int stile_sddmm_plan_upload(const StileSddmmPlanHost* h, StileSddmmPlan** out) {
   a.blk_indptr = P(a5);
   a.blk_dense_pos = P(a6);
   a.blk_out = P(a7);
+  a.n_runs = (int)run_row.size();
+  a.run_ptr = P(a8);
+  a.run_row = P(a9);
   plan->M = h->M;
   plan->K = h->K;
   plan->nnz = h->nnz;
@@ -1003,7 +1016,7 @@ static int sddmm_run(const StileSddmmPlan* plan, const void* X, int64_t ldx, con
   a.F = F;
   cudaError_t e = stile::launch_sddmm(a, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "SDDMM launch");
-  g_launches += (a.n_blk > 0) + (a.n_1d > 0);
+  g_launches += (a.n_blk > 0) + (a.n_runs > 0);
   return STILE_OK;
 }
 

@@ -255,16 +255,16 @@ constexpr int kRunBlocks = 6;  // resident 256-thread blocks per SM (register bu
 
 // kOne: F <= 4 VEC LPR (one pass; the X row stays in registers).
 // kFull: F == 4 VEC LPR exactly (no masking at all).
-template <int LPR, int VEC, int U, int MINB, bool kYb, bool kOne, bool kFull>
+template <int LPR, int VEC, int U, int MINB, bool kYb, bool kOne, bool kFull, bool kXb = false>
 __global__ void __launch_bounds__(256, MINB) sddmm_run_kernel(int n_groups, const int* __restrict__ gptr,
                                                                 const int* __restrict__ grow,
                                                                 const int* __restrict__ cols,
                                                                 const int* __restrict__ outs,
-                                                                const float* __restrict__ X, long ldx,
+                                                                const void* __restrict__ Xv, long ldx,
                                                                 const void* __restrict__ Yv, long ldy,
                                                                 float* __restrict__ out, int F) {
   static_assert(U <= LPR && (U & (U - 1)) == 0, "U must be a power of two no larger than the group");
-  static_assert(!kYb || VEC == 2, "a bf16 load covers 8 features");
+  static_assert((!kYb && !kXb) || VEC == 2, "a bf16 load covers 8 features");
   static_assert(!kFull || kOne, "a full pass is one pass");
   // launched dependent on the previous kernel: wait for its results (X may
   // be one of them), then let the next dependent kernel launch
@@ -277,7 +277,17 @@ __global__ void __launch_bounds__(256, MINB) sddmm_run_kernel(int n_groups, cons
   const long g = ((long)blockIdx.x * blockDim.x + threadIdx.x) / LPR;
   if (g >= n_groups) return;  // the whole group leaves together
   const int p0 = __ldg(gptr + g), p1 = __ldg(gptr + g + 1);
-  const float* __restrict__ xr = X + (long)__ldg(grow + g) * ldx;
+  using TX = typename std::conditional<kXb, uint16_t, float>::type;
+  const TX* __restrict__ xr = static_cast<const TX*>(Xv) + (long)__ldg(grow + g) * ldx;
+  // X's features [f, f + 8) as two float4 (masked past F)
+  auto load_x = [&](int f, float4 (&x)[VEC]) {
+    if constexpr (kXb) {
+      bf16x8_to_f32(kFull ? ldg_u4(xr + f) : ld_row8_bf16(xr, f, F), x[0], x[1]);
+    } else {
+#pragma unroll
+      for (int w = 0; w < VEC; ++w) x[w] = kFull ? ldg4(xr + f + 4 * w) : ld4_live(xr, f + 4 * w, F);
+    }
+  };
   constexpr int FP = 4 * VEC * LPR;  // features per pass
   const int f0 = 4 * VEC * sl;
   auto load_y = [&](int c, int f, float4 (&y)[VEC]) {
@@ -290,10 +300,7 @@ __global__ void __launch_bounds__(256, MINB) sddmm_run_kernel(int n_groups, cons
     }
   };
   float4 x1[VEC];
-  if constexpr (kOne) {
-#pragma unroll
-    for (int w = 0; w < VEC; ++w) x1[w] = kFull ? ldg4(xr + f0 + 4 * w) : ld4_live(xr, f0 + 4 * w, F);
-  }
+  if constexpr (kOne) load_x(f0, x1);
 #pragma unroll 1
   for (int b0 = p0; b0 < p1; b0 += U) {
     int c[U];
@@ -316,8 +323,7 @@ __global__ void __launch_bounds__(256, MINB) sddmm_run_kernel(int n_groups, cons
       for (int fc = 0; fc < F; fc += FP) {
         const int f = fc + f0;
         float4 xv[VEC];
-#pragma unroll
-        for (int w = 0; w < VEC; ++w) xv[w] = ld4_live(xr, f + 4 * w, F);
+        load_x(f, xv);
         float4 y[U][VEC];
 #pragma unroll
         for (int u = 0; u < U; ++u) load_y(c[u], f, y[u]);
@@ -346,24 +352,25 @@ __global__ void __launch_bounds__(256, MINB) sddmm_run_kernel(int n_groups, cons
   }
 }
 
-template <int L, bool kYb>
+template <int L, bool kYb, bool kXb = false>
 static cudaError_t launch_runs_t(int grid, bool one, bool full, cudaStream_t st, int n_groups, const int* gptr,
-                                 const int* grow, const int* cols, const int* outs, const float* X, long ldx,
+                                 const int* grow, const int* cols, const int* outs, const void* X, long ldx,
                                  const void* Y, long ldy, float* out, int F) {
   if (full)
-    return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, true, true>, dim3((unsigned)grid),
+    return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, true, true, kXb>, dim3((unsigned)grid),
                             dim3(256), 0, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
   if (one)
-    return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, true, false>, dim3((unsigned)grid),
+    return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, true, false, kXb>, dim3((unsigned)grid),
                             dim3(256), 0, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
-  return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, false, false>, dim3((unsigned)grid),
+  return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, false, false, kXb>, dim3((unsigned)grid),
                           dim3(256), 0, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
 }
 
 cudaError_t launch_sddmm_runs(int n_groups, const int* gptr, const int* grow, const int* cols, const int* outs,
-                              const float* X, long ldx, const void* Y, bool y_bf16, long ldy, float* out, int F,
-                              cudaStream_t st) {
+                              const void* X, bool x_bf16, long ldx, const void* Y, bool y_bf16, long ldy, float* out,
+                              int F, cudaStream_t st) {
   if (n_groups <= 0) return cudaSuccess;
+  if (x_bf16 && !y_bf16) return cudaErrorNotSupported;  // no caller has a bf16 X with an fp32 Y
   // lanes per run: 8 features per lane (two float4, or one bf16 load);
   // 128 features per pass at most (longer rows take several passes)
   int lpr = 16;
@@ -374,17 +381,19 @@ cudaError_t launch_sddmm_runs(int n_groups, const int* gptr, const int* grow, co
   }
   const bool one = F <= 8 * lpr, full = F == 8 * lpr;
   const int grid = (int)(((long)n_groups * lpr + 255) / 256);
+#define STILE_RUNS_ARGS grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F
   switch (lpr) {
     case 4:
-      return y_bf16 ? launch_runs_t<4, true>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F)
-                    : launch_runs_t<4, false>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+      return x_bf16 ? launch_runs_t<4, true, true>(STILE_RUNS_ARGS)
+                    : (y_bf16 ? launch_runs_t<4, true>(STILE_RUNS_ARGS) : launch_runs_t<4, false>(STILE_RUNS_ARGS));
     case 8:
-      return y_bf16 ? launch_runs_t<8, true>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F)
-                    : launch_runs_t<8, false>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+      return x_bf16 ? launch_runs_t<8, true, true>(STILE_RUNS_ARGS)
+                    : (y_bf16 ? launch_runs_t<8, true>(STILE_RUNS_ARGS) : launch_runs_t<8, false>(STILE_RUNS_ARGS));
     default:
-      return y_bf16 ? launch_runs_t<16, true>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F)
-                    : launch_runs_t<16, false>(grid, one, full, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+      return x_bf16 ? launch_runs_t<16, true, true>(STILE_RUNS_ARGS)
+                    : (y_bf16 ? launch_runs_t<16, true>(STILE_RUNS_ARGS) : launch_runs_t<16, false>(STILE_RUNS_ARGS));
   }
+#undef STILE_RUNS_ARGS
 }
 
 constexpr int kChunk = 128;
@@ -474,8 +483,9 @@ cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  return launch_sddmm_list(p.n_1d, p.mid_idx, p.j_idx, p.remap, p.X, p.xy_bf16, p.ldx, p.Y, p.xy_bf16, p.ldy, p.out,
-                           p.F, st);
+  // 1D tiles: the flattened entries come in runs of one row (cut at upload)
+  return launch_sddmm_runs(p.n_runs, p.run_ptr, p.run_row, p.j_idx, p.remap, p.X, p.xy_bf16, p.ldx, p.Y, p.xy_bf16,
+                           p.ldy, p.out, p.F, st);
 }
 
 // Row softmax over a CSR pattern (the sparse-attention step between the

@@ -1320,8 +1320,8 @@ cudaError_t launch_ell_bwd(const SpmmArgs& p, cudaStream_t st) {
 }
 
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {
-  return launch_sddmm_runs(p.dv_n_groups, p.dv_gptr, p.dv_grow, p.dv_col, p.dv_id, dY, lddy, p.B, p.b_bf16 != 0,
-                           p.ldb, dvals, p.N, st);
+  return launch_sddmm_runs(p.dv_n_groups, p.dv_gptr, p.dv_grow, p.dv_col, p.dv_id, dY, false, lddy, p.B,
+                           p.b_bf16 != 0, p.ldb, dvals, p.N, st);
 }
 
 }  // namespace stile

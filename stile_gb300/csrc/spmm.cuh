@@ -144,6 +144,10 @@ struct SddmmArgs {
   const int* mid_idx;
   const int* j_idx;
   const int* remap;
+  // the 1D entries as runs of one row (at most kRunGroup entries each)
+  int n_runs;
+  const int* run_ptr;
+  const int* run_row;
   int n_blk, bm, bn;
   const int* blk_i;
   const int* blk_j;
@@ -160,8 +164,8 @@ cudaError_t launch_sddmm_list(long n, const int* rows, const int* cols, const in
 // row-run SDDMM: group g is entries [gptr[g], gptr[g+1]) of row grow[g]
 constexpr int kRunGroup = 64;  // entries per run group at most
 cudaError_t launch_sddmm_runs(int n_groups, const int* gptr, const int* grow, const int* cols, const int* outs,
-                              const float* X, long ldx, const void* Y, bool y_bf16, long ldy, float* out, int F,
-                              cudaStream_t st);
+                              const void* X, bool x_bf16, long ldx, const void* Y, bool y_bf16, long ldy, float* out,
+                              int F, cudaStream_t st);
 
 cudaError_t launch_sparse_attention(int n_rows, const int* indptr, const int* indices, const float* Q,
                                     const float* K, const float* V, long ldq, long ldk, long ldv, long q_head,
