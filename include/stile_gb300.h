@@ -315,6 +315,7 @@ int stile_spmm_plan_set_values(StileSpmmPlan* plan, const float* vals, void* str
 /* Device-side error flag of a plan's kernels (bounded waits that gave up):
  * synchronises the stream, returns the flag (0 = none) and clears it. */
 int stile_spmm_plan_error_flag(StileSpmmPlan* plan, void* stream, int32_t* flag);
+int stile_sddmm_plan_error_flag(StileSddmmPlan* plan, void* stream, int32_t* flag);
 
 /* Wait policy of the plan's tensor-core kernel (failure detection; no
  * counterpart in the reference).  Every pipeline wait of the kernel (on an

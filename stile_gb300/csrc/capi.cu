@@ -62,6 +62,7 @@ struct StileSpmmPlan {
 
 struct StileSddmmPlan {
   void* arena = nullptr;
+  int* err_flag = nullptr;
   stile::SddmmArgs args{};
   int M = 0, K = 0;
   long nnz = 0;
@@ -873,6 +874,18 @@ int stile_sparse_attention(int32_t n_rows, const int32_t* indptr, const int32_t*
   return STILE_OK;
 }
 
+int stile_sddmm_plan_error_flag(StileSddmmPlan* plan, void* stream, int32_t* flag) {
+  if (!plan || !flag) return fail(STILE_E_INVALID, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int host = 0;
+  cudaError_t e = cudaMemcpyAsync(&host, plan->err_flag, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(plan->err_flag, 0, 4, st);
+  if (e != cudaSuccess) return cuda_fail(e, "error flag readback");
+  *flag = host;
+  return STILE_OK;
+}
+
 int stile_csr_row_softmax(int32_t M, const int32_t* indptr, int64_t nnz, const float* x, float* out, float scale,
                           int32_t batch, void* stream) {
   if (M < 0 || nnz < 0 || batch < 0) return fail(STILE_E_INVALID, "bad shape");
@@ -948,6 +961,7 @@ int stile_sddmm_plan_upload(const StileSddmmPlanHost* h, StileSddmmPlan** out) {
   size_t a7 = ar.add(h->blk_out, (size_t)h->n_blk_nnz * 4);
   size_t a8 = ar.add(run_ptr.data(), run_ptr.size() * 4);
   size_t a9 = ar.add(run_row.data(), run_row.size() * 4);
+  size_t a10 = ar.add(nullptr, 16);
   auto* plan = new StileSddmmPlan();
   cudaError_t e = cudaMalloc(&plan->arena, ar.total ? ar.total : 256);
   if (e != cudaSuccess) {
@@ -982,6 +996,14 @@ int stile_sddmm_plan_upload(const StileSddmmPlanHost* h, StileSddmmPlan** out) {
   a.n_runs = (int)run_row.size();
   a.run_ptr = P(a8);
   a.run_row = P(a9);
+  plan->err_flag = (int*)(base + ar.offs[a10]);
+  a.err_flag = plan->err_flag;
+  e = cudaMemset(plan->err_flag, 0, 16);
+  if (e != cudaSuccess) {
+    cudaFree(plan->arena);
+    delete plan;
+    return cuda_fail(e, "cudaMemset(plan)");
+  }
   plan->M = h->M;
   plan->K = h->K;
   plan->nnz = h->nnz;

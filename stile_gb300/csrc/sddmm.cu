@@ -4,10 +4,11 @@
 //    the entry-list kernel below over (mid_idx, j_idx, remap); results go
 //    straight to their CSR position -- the reference writes a tile-ordered
 //    buffer and reorders on the host (order_output_BSDDMM, :4247-4288).
-//  * block tiles (the reference's "TC_sddmm", :2324-2415): one CTA per
-//    bm x bn block; the X / Y rows of the block are staged in shared memory
-//    one 128-feature chunk at a time and only the live entries of the block
-//    (indicesDense) are computed.
+//  * block tiles (the reference's "TC_sddmm", :2324-2415, whose kernel runs
+//    each 16x16 block as a wmma product, my_wmmas1.py:422-466): tcgen05.mma
+//    over units of 8 blocks, below; only the live entries of a block
+//    (indicesDense) are written.
+#include <algorithm>
 #include <type_traits>
 
 #include "common.cuh"
@@ -396,81 +397,169 @@ cudaError_t launch_sddmm_runs(int n_groups, const int* gptr, const int* grow, co
 #undef STILE_RUNS_ARGS
 }
 
-constexpr int kChunk = 128;
-constexpr int kPadRow = kChunk + 4;
+// Block tiles on the tensor cores.  A unit is up to 8 consecutive 16x16
+// blocks: its 128 Y rows (16 per block) form the MMA's A operand (M = 128)
+// and its 128 X rows its B operand (N = 128), both K-major with the
+// features along K exactly as the rows are stored, so
+//   D[16 j + n][16 j + m] = <X[blk_i[j][m]], Y[blk_j[j][n]]>
+// on the 8 diagonal 16x16 sub-blocks (the off-diagonal ones are products
+// nobody asked for; the tensor pipe has time to spare).  Per 64-feature
+// chunk every thread gathers one Y row and one X row, converts them to bf16
+// (fp32 inputs: hi = bf16(x) and lo = bf16(x - hi), three MMAs per K-slice,
+// hi.hi + hi.lo + lo.hi), stores them in the no-swizzle K-major layout
+// (core matrices of 8 rows x 16 B, k halves 128 B apart, 8-row groups 256 B
+// apart, one 4 KB slice per 16 features), and one thread issues the MMAs
+// into a 128-column TMEM accumulator.  The epilogue reads each warp's 32 Y
+// rows from TMEM, stages the diagonal blocks in shared memory and writes
+// only the blocks' live entries (indicesDense).  The wait for the MMAs is
+// bounded; a wait that runs out sets the error flag and skips the unit's
+// output.
+constexpr int kBlkUnit = 8;                      // blocks per unit
+constexpr int kBlkFc = 64;                       // features per chunk: 4 K-slices of 16
+constexpr uint32_t kBlkSlice = 4096;             // one K = 16 slice of 128 bf16 rows
+constexpr uint32_t kBlkImg = 4 * kBlkSlice;      // 64 features of 128 rows
+constexpr int kBlkDPad = 17;                     // staged D rows (floats), padded against bank conflicts
 
-// features [f, f+4) of a bf16 row as fp32, masked by F (rows are 16-byte
-// aligned with a stride that is a multiple of 8 elements)
-__device__ __forceinline__ float4 ld_row4_bf16(const uint16_t* row, int f, int F) {
-  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (f < F) {
-    const uint2 u = __ldg(reinterpret_cast<const uint2*>(row + f));
-    v = make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
-                    __uint_as_float(u.y & 0xffff0000u));
-    if (f + 1 >= F) v.y = 0.f;
-    if (f + 2 >= F) v.z = 0.f;
-    if (f + 3 >= F) v.w = 0.f;
-  }
-  return v;
+template <bool kB16>
+struct BlkCfg {
+  static constexpr int kImgs = kB16 ? 2 : 4;     // Y hi, X hi (+ Y lo, X lo)
+  static constexpr uint32_t kDBytes = kBlkUnit * 16 * kBlkDPad * 4;
+  static constexpr uint32_t kBytes = 1024 + kImgs * kBlkImg + kDBytes + 64;
+};
+
+// 16 bytes of 8 bf16 features at element (row, k = 8 q) of a 128-row
+// K-major image (slice q / 2, k half q % 2)
+__device__ __forceinline__ uint32_t blk_off(int row, int q) {
+  return (uint32_t)((q >> 1) * kBlkSlice + (row >> 3) * 256 + (q & 1) * 128 + (row & 7) * 16);
 }
 
 template <bool kB16>
-__global__ void __launch_bounds__(128) sddmm_block_kernel(SddmmArgs p) {
-  __shared__ __align__(16) float xs[16 * kPadRow];
-  __shared__ __align__(16) float ys[16 * kPadRow];
-  const int b = blockIdx.x;
-  const int tid = threadIdx.x;
-  const int e0 = p.blk_indptr[b], e1 = p.blk_indptr[b + 1];
-  const int n_e = e1 - e0;  // <= bm * bn <= 256
-  float acc[2] = {0.f, 0.f};
-  int pos[2];
-#pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    const int e = tid + q * 128;
-    pos[q] = (e < n_e) ? p.blk_dense_pos[e0 + e] : 0;
+__global__ void __launch_bounds__(128) sddmm_block_tc_kernel(SddmmArgs p, int n_units) {
+  using Cfg = BlkCfg<kB16>;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const uint32_t yhi = base, xhi = base + kBlkImg, ylo = base + 2 * kBlkImg, xlo = base + 3 * kBlkImg;
+  const uint32_t dst = base + Cfg::kImgs * kBlkImg;
+  float* dstage = reinterpret_cast<float*>(smem_raw + (dst - smem_u32(smem_raw)));
+  const uint32_t bar = dst + Cfg::kDBytes, tmem_slot = bar + 8;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
   }
-  for (int fc = 0; fc < p.F; fc += kChunk) {
-    __syncthreads();
-    // stage: bm rows of X and bn rows of Y, 32 float4 per row
-    for (int i = tid; i < 16 * (kChunk / 4); i += 128) {
-      const int r = i / (kChunk / 4), c = (i % (kChunk / 4)) * 4;
-      float4 vx = make_float4(0.f, 0.f, 0.f, 0.f), vy = vx;
-      if (kB16) {
-        const uint16_t* X16 = reinterpret_cast<const uint16_t*>(p.X);
-        const uint16_t* Y16 = reinterpret_cast<const uint16_t*>(p.Y);
-        if (r < p.bm) vx = ld_row4_bf16(X16 + (long)p.blk_i[(long)b * p.bm + r] * p.ldx, fc + c, p.F);
-        if (r < p.bn) vy = ld_row4_bf16(Y16 + (long)p.blk_j[(long)b * p.bn + r] * p.ldy, fc + c, p.F);
-      } else {
-        if (r < p.bm) vx = ld_row4(p.X + (long)p.blk_i[(long)b * p.bm + r] * p.ldx, fc + c, p.F);
-        if (r < p.bn) vy = ld_row4(p.Y + (long)p.blk_j[(long)b * p.bn + r] * p.ldy, fc + c, p.F);
-      }
-      *reinterpret_cast<float4*>(&xs[r * kPadRow + c]) = vx;
-      *reinterpret_cast<float4*>(&ys[r * kPadRow + c]) = vy;
-    }
-    __syncthreads();
+  if (warp == 0) {
+    tmem_alloc(tmem_slot, 128);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  uint32_t tmem;
+  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
+  // kind::f16, bf16 x bf16, M = 128, N = 128, both operands K-major
+  constexpr uint32_t idesc = make_idesc(1, 1, 0, 0, 128, 128);
+  const int F = p.F;
+  uint32_t phase = 0;
+  bool ok = true;
+#pragma unroll 1
+  for (int u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+    const int b0 = u * kBlkUnit;
+    const int nb = min(kBlkUnit, p.n_blk - b0);
+    const int j = tid >> 4, r = tid & 15;
+    const int yrow = j < nb ? __ldg(p.blk_j + (long)(b0 + j) * 16 + r) : -1;
+    const int xrow = j < nb ? __ldg(p.blk_i + (long)(b0 + j) * 16 + r) : -1;
+#pragma unroll 1
+    for (int fc = 0; fc < F; fc += kBlkFc) {
+      // gather and convert: this thread's Y row and X row, 64 features
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int e = tid + q * 128;
-      if (e < n_e) {
-        const int m = pos[q] / p.bn, n = pos[q] % p.bn;
-        const float* xr = &xs[m * kPadRow];
-        const float* yr = &ys[n * kPadRow];
-        float s = 0.f;
-#pragma unroll 8
-        for (int c = 0; c < kChunk; c += 4) {
-          const float4 a = *reinterpret_cast<const float4*>(xr + c);
-          const float4 bb = *reinterpret_cast<const float4*>(yr + c);
-          s += dot4(a, bb);
+      for (int side = 0; side < 2; ++side) {
+        const int row = side ? xrow : yrow;
+        const uint32_t hi = side ? xhi : yhi, lo = side ? xlo : ylo;
+#pragma unroll 2
+        for (int q = 0; q < kBlkFc / 8; ++q) {
+          const int f = fc + 8 * q;
+          float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+          if (row >= 0) {
+            if constexpr (kB16) {
+              const uint16_t* src = reinterpret_cast<const uint16_t*>(side ? (const void*)p.X : (const void*)p.Y);
+              bf16x8_to_f32(ld_row8_bf16(src + (long)row * (side ? p.ldx : p.ldy), f, F), a, b);
+            } else {
+              const float* src = (side ? p.X : p.Y) + (long)row * (side ? p.ldx : p.ldy);
+              a = ld4_live(src, f, F);
+              b = ld4_live(src, f + 4, F);
+            }
+          }
+          const uint32_t h01 = pack_bf16x2(a.x, a.y), h23 = pack_bf16x2(a.z, a.w);
+          const uint32_t h45 = pack_bf16x2(b.x, b.y), h67 = pack_bf16x2(b.z, b.w);
+          st_shared_v4(hi + blk_off(tid, q), make_uint4(h01, h23, h45, h67));
+          if constexpr (!kB16) {
+            auto lo2 = [](uint32_t h, float x0, float x1) {
+              return pack_bf16x2(x0 - __uint_as_float(h << 16), x1 - __uint_as_float(h & 0xffff0000u));
+            };
+            st_shared_v4(lo + blk_off(tid, q),
+                         make_uint4(lo2(h01, a.x, a.y), lo2(h23, a.z, a.w), lo2(h45, b.x, b.y), lo2(h67, b.z, b.w)));
+          }
         }
-        acc[q] += s;
+      }
+      fence_proxy_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      if (tid == 0) {
+        const int ns = min(4, (F - fc + 15) / 16);
+        for (int s = 0; s < ns; ++s) {
+          const uint64_t ah = smem_desc(yhi + s * kBlkSlice, 128, 256, kSwizzleNone);
+          const uint64_t bh = smem_desc(xhi + s * kBlkSlice, 128, 256, kSwizzleNone);
+          umma_f16(tmem, ah, bh, idesc, (fc > 0 || s > 0) ? 1u : 0u);
+          if constexpr (!kB16) {
+            umma_f16(tmem, ah, smem_desc(xlo + s * kBlkSlice, 128, 256, kSwizzleNone), idesc, 1u);
+            umma_f16(tmem, smem_desc(ylo + s * kBlkSlice, 128, 256, kSwizzleNone), bh, idesc, 1u);
+          }
+        }
+        umma_commit(bar);
+      }
+      // the MMAs read the images: nobody rewrites them, or reads TMEM, first
+      const bool done = __syncthreads_and(tid == 0 ? mbar_wait_bounded(bar, phase) : true) != 0;
+      phase ^= 1u;
+      if (!done) {
+        ok = false;
+        break;
+      }
+      if (tid != 0) mbar_wait_bounded(bar, phase ^ 1u);  // completed: returns at once
+      tc_fence_after();
+    }
+    if (!ok) break;
+    // epilogue: warp w holds TMEM lanes (Y rows) 32 w .. 32 w + 31, i.e.
+    // blocks 2 w and 2 w + 1, whose X rows are TMEM columns 16 j .. 16 j + 15
+    uint32_t v0[16], v1[16];
+    tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * warp), v0);
+    tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * warp + 16), v1);
+    tmem_wait_ld();
+    {
+      const int jj = tid >> 4, n = tid & 15;
+#pragma unroll
+      for (int m = 0; m < 16; ++m)
+        dstage[(jj * 16 + n) * kBlkDPad + m] = __uint_as_float(lane < 16 ? v0[m] : v1[m]);
+    }
+    tc_fence_before();
+    __syncthreads();
+    for (int jj = 0; jj < nb; ++jj) {
+      const int e0 = __ldg(p.blk_indptr + b0 + jj), e1 = __ldg(p.blk_indptr + b0 + jj + 1);
+      for (int e = e0 + tid; e < e1; e += 128) {
+        const int pos = __ldg(p.blk_dense_pos + e);
+        const int m = pos / p.bn, n = pos % p.bn;
+        __stcs(p.out + __ldg(p.blk_out + e), dstage[(jj * 16 + n) * kBlkDPad + m]);
       }
     }
+    __syncthreads();
   }
-#pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    const int e = tid + q * 128;
-    if (e < n_e) p.out[p.blk_out[e0 + e]] = acc[q];
-  }
+  if (!ok && tid == 0 && p.err_flag) atomicOr(p.err_flag, 1);
+  // every MMA this CTA issued has completed before TMEM is freed
+  if (!ok && tid == 0) mbar_wait_bounded(bar, phase ^ 1u);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, 128);
 }
 
 cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st) {
@@ -478,9 +567,17 @@ cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st) {
   // result is the one kept, as in the reference's host reorder
   // (order_output_BSDDMM writes the TC results first, then the 1D ones)
   if (p.n_blk > 0) {
-    if (p.xy_bf16) sddmm_block_kernel<true><<<p.n_blk, 128, 0, st>>>(p);
-    else sddmm_block_kernel<false><<<p.n_blk, 128, 0, st>>>(p);
-    cudaError_t e = cudaGetLastError();
+    if (p.bm != 16 || p.bn != 16) return cudaErrorNotSupported;
+    const int n_units = (p.n_blk + kBlkUnit - 1) / kBlkUnit;
+    // at least 57 KB of shared memory per CTA: at most 4 CTAs share an SM,
+    // whose 512 TMEM columns then hold their 128-column accumulators
+    const size_t smem = std::max<size_t>(p.xy_bf16 ? BlkCfg<true>::kBytes : BlkCfg<false>::kBytes, 57 * 1024);
+    auto k = p.xy_bf16 ? sddmm_block_tc_kernel<true> : sddmm_block_tc_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int grid = std::min(n_units, device_sm_count() * (p.xy_bf16 ? 4 : 2));
+    k<<<grid, 128, smem, st>>>(p, n_units);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   // 1D tiles: the flattened entries come in runs of one row (cut at upload)

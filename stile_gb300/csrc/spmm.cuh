@@ -154,6 +154,8 @@ struct SddmmArgs {
   const int* blk_indptr;
   const int* blk_dense_pos;
   const int* blk_out;
+  // device error flag (the block kernel's bounded MMA wait gave up)
+  int* err_flag;
 };
 
 cudaError_t launch_sddmm(const SddmmArgs& p, cudaStream_t st);

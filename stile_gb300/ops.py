@@ -316,6 +316,12 @@ class DeviceSddmmPlan:
                    "stile_sddmm_plan_upload")
         self.handle = handle
 
+    def error_flag(self) -> int:
+        f = ctypes.c_int32(0)
+        _lib.check(self.lib.stile_sddmm_plan_error_flag(self.handle, _stream(), ctypes.byref(f)),
+                   "stile_sddmm_plan_error_flag")
+        return int(f.value)
+
     def run(self, X: torch.Tensor, Y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """out[t] = <X[row(t)], Y[col(t)]> in fp32; X and Y both bf16 are read
         as is, any other mix is computed from fp32 copies."""

@@ -158,3 +158,36 @@ def run_probe_f8(Abytes, Bbytes):
     _lib.check(rc, "probe")
     torch.cuda.synchronize()
     return out.cpu().numpy().reshape(128, 16), int(err.item())
+
+
+def kmajor_image_16bit(vals_rk):
+    """[rows, 16 (k)] bf16 values -> K-major, no-swizzle image: core
+    matrices of 8 rows x 16 bytes (8 k), the two k halves 128 B apart
+    (LBO), 8-row groups 256 B apart (SBO)."""
+    from stile_gb300.device import _to_bf16_bits
+    rows = vals_rk.shape[0]
+    bits = _to_bf16_bits(np.asarray(vals_rk, np.float32))
+    img = np.zeros(4096, dtype=np.uint16)
+    for r in range(rows):
+        for k in range(16):
+            img[((r // 8) * 256 + (k // 8) * 128 + (r % 8) * 16 + (k % 8) * 2) // 2] = bits[r, k]
+    return img
+
+
+def run_probe_bf16_kmajor(A, Bm):
+    """One kind::f16 MMA (bf16, K = 16) with both operands K-major without
+    swizzle (the SDDMM block kernel's layout)."""
+    import torch
+    from stile_gb300 import _lib
+    lib = _lib.load()
+    ai = torch.as_tensor(kmajor_image_16bit(A).view(np.int16).copy(), device="cuda")
+    bi = torch.as_tensor(kmajor_image_16bit(Bm).view(np.int16).copy(), device="cuda")
+    out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    d = (ctypes.c_uint32 * 6)(128, 256, 0, 128, 256, 0)
+    idesc = (1 << 4) | (1 << 7) | (1 << 10) | (0 << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
+    rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, 0, out.data_ptr(), err.data_ptr(),
+                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc, "probe")
+    torch.cuda.synchronize()
+    return out.cpu().numpy().reshape(128, 16), int(err.item())

@@ -44,3 +44,16 @@ def test_umma_f8_kmajor_layout():
     ref = A.astype(np.float64) @ Bm.astype(np.float64).T
     D, err = run_probe_f8(Ab, Bb)
     assert err == 0 and float(np.abs(D - ref).max()) < 1e-3 * max(1.0, float(np.abs(ref).max()))
+
+
+def test_umma_bf16_kmajor_layout():
+    """kind::f16 (bf16) with both operands K-major, no swizzle (core matrices
+    of 8 rows x 16 B, LBO 128 B along k, SBO 256 B between 8-row groups): the
+    layout of the SDDMM block kernel's gathered rows."""
+    from gpu_util import run_probe_bf16_kmajor
+    rng = np.random.default_rng(9)
+    A = bf16_round(rng.standard_normal((128, 16)))
+    Bm = bf16_round(rng.standard_normal((16, 16)))
+    ref = A.astype(np.float64) @ Bm.astype(np.float64).T
+    D, err = run_probe_bf16_kmajor(A, Bm)
+    assert err == 0 and float(np.abs(D - ref).max()) < 1e-3
