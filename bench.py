@@ -407,6 +407,19 @@ class SparseStep:
         self.forward(ev)
         self.backward()
 
+    def breakdown(self, timed, steps):
+        """Median ms of every operation of the step on its own (L2 flushed
+        before each) and the backward variant each width runs."""
+        out = {}
+        for i, op in enumerate(self.ops):
+            N = self.B[i].shape[1]
+            t, _ = timed(lambda: op(self.B[i], out=self.C[i]), steps)
+            out[f"forward_N{N}_ms"] = float(np.median(t))
+            t, _ = timed(lambda: op.backward(self.dC[i], self.B[i], self.dB[i]), steps)
+            out[f"backward_N{N}_ms"] = float(np.median(t))
+            out[f"backward_N{N}_variant"] = op._bwd_choice.get(N, op.cfg.backward)
+        return out
+
     def accuracy(self, layers):
         import oracle.semantics as S
         from stile_gb300 import workloads as W
@@ -610,6 +623,7 @@ def run_gpu(args):
     plain_times, _ = timed(plain, args.steps)
     plain_ms = float(np.sum(plain_times)) / args.steps
     plain_value = flops / (plain_ms * 1e-3) / 1e9
+    breakdown = st.breakdown(timed, args.steps)
 
     # roofline of the dominant kernel: the layer-1 forward SpMM (N = 128)
     fwd_ms = float(np.mean(fwd_times))
@@ -722,6 +736,7 @@ def run_gpu(args):
             "csr_baseline": {"value": plain_value, "unit": "GFLOP/s", "ms_per_step": plain_ms,
                              "speedup_hybrid_over_csr": value / plain_value},
             "accuracy": acc,
+            "breakdown": breakdown,
             "gcn_training_step": {"ms": train_ms, "what": "whole two-layer GCN step (X W1, Z1 W2 and their "
                                                           "gradients in torch fp32 GEMMs, ReLU, the sparse "
                                                           "products), X resident"},
