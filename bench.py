@@ -745,6 +745,7 @@ def run_gpu(args):
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
             "wall_s_timed_region": wall,
+            "device_mem_peak_gb": torch.cuda.max_memory_allocated() / 1e9,
         }
         print(json.dumps(out), flush=True)
     if world > 1:
