@@ -463,25 +463,30 @@ class SparseStep:
 def make_timer(flush):
     import torch
 
-    def timed(fn, steps, per_step_events=False):
-        times, fwd = [], []
+    def timed(fn, steps, per_step_events=False, host_sync=False):
+        """Per-step device times between CUDA events, L2 flushed before each
+        step outside the events.  The host enqueues every step before the
+        first has ended (one synchronize after the last), so the events see
+        the GPU's time for the step, not the host's launch latency after a
+        synchronize; host_sync=True waits for each step (an end-to-end step
+        whose result the host reads)."""
+        rec = []
         for _ in range(steps):
             flush.zero_()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)] if per_step_events else None
+            s.record()
             if per_step_events:
-                ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-                s.record()
                 fn(ev)
-                e.record()
-                e.synchronize()
-                times.append(s.elapsed_time(e))
-                fwd.append(ev[0].elapsed_time(ev[1]))
             else:
-                s.record()
                 fn()
-                e.record()
+            e.record()
+            if host_sync:
                 e.synchronize()
-                times.append(s.elapsed_time(e))
+            rec.append((s, e, ev))
+        torch.cuda.synchronize()
+        times = [s.elapsed_time(e) for s, e, _ in rec]
+        fwd = [ev[0].elapsed_time(ev[1]) for _, _, ev in rec] if per_step_events else []
         return times, fwd
     return timed
 
@@ -613,7 +618,11 @@ def run_gpu(args):
     launches0 = launch_count()
     wall0 = time.perf_counter()
     with ClockSampler(local) as clk:
+        # an NVTX range around the timed steps (a profiler's launch list can
+        # be limited to it)
+        torch.cuda.nvtx.range_push("timed_steps")
         times, fwd_times = timed(st.step, args.steps, per_step_events=True)
+        torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     launches = launch_count() - launches0
@@ -692,7 +701,7 @@ def run_gpu(args):
     for _ in range(2):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_times, _ = timed(e2e_step, args.steps)
+    e2e_times, _ = timed(e2e_step, args.steps, host_sync=True)
     e2e_ms = max_over_ranks(float(np.sum(e2e_times)) / args.steps, dev)
     e2e_val = world * flops / (e2e_ms * 1e-3) / 1e9
     h2d = sum(B.shape[0] * B.shape[1] * 4 + dC.shape[0] * dC.shape[1] * 4 for B, dC in layers)
@@ -774,16 +783,16 @@ def run_attention(args):
     def timed(fn):
         for _ in range(max(args.warmup, 3)):
             fn()
-        ts = []
-        for _ in range(args.steps):
+        rec = []
+        for _ in range(args.steps):  # enqueued ahead, one synchronize (as make_timer)
             flush.zero_()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record()
             fn()
             e.record()
-            e.synchronize()
-            ts.append(s.elapsed_time(e))
-        return float(np.median(ts))
+            rec.append((s, e))
+        torch.cuda.synchronize()
+        return float(np.median([s.elapsed_time(e) for s, e in rec]))
 
     out = {"workload": "sparse_attention", "n": n, "heads": H, "F": F, "Fv": F, "steps": args.steps,
            "l2": "flushed between iterations (256 MiB write)"}
@@ -824,16 +833,16 @@ def run_config(args):
     def timed(fn, steps):
         for _ in range(max(args.warmup, 3)):
             fn()
-        ts = []
-        for _ in range(steps):
+        rec = []
+        for _ in range(steps):  # enqueued ahead, one synchronize (as make_timer)
             flush.zero_()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record()
             fn()
             e.record()
-            e.synchronize()
-            ts.append(s.elapsed_time(e))
-        return float(np.median(ts))
+            rec.append((s, e))
+        torch.cuda.synchronize()
+        return float(np.median([s.elapsed_time(e) for s, e in rec]))
 
     def plan_summary(plan):
         return {f"{k[0]}{'/atomic' if k[1] else ''}": v for k, v in plan.summary().items()}

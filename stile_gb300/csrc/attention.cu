@@ -9,7 +9,7 @@
 // (my_3rdparty/Magicube/Magicube1/end2end_eval/sparse_transformer_magicube/
 // src/cuda/softmax_kernel.cu) and the SpMM with the probabilities as values,
 // here in one pass per row: an LPR-lane group holds its query row (8
-// features a lane), gathers the K and V rows of two entries at a time,
+// features a lane, as two float4 4 LPR features apart), gathers the K and V rows of two entries at a time,
 // reduces the two scores with a transposing butterfly, broadcasts them, and
 // keeps an online softmax -- running maximum m, running sum l and an output
 // accumulator rescaled by exp(m_old - m_new) whenever the maximum grows --
@@ -37,9 +37,11 @@ __global__ void __launch_bounds__(256, 4) sparse_attention_kernel(int n_rows, co
   const float* Qh = Q + h * q_head;
   const float* Kh = K + h * k_head;
   const float* Vh = V + h * v_head;
-  const int f = 8 * sl;
+  // this lane's features: f .. f + 3 and f2 .. f2 + 3 (each load
+  // instruction of the group reads 16 LPR contiguous bytes of a row)
+  const int f = 4 * sl, f2 = f + 4 * LPR;
   const float* qr = Qh + r * ldq;
-  const float4 q0 = ld4_live(qr, f, F), q1 = ld4_live(qr, f + 4, F);
+  const float4 q0 = ld4_live(qr, f, F), q1 = ld4_live(qr, f2, F);
   const int rb = __ldg(indptr + r), re = __ldg(indptr + r + 1);
   float m = -INFINITY, l = 0.f;
   float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
@@ -51,10 +53,10 @@ __global__ void __launch_bounds__(256, 4) sparse_attention_kernel(int n_rows, co
     const float* k1 = Kh + (long)c1 * ldk;
     const float* w0 = Vh + (long)c0 * ldv;
     const float* w1 = Vh + (long)c1 * ldv;
-    const float4 ka0 = ld4_live(k0, f, F), kb0 = ld4_live(k0, f + 4, F);
-    const float4 ka1 = ld4_live(k1, f, F), kb1 = ld4_live(k1, f + 4, F);
-    const float4 va0 = ld4_live(w0, f, Fv), vb0 = ld4_live(w0, f + 4, Fv);
-    const float4 va1 = ld4_live(w1, f, Fv), vb1 = ld4_live(w1, f + 4, Fv);
+    const float4 ka0 = ld4_live(k0, f, F), kb0 = ld4_live(k0, f2, F);
+    const float4 ka1 = ld4_live(k1, f, F), kb1 = ld4_live(k1, f2, F);
+    const float4 va0 = ld4_live(w0, f, Fv), vb0 = ld4_live(w0, f2, Fv);
+    const float4 va1 = ld4_live(w1, f, Fv), vb1 = ld4_live(w1, f2, Fv);
     const float s0 = dot4(q0, ka0) + dot4(q1, kb0);
     const float s1 = dot4(q0, ka1) + dot4(q1, kb1);
     // transposing butterfly: the upper half of the group keeps entry 1
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(256, 4) sparse_attention_kernel(int n_rows, co
   const float inv = l > 0.f ? 1.f / l : 0.f;
   float* orow = out + h * o_head + r * ldo;
   st_row4(orow, f, Fv, make_float4(acc0.x * inv, acc0.y * inv, acc0.z * inv, acc0.w * inv));
-  st_row4(orow, f + 4, Fv, make_float4(acc1.x * inv, acc1.y * inv, acc1.z * inv, acc1.w * inv));
+  st_row4(orow, f2, Fv, make_float4(acc1.x * inv, acc1.y * inv, acc1.z * inv, acc1.w * inv));
 }
 
 cudaError_t launch_sparse_attention(int n_rows, const int* indptr, const int* indices, const float* Q,

@@ -45,6 +45,14 @@ __device__ __forceinline__ float4 ld4_live(const float* row, int f, int N) {
   return v;
 }
 
+// The float4 at feature f when f < N, else zeros: the features of that
+// float4 past N are the row's padding (any bits).  Only for sums kept per
+// feature (SpMM rows), whose padding features are never stored; a dot
+// product over features needs ld4_live.
+__device__ __forceinline__ float4 ld4_pad(const float* row, int f, int N) {
+  return f < N ? ldg4(row + f) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 // Output rows are written once and not read again by the writing kernel:
 // streaming (evict-first) stores leave L2 to the gathered operand rows.
 __device__ __forceinline__ void st_row4(float* row, int f, int N, float4 v) {

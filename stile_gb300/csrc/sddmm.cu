@@ -280,24 +280,29 @@ __global__ void __launch_bounds__(256, MINB) sddmm_run_kernel(int n_groups, cons
   const int p0 = __ldg(gptr + g), p1 = __ldg(gptr + g + 1);
   using TX = typename std::conditional<kXb, uint16_t, float>::type;
   const TX* __restrict__ xr = static_cast<const TX*>(Xv) + (long)__ldg(grow + g) * ldx;
-  // X's features [f, f + 8) as two float4 (masked past F)
+  // A bf16 Y row gives a lane 8 consecutive features (one 16-byte load);
+  // fp32 rows give it float4 w at features 4 (w LPR + lane), so that each
+  // load instruction of the group reads 16 LPR contiguous bytes.  X follows
+  // Y's split.
+  constexpr int FP = 4 * VEC * LPR;  // features per pass
+  constexpr int kStep = kYb ? 4 : 4 * LPR;  // features between a lane's float4
+  const int f0 = kYb ? 4 * VEC * sl : 4 * sl;
+  // X's features of this lane as VEC float4 (masked past F)
   auto load_x = [&](int f, float4 (&x)[VEC]) {
     if constexpr (kXb) {
       bf16x8_to_f32(kFull ? ldg_u4(xr + f) : ld_row8_bf16(xr, f, F), x[0], x[1]);
     } else {
 #pragma unroll
-      for (int w = 0; w < VEC; ++w) x[w] = kFull ? ldg4(xr + f + 4 * w) : ld4_live(xr, f + 4 * w, F);
+      for (int w = 0; w < VEC; ++w) x[w] = kFull ? ldg4(xr + f + kStep * w) : ld4_live(xr, f + kStep * w, F);
     }
   };
-  constexpr int FP = 4 * VEC * LPR;  // features per pass
-  const int f0 = 4 * VEC * sl;
   auto load_y = [&](int c, int f, float4 (&y)[VEC]) {
     const TY* row = Y + (long)c * ldy;
     if constexpr (kYb) {
       bf16x8_to_f32(kFull ? ldg_u4(row + f) : ld_row8_bf16(row, f, F), y[0], y[1]);
     } else {
 #pragma unroll
-      for (int w = 0; w < VEC; ++w) y[w] = kFull ? ldg4(row + f + 4 * w) : ld4_live(row, f + 4 * w, F);
+      for (int w = 0; w < VEC; ++w) y[w] = kFull ? ldg4(row + f + kStep * w) : ld4_live(row, f + kStep * w, F);
     }
   };
   float4 x1[VEC];

@@ -584,7 +584,11 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
 // ELL tiles as a stream of live entries in row order, packed as 16-byte
 // records {column, value, 2 * row code + run end, 0}.  An LPR-lane
 // sub-group owns one group of <= kSegNnz entries; each lane covers 4 * VEC
-// features of a row.  The sub-group holds the group's records LPR at a time
+// features of a row, float4 w at features 4 (w LPR + lane), so that every
+// load instruction of the sub-group reads 16 LPR contiguous bytes (whole
+// 128-byte lines: the L1 tag stage, not DRAM, limits these gathers, and an
+// interleaved 8-features-per-lane split touched twice the lines per
+// instruction).  The sub-group holds the group's records LPR at a time
 // (one per lane, the next LPR loaded while these are consumed), broadcasts
 // them by shuffle, keeps 4 float4 B-row gathers in flight per lane and
 // flushes the running sum after every entry that ends its row's run (store
@@ -593,7 +597,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
 // instructions per gathered byte halve; no gather waits on a metadata load,
 // and few registers leave room for many warps per SM.
 // kFull: N % (4 * VEC * LPR) == 0, every lane's features are in range
-// (otherwise each float4 is masked by the row's width N).
+// (otherwise a float4 that starts past N reads as zero).
 // kOff32: every B row offset col * ldb fits in 32 bits.
 // kSpanY: blockIdx.y takes features [y span, (y + 1) span) (a wide B over
 // few groups; span = p.ell_fc_span, a multiple of the pass width).
@@ -626,7 +630,9 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
   auto rec = [&](int i) { return i < n ? __ldcs(ent + i) : make_int4(0, 0, 0, 0); };
   for (int fc = kSpanY ? blockIdx.y * p.ell_fc_span : 0;
        fc < (kSpanY ? min(N, (int)(blockIdx.y + 1) * p.ell_fc_span) : N); fc += 4 * VEC * LPR) {
-    const int f = fc + 4 * VEC * sl;
+    // float4 w of this lane holds features f + 4 LPR w: each load
+    // instruction of the group reads 16 LPR contiguous bytes of a row
+    const int f = fc + 4 * sl;
     const float* Bf = p.B + head * p.b_head_stride + f;
     float4 acc[VEC];
 #pragma unroll
@@ -645,12 +651,13 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
           if (kFull) {
             const float* row = kOff32 ? Bf + (unsigned)(c * ldb32) : Bf + (long)c * p.ldb;
 #pragma unroll
-            for (int w = 0; w < VEC; ++w) bv[u][w] = ldg4(row + 4 * w);
+            for (int w = 0; w < VEC; ++w) bv[u][w] = ldg4(row + 4 * LPR * w);
           } else {
-            // features past N (row padding, any bits) read as zero
+            // float4 past N read as zero; padding features inside the last
+            // live float4 only reach features that are never stored
             const float* row = p.B + head * p.b_head_stride + (long)c * p.ldb;
 #pragma unroll
-            for (int w = 0; w < VEC; ++w) bv[u][w] = ld4_live(row, f + 4 * w, N);
+            for (int w = 0; w < VEC; ++w) bv[u][w] = ld4_pad(row, f + 4 * LPR * w, N);
           }
         }
 #pragma unroll
@@ -664,7 +671,7 @@ __global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
             float* row = p.C + head * p.c_head_stride + (long)(code >= 0 ? code : -code - 1) * p.ldc;
 #pragma unroll
             for (int w = 0; w < VEC; ++w) {
-              const int fw = f + 4 * w;
+              const int fw = f + 4 * LPR * w;
               if (code < 0 && p.ell_lazy_wait) griddep_wait();
               if (kFull) {
                 if (code >= 0) __stcs(reinterpret_cast<float4*>(row + fw), acc[w]);  // evict first
@@ -711,12 +718,14 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_bwd_kernel(SpmmArgs p) {
   const int n = __ldg(p.ell_group_ptr + g + 1) - p0;
   const int4* __restrict__ ent = p.ell_entry + p0;
   const int N = p.N;
-  const int f = 8 * sl;
+  // this lane's features: f .. f + 3 and f + 4 LPR .. f + 4 LPR + 3 (each
+  // load instruction of the group reads 16 LPR contiguous bytes of a row)
+  const int f = 4 * sl, f2 = f + 4 * LPR;
   auto rec = [&](int i) { return i < n ? __ldcs(ent + i) : make_int4(0, 0, 0, -1); };
   auto row_of = [](int ce) { const int code = ce >> 1; return code >= 0 ? code : -code - 1; };
   auto ld8 = [&](const float* row, float4& a, float4& b) {
     a = kFull ? ldg4(row + f) : ld4_live(row, f, N);
-    b = kFull ? ldg4(row + f + 4) : ld4_live(row, f + 4, N);
+    b = kFull ? ldg4(row + f2) : ld4_live(row, f2, N);
   };
   float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
   float4 xa0 = acc0, xa1 = acc0;  // dvx row of the last entry handled
@@ -762,17 +771,17 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_bwd_kernel(SpmmArgs p) {
           if (kFull) {
             if (code >= 0) {
               __stcs(reinterpret_cast<float4*>(crow + f), acc0);
-              __stcs(reinterpret_cast<float4*>(crow + f + 4), acc1);
+              __stcs(reinterpret_cast<float4*>(crow + f2), acc1);
             } else {
               atomicAdd(reinterpret_cast<float4*>(crow + f), acc0);
-              atomicAdd(reinterpret_cast<float4*>(crow + f + 4), acc1);
+              atomicAdd(reinterpret_cast<float4*>(crow + f2), acc1);
             }
           } else if (code >= 0) {
             st_row4(crow, f, N, acc0);
-            st_row4(crow, f + 4, N, acc1);
+            st_row4(crow, f2, N, acc1);
           } else {
             red_row4(crow, f, N, acc0);
-            red_row4(crow, f + 4, N, acc1);
+            red_row4(crow, f2, N, acc1);
           }
           acc0 = make_float4(0.f, 0.f, 0.f, 0.f);
           acc1 = acc0;
