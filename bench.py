@@ -460,6 +460,16 @@ class SparseStep:
         return [{f"{k[0]}{'/atomic' if k[1] else ''}": v for k, v in op.plan.summary().items()} for op in self.ops]
 
 
+TC_DESC = {"bf16": "bf16 operands, fp32 accumulate (tcgen05, TMEM)",
+           "tf32": "tf32 operands (B's fp32 rows read as tf32, values rounded to tf32), fp32 accumulate "
+                   "(tcgen05, TMEM)"}
+
+
+def tc_modes():
+    from stile_gb300 import device as D
+    return {"bf16": D.TC_BF16, "tf32": D.TC_TF32}
+
+
 def make_timer(flush):
     import torch
 
@@ -592,7 +602,7 @@ def run_gpu(args):
     t0 = time.time()
     A, layers = make_gcn_workload()
     log(f"[bench] workload {A.shape} nnz={A.nnz} ({time.time() - t0:.1f}s)")
-    tc_mode = D.TC_BF16
+    tc_mode = tc_modes()[args.tc_mode]
     st = SparseStep(A, layers, dev, tc_mode, args.plan_cache)
     log(f"[bench] plans {st.plan_summary()} ({st.plan_s:.1f}s)")
     flops = st.flops
@@ -714,7 +724,7 @@ def run_gpu(args):
 
     if rank == 0:
         cfg = base_config(A, layers, WORKLOAD)
-        cfg.update({"tc_tiles": "bf16 operands, fp32 accumulate (tcgen05, TMEM)", "row_tiles": "fp32 (CUDA cores)",
+        cfg.update({"tc_tiles": TC_DESC[args.tc_mode], "row_tiles": "fp32 (CUDA cores)",
                     "plans": st.plan_summary(), "plan_search_s": round(st.plan_s, 2),
                     "cost_model": st.ops[0].plan.meta.get("cost_model"),
                     "l2": "flushed between steps (256 MiB write, untimed)",
@@ -722,7 +732,7 @@ def run_gpu(args):
         out = {
             "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic", "config": cfg,
+            "vs_baseline": None, "dtype": "f32+" + args.tc_mode, "data": "synthetic", "config": cfg,
             "e2e": {"value": e2e_val, "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
                     "path": "HybridSpMMFunction forward of both layers + torch.autograd.grad, pinned host "
@@ -1003,6 +1013,9 @@ def main():
                     help="gcn2 (the headline line: the two-layer GCN step) or one of the configurations: "
                          "plain, plain_min10, graph, pruned, pruned_t, sddmm, gcn, gcn_41, attention (one JSON "
                          "line of measurements each)")
+    ap.add_argument("--tc-mode", default="bf16", choices=sorted(TC_DESC),
+                    help="tensor-tile arithmetic of the headline step: bf16 (B rows converted to bf16 in the "
+                         "kernel) or tf32 (B's fp32 rows read as tf32); row tiles are fp32 either way")
     ap.add_argument("--plan-cache", default=None,
                     help="directory of the on-disk plan cache (searched plans are stored and reloaded); "
                          "default: search every run")
