@@ -420,6 +420,31 @@ class SparseStep:
             out[f"backward_N{N}_variant"] = op._bwd_choice.get(N, op.cfg.backward)
         return out
 
+    def graph_step_ms(self, timed, steps):
+        """Median ms of the step replayed as one CUDA graph (the same kernels
+        and arguments, captured once; L2 flushed before each replay): the
+        step without the host's per-launch work.  None (with the reason) if
+        the capture fails."""
+        import torch
+        try:
+            side = torch.cuda.Stream(self.dev)
+            side.wait_stream(torch.cuda.current_stream(self.dev))
+            with torch.cuda.stream(side):
+                self.step()
+            torch.cuda.current_stream(self.dev).wait_stream(side)
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self.step()
+            torch.cuda.synchronize()
+            g.replay()
+            torch.cuda.synchronize()
+            t, _ = timed(g.replay, steps)
+            return float(np.median(t)), None
+        except Exception as e:  # noqa: BLE001 -- reported, the eager numbers stand
+            torch.cuda.synchronize()
+            return None, f"{type(e).__name__}: {e}"[:200]
+
     def accuracy(self, layers):
         import oracle.semantics as S
         from stile_gb300 import workloads as W
@@ -643,6 +668,8 @@ def run_gpu(args):
     plain_ms = float(np.sum(plain_times)) / args.steps
     plain_value = flops / (plain_ms * 1e-3) / 1e9
     breakdown = st.breakdown(timed, args.steps)
+    breakdown["step_ms_first_median_min_max"] = [float(times[0]), float(np.median(times)), float(np.min(times)),
+                                                 float(np.max(times))]
 
     # roofline of the dominant kernel: the layer-1 forward SpMM (N = 128)
     fwd_ms = float(np.mean(fwd_times))
@@ -670,6 +697,10 @@ def run_gpu(args):
     main = torch.cuda.current_stream(dev)
     up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
     L = len(layers)
+    # the edge values are a parameter resident on the device (one leaf for
+    # every step, as a training loop holds it): the operators reload them
+    # only when they change
+    v = vals.detach().requires_grad_(True)
 
     def e2e_step():
         ev_b = [torch.cuda.Event() for _ in range(L)]
@@ -682,7 +713,6 @@ def run_gpu(args):
             for i in range(L):
                 dCd[i].copy_(hdC[i], non_blocking=True)
             ev_dc.record(up)
-        v = vals.detach().requires_grad_(True)
         Bin, Cs = [], []
         for i in range(L):
             main.wait_event(ev_b[i])
@@ -721,6 +751,10 @@ def run_gpu(args):
     secondary = run_secondary_graph(dev, tc_mode, args.steps, timed, peak, args.plan_cache) if rank == 0 else None
 
     cpu = run_cpu_baseline(A, layers, flops) if (rank == 0 and world == 1) else None
+    # last: the step as one CUDA graph (a failed capture leaves nothing after it to disturb)
+    breakdown["graph_step_ms"], graph_err = st.graph_step_ms(timed, args.steps)
+    if graph_err:
+        breakdown["graph_error"] = graph_err
 
     if rank == 0:
         cfg = base_config(A, layers, WORKLOAD)

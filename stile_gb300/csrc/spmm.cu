@@ -274,9 +274,15 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
     mbar_init(drain, 1);
     fence_mbar_init();
   }
-  if constexpr (MODE == STILE_TC_FP8) {
-    // the A images' upper k halves stay zero (each k-step fills the lower
-    // half of a K = 32 operand); made visible to the tensor core's proxy
+  // direct copies of a single partial slice (N < 128) skip the 16-byte
+  // chunks wholly past N, which keep the zeros written here (with several
+  // slices a slot also holds full slices, so every chunk is copied, the
+  // ones past N zero-filled)
+  const bool keep_zero = W::kDirect && !kFull && p.n_fchunks == 1;
+  if (MODE == STILE_TC_FP8 || keep_zero) {
+    // fp8: the A images' upper k halves stay zero (each k-step fills the
+    // lower half of a K = 32 operand); made visible to the tensor core's
+    // proxy
     for (int i = tid; i < (int)(kWsSlots * W::kAImg / 16); i += kWsThreads)
       st_shared_v4(slots + W::a_off(0) + 16 * i, make_uint4(0u, 0u, 0u, 0u));
     fence_proxy_async_smem();
@@ -345,7 +351,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
             const int r = 2 * j + rh;
             const int col = __shfl_sync(0xffffffffu, cols, r);
             const uint16_t* row = B16 + (long)col * p.ldb;
-            cp_async16(sa + a_img_off(8 * ch, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
+            if (bytes || !keep_zero) cp_async16(sa + a_img_off(8 * ch, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
           }
         } else {
           // fp32 rows 0..15, features ff + 4 lane .. (a row's 512 bytes per
@@ -356,7 +362,8 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
           for (int r = 0; r < 16; ++r) {
             const int col = __shfl_sync(0xffffffffu, cols, r);
             const float* row = p.B + blockIdx.z * p.b_head_stride + (long)col * p.ldb;
-            cp_async16(sa + a_tf32_off(4 * lane, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
+            if (bytes || !keep_zero)
+              cp_async16(sa + a_tf32_off(4 * lane, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
           }
         }
 #pragma unroll
