@@ -391,21 +391,34 @@ class SparseStep:
         self.flops = step_flops(A, layers)
 
     def forward(self, ev=None):
+        # ev: events at the boundaries of the step's operations (forward of
+        # every layer, then backward of every layer in reverse)
         for i, op in enumerate(self.ops):
             if ev is not None and i == 0:
                 ev[0].record()
             op(self.B[i], out=self.C[i])
-            if ev is not None and i == 0:
-                ev[1].record()
+            if ev is not None:
+                ev[1 + i].record()
 
-    def backward(self):
-        # dB_l and dvals_l from one pass over the transposed plan's tiles
-        for i in reversed(range(len(self.ops))):
+    def backward(self, ev=None):
+        # dB_l and dvals_l (fused or separate, as each operator chose)
+        L = len(self.ops)
+        for j, i in enumerate(reversed(range(L))):
             _, self.dv[i] = self.ops[i].backward(self.dC[i], self.B[i], self.dB[i])
+            if ev is not None:
+                ev[1 + L + j].record()
+
+    def n_events(self):
+        return 1 + 2 * len(self.ops)
+
+    def op_names(self):
+        L = len(self.ops)
+        return ([f"forward_N{self.B[i].shape[1]}" for i in range(L)]
+                + [f"backward_N{self.B[i].shape[1]}" for i in reversed(range(L))])
 
     def step(self, ev=None):
         self.forward(ev)
-        self.backward()
+        self.backward(ev)
 
     def breakdown(self, timed, steps):
         """Median ms of every operation of the step on its own (L2 flushed
@@ -485,16 +498,6 @@ class SparseStep:
         return [{f"{k[0]}{'/atomic' if k[1] else ''}": v for k, v in op.plan.summary().items()} for op in self.ops]
 
 
-TC_DESC = {"bf16": "bf16 operands, fp32 accumulate (tcgen05, TMEM)",
-           "tf32": "tf32 operands (B's fp32 rows read as tf32, values rounded to tf32), fp32 accumulate "
-                   "(tcgen05, TMEM)"}
-
-
-def tc_modes():
-    from stile_gb300 import device as D
-    return {"bf16": D.TC_BF16, "tf32": D.TC_TF32}
-
-
 def make_timer(flush):
     import torch
 
@@ -509,7 +512,8 @@ def make_timer(flush):
         for _ in range(steps):
             flush.zero_()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)] if per_step_events else None
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(int(per_step_events))] \
+                if per_step_events else None
             s.record()
             if per_step_events:
                 fn(ev)
@@ -521,7 +525,9 @@ def make_timer(flush):
             rec.append((s, e, ev))
         torch.cuda.synchronize()
         times = [s.elapsed_time(e) for s, e, _ in rec]
-        fwd = [ev[0].elapsed_time(ev[1]) for _, _, ev in rec] if per_step_events else []
+        # per step: the times between consecutive events
+        fwd = [[ev[k].elapsed_time(ev[k + 1]) for k in range(len(ev) - 1)] for _, _, ev in rec] \
+            if per_step_events else []
         return times, fwd
     return timed
 
@@ -540,9 +546,9 @@ def run_secondary_graph(dev, tc_mode, steps, timed, peak, cache_dir=None):
     acc = st.accuracy(layers)
     for _ in range(3):
         st.step()
-    t, fwd = timed(st.step, steps, per_step_events=True)
+    t, ops_t = timed(st.step, steps, per_step_events=st.n_events())
     ms = float(np.mean(t))
-    fwd_ms = float(np.mean(fwd))
+    fwd_ms = float(np.mean([o[0] for o in ops_t]))
     plain = st.plain()
     for _ in range(3):
         plain()
@@ -627,7 +633,7 @@ def run_gpu(args):
     t0 = time.time()
     A, layers = make_gcn_workload()
     log(f"[bench] workload {A.shape} nnz={A.nnz} ({time.time() - t0:.1f}s)")
-    tc_mode = tc_modes()[args.tc_mode]
+    tc_mode = D.TC_BF16
     st = SparseStep(A, layers, dev, tc_mode, args.plan_cache)
     log(f"[bench] plans {st.plan_summary()} ({st.plan_s:.1f}s)")
     flops = st.flops
@@ -656,7 +662,7 @@ def run_gpu(args):
         # an NVTX range around the timed steps (a profiler's launch list can
         # be limited to it)
         torch.cuda.nvtx.range_push("timed_steps")
-        times, fwd_times = timed(st.step, args.steps, per_step_events=True)
+        times, ops_t = timed(st.step, args.steps, per_step_events=st.n_events())
         torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
@@ -670,9 +676,12 @@ def run_gpu(args):
     breakdown = st.breakdown(timed, args.steps)
     breakdown["step_ms_first_median_min_max"] = [float(times[0]), float(np.median(times)), float(np.min(times)),
                                                  float(np.max(times))]
+    # every operation's median time inside the timed steps (events between them)
+    breakdown["in_step_ms"] = {name: float(np.median([o[k] for o in ops_t]))
+                               for k, name in enumerate(st.op_names())}
 
     # roofline of the dominant kernel: the layer-1 forward SpMM (N = 128)
-    fwd_ms = float(np.mean(fwd_times))
+    fwd_ms = float(np.mean([o[0] for o in ops_t]))
     alg = algorithmic_bytes_spmm(A, WIDTHS[0])
     achieved = alg / (fwd_ms * 1e-3) / 1e9
     gathered = gathered_bytes_spmm(st.ops[0], WIDTHS[0])
@@ -758,7 +767,7 @@ def run_gpu(args):
 
     if rank == 0:
         cfg = base_config(A, layers, WORKLOAD)
-        cfg.update({"tc_tiles": TC_DESC[args.tc_mode], "row_tiles": "fp32 (CUDA cores)",
+        cfg.update({"tc_tiles": "bf16 operands, fp32 accumulate (tcgen05, TMEM)", "row_tiles": "fp32 (CUDA cores)",
                     "plans": st.plan_summary(), "plan_search_s": round(st.plan_s, 2),
                     "cost_model": st.ops[0].plan.meta.get("cost_model"),
                     "l2": "flushed between steps (256 MiB write, untimed)",
@@ -766,7 +775,7 @@ def run_gpu(args):
         out = {
             "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+" + args.tc_mode, "data": "synthetic", "config": cfg,
+            "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic", "config": cfg,
             "e2e": {"value": e2e_val, "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
                     "path": "HybridSpMMFunction forward of both layers + torch.autograd.grad, pinned host "
@@ -1047,9 +1056,6 @@ def main():
                     help="gcn2 (the headline line: the two-layer GCN step) or one of the configurations: "
                          "plain, plain_min10, graph, pruned, pruned_t, sddmm, gcn, gcn_41, attention (one JSON "
                          "line of measurements each)")
-    ap.add_argument("--tc-mode", default="bf16", choices=sorted(TC_DESC),
-                    help="tensor-tile arithmetic of the headline step: bf16 (B rows converted to bf16 in the "
-                         "kernel) or tf32 (B's fp32 rows read as tf32); row tiles are fp32 either way")
     ap.add_argument("--plan-cache", default=None,
                     help="directory of the on-disk plan cache (searched plans are stored and reloaded); "
                          "default: search every run")

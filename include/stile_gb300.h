@@ -58,9 +58,6 @@ extern "C" {
 #define STILE_TC_SPLIT_BF16 4  /* hi+lo bf16 split of A and B, 4 products */
 #define STILE_TC_FP8 3         /* A e4m3 (per-tensor scale), B e4m3 (per tile-row
                                   scale), fp32 accumulate; fp32 B operands */
-#define STILE_TC_TF32 5        /* A tf32 (rounded to nearest), B's fp32 rows read
-                                  as tf32 by the tensor core, fp32 accumulate;
-                                  fp32 B operands */
 
 
 /*
@@ -75,10 +72,7 @@ extern "C" {
  * followed by the lo image (1024 B per k-step).  STILE_TC_FP8 stores, per
  * k-step, the e4m3 bytes of value / tc_row_scale[item * 16 + n] as a K = 32
  * operand whose upper 16 k are zero: byte (n/8)*256 + (k/16)*128 +
- * (n%8)*16 + k%16 (512 B per k-step).  STILE_TC_TF32 stores the fp32 bits
- * of each value rounded to tf32 as two K = 8 operands (k < 8, then k >= 8):
- * byte (k/8)*512 + (n/8)*256 + ((k%8)/4)*128 + (n%8)*16 + (k%4)*4 (1024 B per
- * k-step).
+ * (n%8)*16 + k%16 (512 B per k-step).
  *
  * ELL items: one per row-bucket tile; rows [ell_item_row0[i],
  * ell_item_row0[i+1]), every row with ell_item_K[i] slots starting at
@@ -97,7 +91,7 @@ typedef struct StileSpmmPlanHost {
   const int32_t* tc_out_rows;    /* [tc_n_items * 16] */
   const int32_t* tc_cols;        /* [tc_n_ksteps * 16] */
   const void* tc_vals;           /* [tc_n_ksteps * tc_kstep_bytes] */
-  int32_t tc_kstep_bytes;        /* 512 (bf16/fp16/fp8), 1024 (split, tf32) */
+  int32_t tc_kstep_bytes;        /* 512 (bf16/fp16), 1024 (split) */
   const int32_t* tc_nnz_id;      /* [tc_n_ksteps * 256] row-major (n,k); -1: empty */
   int32_t ell_n_items, ell_n_rows, ell_n_slots;
   const int32_t* ell_item_row0;  /* [ell_n_items + 1] */

@@ -89,8 +89,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
     return fail(STILE_E_INVALID, "negative count");
   const int mode = h->tc_mode;
   if (h->tc_n_items > 0) {
-    if (mode != STILE_TC_BF16 && mode != STILE_TC_F16 && mode != STILE_TC_SPLIT_BF16 && mode != STILE_TC_FP8 &&
-        mode != STILE_TC_TF32)
+    if (mode != STILE_TC_BF16 && mode != STILE_TC_F16 && mode != STILE_TC_SPLIT_BF16 && mode != STILE_TC_FP8)
       return fail(STILE_E_UNSUPPORTED, "tensor-tile mode not supported by this build");
     if (mode == STILE_TC_FP8) {
       if (!h->tc_row_scale) return fail(STILE_E_INVALID, "fp8 tensor tiles need tc_row_scale");
@@ -98,7 +97,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
         if (!(h->tc_row_scale[i] > 0.f) || !(h->tc_row_scale[i] < 3.0e38f))
           return fail(STILE_E_INVALID, "tc_row_scale must be positive and finite");
     }
-    const int want = (mode == STILE_TC_SPLIT_BF16 || mode == STILE_TC_TF32) ? 1024 : 512;
+    const int want = (mode == STILE_TC_SPLIT_BF16) ? 1024 : 512;
     if (h->tc_kstep_bytes != want) return fail(STILE_E_INVALID, "tc_kstep_bytes does not match mode");
     if (!h->tc_item_kbeg || !h->tc_item_flags || !h->tc_out_rows || !h->tc_cols || !h->tc_vals)
       return fail(STILE_E_INVALID, "missing tensor-tile array");
@@ -554,7 +553,7 @@ static int check_dense(long ld, int N, const void* ptr, const char* name) {
 // value sets of a batched run: ELL records, then tensor-tile images, per head
 static size_t values_ell_bytes(const StileSpmmPlan* plan) { return (size_t)plan->ell_n_slots * 16; }
 static size_t values_tc_bytes(const StileSpmmPlan* plan) {
-  const size_t kb = (plan->args.tc_mode == STILE_TC_SPLIT_BF16 || plan->args.tc_mode == STILE_TC_TF32) ? 1024 : 512;
+  const size_t kb = plan->args.tc_mode == STILE_TC_SPLIT_BF16 ? 1024 : 512;
   return (size_t)plan->args.tc_n_ksteps * kb;
 }
 static size_t values_tc_offset(const StileSpmmPlan* plan, int heads) {

@@ -156,21 +156,6 @@ constexpr uint32_t kRawRows = 8192;  // 16 rows x 128 fp32 per stage
 constexpr uint32_t kF8Lbo = 128, kF8Sbo = 256;
 constexpr float kE4m3Max = 448.f;
 
-// tf32 (STILE_TC_TF32): the A image holds the B rows' fp32 bits as copied
-// (the tensor core reads them as tf32), MN-major with the 128-byte swizzle:
-// atoms of 32 features (128 B) x 8 k, the 16-byte chunks of row k XOR-ed
-// with k % 8, four atoms along M 2048 B apart (LBO), the two 8-k groups
-// 1024 B apart (SBO), 8 KB per step; each K = 8 MMA starts at its group.
-// The value image holds two K = 8 operands (K-major, no swizzle, core
-// matrices 8 rows x 16 B, LBO 128 B, SBO 256 B) 512 B apart.
-constexpr uint32_t kTf32Img = 8192, kTf32Vals = 1024;
-constexpr uint32_t kTf32Lbo = 2048, kTf32Sbo = 1024;
-__device__ __forceinline__ uint32_t a_tf32_off(int m, int k) {
-  // m: feature (0..127, a multiple of 4: one 16-byte chunk), k: column (0..15)
-  const int r = k & 7;
-  return (uint32_t)((m >> 5) * kTf32Lbo + (k >> 3) * kTf32Sbo + r * 128 + ((((m & 31) >> 2) ^ r) << 4));
-}
-
 __device__ __forceinline__ uint32_t a_img_off(int m, int k) {
   // m: feature (0..127), k: column within the k-step (0..15)
   const int atom = m >> 6, grp = k >> 3, r = k & 7, chunk = (m & 63) >> 3;
@@ -220,29 +205,22 @@ constexpr int kWsThreads = (kProdWarps + 1 + 4) * 32;   // producers, MMA warp, 
 // stage and every producer warp keeps two steps in flight in its two slots.
 // Slot s holds the A image(s) at a_off(s) (1024-aligned) and the value
 // image(s) at v_off(s): A images first, then all value images.
-//
-// tf32 (kTf32) copies B's fp32 rows the same way, straight into the slot's
-// tf32 A image (no conversion at all), with two steps in flight per
-// producer warp and three CTAs per SM.
 template <int MODE, bool kIn16 = false>
 struct WsCfg {
   static constexpr bool kSplit = MODE == STILE_TC_SPLIT_BF16;
-  static constexpr bool kTf32 = MODE == STILE_TC_TF32;
-  static constexpr bool kDirect = kIn16 || kTf32;                     // copies land in the operand image
-  static constexpr int kSlots = kIn16 ? 3 * kProdWarps : (kTf32 ? 2 * kProdWarps : kProdWarps);  // warp w fills slots w, w + 4, ..
-  static constexpr uint32_t kVals = kTf32 ? kTf32Vals : (kSplit ? 2 * kBStage : kBStage);  // value image(s) per step
-  static constexpr uint32_t kAImg = kTf32 ? kTf32Img : (kSplit ? 2 * kAStage : kAStage);   // A image(s) per step
+  static constexpr int kSlots = kIn16 ? 3 * kProdWarps : kProdWarps;  // warp w fills slots w, w + 4, ..
+  static constexpr uint32_t kVals = kSplit ? 2 * kBStage : kBStage;   // value image(s) per step
+  static constexpr uint32_t kAImg = kSplit ? 2 * kAStage : kAStage;   // A image(s) per step
   static constexpr uint32_t kSlotBytes = kSlots * (kAImg + kVals);
-  static constexpr uint32_t kRaw = kDirect ? 0 : kRawRows + kVals;    // 16 fp32 rows + value image(s)
+  static constexpr uint32_t kRaw = kIn16 ? 0 : kRawRows + kVals;      // 16 fp32 rows + value image(s)
   // full / empty barrier per slot, full / empty per accumulator, drain, TMEM address
   static constexpr uint32_t kBarBytes = (16 * kSlots + 16 * kAccBufs + 16 + 63) / 64 * 64;
   static constexpr uint32_t kBytes = 1024 + kSlotBytes + kProdWarps * kRaw + kBarBytes;
   static __device__ __forceinline__ uint32_t a_off(int s) { return (uint32_t)s * kAImg; }
   static __device__ __forceinline__ uint32_t v_off(int s) { return kSlots * kAImg + (uint32_t)s * kVals; }
-  static constexpr int kCtas = (kSplit || kTf32) ? 3 : 4;             // resident CTAs per SM
+  static constexpr int kCtas = kSplit ? 3 : 4;                        // resident CTAs per SM
   static constexpr int kGroup = kSplit ? 4 : (1 << 30);               // k-steps per accumulator drain
   static_assert(!(kIn16 && MODE != STILE_TC_BF16), "a bf16 B feeds bf16 MMAs");
-  static_assert(kCtas * (kBytes + 1024) <= 228 * 1024, "resident CTAs exceed the SM's shared memory");
 };
 
 // kFull: every 128-feature slice is complete (N % 128 == 0)
@@ -274,11 +252,11 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
     mbar_init(drain, 1);
     fence_mbar_init();
   }
-  // direct copies of a single partial slice (N < 128) skip the 16-byte
-  // chunks wholly past N, which keep the zeros written here (with several
-  // slices a slot also holds full slices, so every chunk is copied, the
-  // ones past N zero-filled)
-  const bool keep_zero = W::kDirect && !kFull && p.n_fchunks == 1;
+  // a bf16 B of a single partial slice (N < 128) skips the 16-byte chunks
+  // wholly past N, which keep the zeros written here (with several slices a
+  // slot also holds full slices, so every chunk is copied, the ones past N
+  // zero-filled)
+  const bool keep_zero = kIn16 && !kFull && p.n_fchunks == 1;
   if (MODE == STILE_TC_FP8 || keep_zero) {
     // fp8: the A images' upper k halves stay zero (each k-step fills the
     // lower half of a K = 32 operand); made visible to the tensor core's
@@ -336,39 +314,23 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
         fn += 128;
       }
     };
-    if constexpr (W::kDirect) {
-      // the step at (l, ff) into `slot`
+    if constexpr (kIn16) {
+      const uint16_t* B16 = reinterpret_cast<const uint16_t*>(p.B) + blockIdx.z * p.b_head_stride;
+      const int ch = lane & 15, rh = lane >> 4;  // this lane's 16-byte chunk (8 features) and row parity
+      // the step at (l, ff) into `slot`: rows 2j + rh, features ff + 8 ch ..
       auto issue16 = [&](int cols, int l, int ff, int slot) {
         const uint32_t sa = slots + W::a_off(slot);
-        if constexpr (kIn16) {
-          // bf16 rows 2j + rh, features ff + 8 ch .. (16-byte chunk ch)
-          const uint16_t* B16 = reinterpret_cast<const uint16_t*>(p.B) + blockIdx.z * p.b_head_stride;
-          const int ch = lane & 15, rh = lane >> 4;
-          const int f = ff + 8 * ch;
-          const uint32_t bytes = kFull ? 16u : ((f + 8 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 2u : 0u));
+        const int f = ff + 8 * ch;
+        const uint32_t bytes = kFull ? 16u : ((f + 8 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 2u : 0u));
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int r = 2 * j + rh;
-            const int col = __shfl_sync(0xffffffffu, cols, r);
-            const uint16_t* row = B16 + (long)col * p.ldb;
-            if (bytes || !keep_zero) cp_async16(sa + a_img_off(8 * ch, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
-          }
-        } else {
-          // fp32 rows 0..15, features ff + 4 lane .. (a row's 512 bytes per
-          // instruction); bytes past N are zero-filled
-          const int f = ff + 4 * lane;
-          const uint32_t bytes = kFull ? 16u : ((f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u));
-#pragma unroll
-          for (int r = 0; r < 16; ++r) {
-            const int col = __shfl_sync(0xffffffffu, cols, r);
-            const float* row = p.B + blockIdx.z * p.b_head_stride + (long)col * p.ldb;
-            if (bytes || !keep_zero)
-              cp_async16(sa + a_tf32_off(4 * lane, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
-          }
+        for (int j = 0; j < 8; ++j) {
+          const int r = 2 * j + rh;
+          const int col = __shfl_sync(0xffffffffu, cols, r);
+          const uint16_t* row = B16 + (long)col * p.ldb;
+          if (bytes || !keep_zero)
+            cp_async16(sa + a_img_off(8 * ch, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
         }
-#pragma unroll
-        for (int c = lane; c < (int)(W::kVals / 16); c += 32)
-          cp_async16(slots + W::v_off(slot) + c * 16, vals + (long)(s_beg + l) * W::kVals + c * 16, 16u);
+        cp_async16(slots + W::v_off(slot) + lane * 16, vals + (long)(s_beg + l) * kBStage + lane * 16, 16u);
         cp_async_commit();
       };
       // kD steps of this warp in flight; once the oldest (g) has landed and
@@ -511,11 +473,9 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       // fp8: e4m3 x e4m3, both operands K-major
-      // tf32: A MN-major (the copied rows), values K-major
-      const uint32_t idesc = (MODE == STILE_TC_F16)    ? make_idesc(0, 0, 1, 0, 128, 16)
-                             : (MODE == STILE_TC_FP8)  ? make_idesc(0, 0, 0, 0, 128, 16)
-                             : (MODE == STILE_TC_TF32) ? make_idesc(2, 2, 1, 0, 128, 16)
-                                                       : make_idesc(1, 1, 1, 0, 128, 16);
+      const uint32_t idesc = (MODE == STILE_TC_F16)   ? make_idesc(0, 0, 1, 0, 128, 16)
+                             : (MODE == STILE_TC_FP8) ? make_idesc(0, 0, 0, 0, 128, 16)
+                                                      : make_idesc(1, 1, 1, 0, 128, 16);
       long g = 0;
       int u = 0;  // accumulation groups issued so far (accumulator u % kAccBufs)
       // failure-detection test: nothing arrives on `drain` before the
@@ -545,18 +505,11 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
             const uint32_t sa = slots + W::a_off(slot), sv = slots + W::v_off(slot);
             const uint64_t a_hi = smem_desc(sa, kALbo, kASbo, kSwizzle128B);
             const uint64_t v_hi = smem_desc(sv, kBLbo, kBSbo, kSwizzleNone);
-            if constexpr (MODE == STILE_TC_FP8) {
+            if constexpr (MODE == STILE_TC_FP8)
               umma_f8(d, smem_desc(sa, kF8Lbo, kF8Sbo, kSwizzleNone), smem_desc(sv, kF8Lbo, kF8Sbo, kSwizzleNone),
                       idesc, s > s0 ? 1u : 0u);
-            } else if constexpr (MODE == STILE_TC_TF32) {
-              // two K = 8 MMAs: k 0..7, then k 8..15
-              umma_tf32(d, smem_desc(sa, kTf32Lbo, kTf32Sbo, kSwizzle128B), smem_desc(sv, kBLbo, kBSbo, kSwizzleNone),
-                        idesc, s > s0 ? 1u : 0u);
-              umma_tf32(d, smem_desc(sa + kTf32Sbo, kTf32Lbo, kTf32Sbo, kSwizzle128B),
-                        smem_desc(sv + 512, kBLbo, kBSbo, kSwizzleNone), idesc, 1u);
-            } else {
+            else
               umma_f16(d, a_hi, v_hi, idesc, s > s0 ? 1u : 0u);
-            }
             if (W::kSplit) {
               umma_f16(d, a_hi, smem_desc(sv + kBStage, kBLbo, kBSbo, kSwizzleNone), idesc, 1u);
               umma_f16(d, smem_desc(sa + kAStage, kALbo, kASbo, kSwizzle128B), v_hi, idesc, 1u);
@@ -980,17 +933,6 @@ __global__ void __launch_bounds__(256, 4) spmm_ell_seg_bf16_kernel(SpmmArgs p) {
 // value re-pack: refresh the plan's tile values from a CSR-ordered value
 // array (used when the matrix values change but the pattern does not)
 // ===========================================================================
-// tf32 value image: 32-bit index of element (row n, column k) of a k-step
-// (two K = 8 operands; core matrices 8 rows x 4 elements)
-__device__ __forceinline__ int tf32_img_index(int n, int k) {
-  return (k >> 3) * 128 + (n >> 3) * 64 + ((k & 7) >> 2) * 32 + (n & 7) * 4 + (k & 3);
-}
-__device__ __forceinline__ uint32_t to_tf32_bits(float v) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
-  return r;
-}
-
 __global__ void repack_values_kernel(SpmmArgs p, const float* __restrict__ vals, int4* ell_entry,
                                      uint16_t* tc_img, long n_ell_slots) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1001,9 +943,7 @@ __global__ void repack_values_kernel(SpmmArgs p, const float* __restrict__ vals,
     const int id = p.tc_nnz_id[i];
     const float v = id >= 0 ? vals[id] : 0.f;
     const int img = (n >> 3) * 128 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7);
-    if (p.tc_mode == STILE_TC_TF32) {
-      reinterpret_cast<uint32_t*>(tc_img)[ks * 256 + tf32_img_index(n, k)] = to_tf32_bits(v);
-    } else if (p.tc_mode == STILE_TC_F16) {
+    if (p.tc_mode == STILE_TC_F16) {
       __half h = __float2half_rn(v);
       tc_img[ks * 256 + img] = *reinterpret_cast<uint16_t*>(&h);
     } else {
@@ -1039,9 +979,7 @@ __global__ void pack_values_kernel(SpmmArgs p, const float* __restrict__ vals, l
     const float v = id >= 0 ? hv[id] : 0.f;
     const int img = (n >> 3) * 128 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7);
     uint16_t* out = tc_out + h * tc_head_elems;
-    if (p.tc_mode == STILE_TC_TF32) {
-      reinterpret_cast<uint32_t*>(out)[ks * 256 + tf32_img_index(n, k)] = to_tf32_bits(v);
-    } else if (p.tc_mode == STILE_TC_F16) {
+    if (p.tc_mode == STILE_TC_F16) {
       __half x = __float2half_rn(v);
       out[ks * 256 + img] = *reinterpret_cast<uint16_t*>(&x);
     } else {
@@ -1205,8 +1143,7 @@ int tc_persistent_ctas(int mode) {
   static std::map<std::pair<int, int>, int> cache;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-  const int cls = mode == STILE_TC_SPLIT_BF16 ? 1 : (mode == STILE_TC_TF32 ? 2 : 0);
-  const std::pair<int, int> key{dev, cls};
+  const std::pair<int, int> key{dev, mode == STILE_TC_SPLIT_BF16 ? 1 : 0};
   {
     std::lock_guard<std::mutex> lock(mu);
     auto it = cache.find(key);
@@ -1214,12 +1151,11 @@ int tc_persistent_ctas(int mode) {
   }
   int sms = 0, per_sm = 0;
   const cudaError_t e =
-      cls == 1   ? resident_ctas(spmm_tc_ws_kernel<STILE_TC_SPLIT_BF16, true, false>, kWsThreads,
-                                 WsCfg<STILE_TC_SPLIT_BF16>::kBytes, &sms, &per_sm)
-      : cls == 2 ? resident_ctas(spmm_tc_ws_kernel<STILE_TC_TF32, true, false>, kWsThreads,
-                                 WsCfg<STILE_TC_TF32>::kBytes, &sms, &per_sm)
-                 : resident_ctas(spmm_tc_ws_kernel<STILE_TC_BF16, true, false>, kWsThreads,
-                                 WsCfg<STILE_TC_BF16>::kBytes, &sms, &per_sm);
+      mode == STILE_TC_SPLIT_BF16
+          ? resident_ctas(spmm_tc_ws_kernel<STILE_TC_SPLIT_BF16, true, false>, kWsThreads,
+                          WsCfg<STILE_TC_SPLIT_BF16>::kBytes, &sms, &per_sm)
+          : resident_ctas(spmm_tc_ws_kernel<STILE_TC_BF16, true, false>, kWsThreads, WsCfg<STILE_TC_BF16>::kBytes,
+                          &sms, &per_sm);
   if (e != cudaSuccess) return 0;
   std::lock_guard<std::mutex> lock(mu);
   cache[key] = sms * per_sm;
@@ -1254,8 +1190,6 @@ cudaError_t launch_tc(const SpmmArgs& args, cudaStream_t st) {
       return p.N % 128 == 0 ? launch_ws_t<STILE_TC_F16, true>(p, st) : launch_ws_t<STILE_TC_F16, false>(p, st);
     case STILE_TC_FP8:
       return p.N % 128 == 0 ? launch_ws_t<STILE_TC_FP8, true>(p, st) : launch_ws_t<STILE_TC_FP8, false>(p, st);
-    case STILE_TC_TF32:
-      return p.N % 128 == 0 ? launch_ws_t<STILE_TC_TF32, true>(p, st) : launch_ws_t<STILE_TC_TF32, false>(p, st);
     case STILE_TC_SPLIT_BF16:
       return p.N % 128 == 0 ? launch_ws_t<STILE_TC_SPLIT_BF16, true>(p, st)
                             : launch_ws_t<STILE_TC_SPLIT_BF16, false>(p, st);

@@ -30,7 +30,7 @@ import scipy.sparse as sp
 from .emit import emit_sddmm_reference, emit_spmm_reference
 from .plan import ELL, ONE_D, TC, TC_SDDMM
 
-TC_BF16, TC_F16, TC_FP8, TC_SPLIT_BF16, TC_TF32 = 1, 2, 3, 4, 5
+TC_BF16, TC_F16, TC_FP8, TC_SPLIT_BF16 = 1, 2, 3, 4
 E4M3_MAX = 448.0
 
 
@@ -86,26 +86,6 @@ def operand_image_16bit(vals16):
     nk = vals16.shape[0]
     v = vals16.reshape(nk, 2, 8, 2, 8)            # (ks, n_grp, n_in, k_grp, k_in)
     v = v.transpose(0, 1, 3, 2, 4)                # (ks, n_grp, k_grp, n_in, k_in)
-    return np.ascontiguousarray(v.reshape(nk, 256))
-
-
-def to_tf32(x):
-    """float32 -> float32 rounded to tf32 (10 explicit mantissa bits): to
-    nearest, ties away from zero (the rounding of cvt.rna.tf32.f32)."""
-    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32)
-    r = ((u.astype(np.uint64) + 0x1000) & 0xFFFFE000).astype(np.uint32)
-    fin = np.isfinite(np.asarray(x, dtype=np.float32))
-    return np.where(fin, r, u).view(np.float32)
-
-
-def operand_image_tf32(vals):
-    """[n_ksteps, 16 (n), 16 (k)] float32 -> [n_ksteps, 256] float32: two
-    K = 8 operands (k < 8, then k >= 8), each K-major without swizzle (core
-    matrices of 8 rows x 4 elements; element (n, k) at 32-bit index
-    (k//8)*128 + (n//8)*64 + ((k%8)//4)*32 + (n%8)*4 + k%4)."""
-    nk = vals.shape[0]
-    v = np.asarray(vals, np.float32).reshape(nk, 2, 8, 2, 2, 4)   # (ks, n_grp, n_in, k_slice, k_core, k_in)
-    v = v.transpose(0, 3, 1, 4, 2, 5)                              # (ks, k_slice, n_grp, k_core, n_in, k_in)
     return np.ascontiguousarray(v.reshape(nk, 256))
 
 
@@ -264,9 +244,6 @@ def build_spmm_device(tiles, A, N=32, tc_mode=TC_BF16, emitted=None):
         lo = _to_bf16_bits(vals_f - _bf16_bits_to_f32(hi))
         img = np.concatenate([operand_image_16bit(hi.reshape(n_ks, 16, 16)),
                               operand_image_16bit(lo.reshape(n_ks, 16, 16))], axis=1)
-        tc_bytes = 1024
-    elif tc_mode == TC_TF32:
-        img = operand_image_tf32(to_tf32(vals_f).reshape(n_ks, 16, 16))
         tc_bytes = 1024
     elif tc_mode == TC_FP8:
         row_scale = fp8_row_scales(vals_f, np.asarray(kbeg, dtype=np.int64))

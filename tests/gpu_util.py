@@ -98,31 +98,18 @@ def a_image_tf32_kmajor(A, lbo=128, sbo=256):
     return img
 
 
-def a_image_tf32_mnmajor(A, lbo=2048, sbo=1024):
-    """A [128 (m) x 8 (k)] fp32, MN-major with the 128-byte swizzle: atoms of
-    32 m (128 B) x 8 k, the 16-byte chunks of row k XOR-ed with k; atoms
-    along m LBO apart (the tensor-tile kernel's tf32 slot layout)."""
-    img = np.zeros(2048, dtype=np.uint32)
-    bits = np.ascontiguousarray(A, dtype=np.float32).view(np.uint32)
-    for m in range(128):
-        for k in range(8):
-            off = (m // 32) * lbo + (k // 8) * sbo + (k % 8) * 128 + ((((m % 32) // 4) ^ (k % 8)) << 4) + (m % 4) * 4
-            img[off // 4] = bits[m, k]
-    return img
-
-
 def run_probe_tf32(A, Bm, desc6=(128, 256, 0, 128, 256, 0), a_kmajor=True):
     import torch
     from stile_gb300 import _lib
     lib = _lib.load()
-    aimg = a_image_tf32_kmajor(A, desc6[0], desc6[1]) if a_kmajor else a_image_tf32_mnmajor(A, desc6[0], desc6[1])
+    assert a_kmajor, "the kernels use K-major tf32 operands only"
+    aimg = a_image_tf32_kmajor(A, desc6[0], desc6[1])
     ai = torch.as_tensor(aimg.view(np.int32).copy(), device="cuda")
     bi = torch.as_tensor(b_image_tf32(Bm, desc6[3], desc6[4]).view(np.int32).copy(), device="cuda")
     out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     d = (ctypes.c_uint32 * 6)(*desc6)
-    a_mn = 0 if a_kmajor else 1
-    idesc = (1 << 4) | (2 << 7) | (2 << 10) | (a_mn << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
+    idesc = (1 << 4) | (2 << 7) | (2 << 10) | (0 << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
     rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, 1, out.data_ptr(), err.data_ptr(),
                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     _lib.check(rc, "probe")

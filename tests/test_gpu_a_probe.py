@@ -32,18 +32,6 @@ def test_umma_tf32_kmajor_layout():
     assert err == 0 and float(np.abs(D - ref).max()) < 1e-3
 
 
-def test_umma_tf32_mnmajor_swizzled_layout():
-    """kind::tf32 with A MN-major and the 128-byte swizzle (atoms of 32 fp32
-    along m x 8 k, LBO 2048 B between atoms), B K-major without swizzle: the
-    tf32 tensor tiles' layout, B rows copied in as fp32."""
-    rng = np.random.default_rng(7)
-    A = tf32_trunc(rng.standard_normal((128, 8)))
-    Bm = tf32_trunc(rng.standard_normal((16, 8)))
-    ref = A.astype(np.float64) @ Bm.astype(np.float64).T
-    D, err = run_probe_tf32(A, Bm, (2048, 1024, 2, 128, 256, 0), a_kmajor=False)
-    assert err == 0 and float(np.abs(D - ref).max()) < 1e-3
-
-
 def test_umma_f8_kmajor_layout():
     """kind::f8f6f4 with e4m3 operands, both K-major without swizzle (core
     matrices 8 rows x 16 B, the two 16-byte k halves 128 B apart, 8-row

@@ -28,8 +28,8 @@ def _needs_tc(plan):
     return any(t.template == "TensorCore_template" for t in plan.tiles)
 
 
-@pytest.mark.parametrize("mode,tol", [(D.TC_BF16, 1e-2), (D.TC_F16, 2e-3), (D.TC_SPLIT_BF16, 1e-5),
-                                      (D.TC_TF32, 2e-3)], ids=["bf16", "f16", "split", "tf32"])
+@pytest.mark.parametrize("mode,tol", [(D.TC_BF16, 1e-2), (D.TC_F16, 2e-3), (D.TC_SPLIT_BF16, 1e-5)],
+                         ids=["bf16", "f16", "split"])
 @pytest.mark.parametrize("path", SPMM_FIXTURES, ids=lambda p: p.split("/")[-1][:-4])
 def test_fused_spmm_matches_fp64(path, mode, tol):
     meta, plan, A = _case(path)
@@ -99,8 +99,7 @@ def test_dvals_matches_fp64_sddmm(path):
     assert S.rel_fro(dv, ref) <= 1e-5
 
 
-@pytest.mark.parametrize("mode,tol", [(D.TC_BF16, 1e-2), (D.TC_SPLIT_BF16, 1e-5), (D.TC_TF32, 2e-3)],
-                         ids=["bf16", "split", "tf32"])
+@pytest.mark.parametrize("mode,tol", [(D.TC_BF16, 1e-2), (D.TC_SPLIT_BF16, 1e-5)], ids=["bf16", "split"])
 def test_set_values_repacks_in_place(mode, tol):
     path = [p for p in SPMM_FIXTURES if "community_1024" in p][0]
     meta, plan, A = _case(path, seed=5)
