@@ -367,6 +367,28 @@ def aligned_empty(rows, n, dev, pin=False):
     return torch.empty((rows, ld), dtype=torch.float32, device=dev)[:, :n]
 
 
+def padded(t):
+    """The row-padded buffer under a [rows, n] view whose row stride exceeds
+    n (a contiguous [rows, stride] tensor on the same storage), else t: a
+    copy between host and device of that buffer is one contiguous
+    asynchronous transfer, where a strided view would go through a
+    synchronous staging copy."""
+    import torch
+    if t.dim() == 2 and t.stride(1) == 1 and t.stride(0) > t.shape[1]:
+        return torch.as_strided(t, (t.shape[0], t.stride(0)), (t.stride(0), 1))
+    return t
+
+
+def xfer(dst, src):
+    """dst <- src across host and device: the padded buffers when both have
+    the same padding (one contiguous asynchronous copy), else the views."""
+    pd, ps = padded(dst), padded(src)
+    if pd.shape == ps.shape:
+        pd.copy_(ps, non_blocking=True)
+    else:
+        dst.copy_(src, non_blocking=True)
+
+
 class SparseStep:
     """The step's sparse products on the GPU for one adjacency and a list of
     layer widths: operators (one plan per width; the transposed operator of
@@ -698,6 +720,7 @@ def run_gpu(args):
     for i, (B, dC) in enumerate(layers):
         hB[i].copy_(torch.as_tensor(B))
         hdC[i].copy_(torch.as_tensor(dC))
+    # every transfer moves the row-padded buffers (contiguous, asynchronous)
     hC = [aligned_empty(A.shape[0], B.shape[1], dev, pin=True) for B, _ in layers]
     hdB = [aligned_empty(A.shape[1], B.shape[1], dev, pin=True) for B, _ in layers]
     hdv = torch.empty(A.nnz, dtype=torch.float32, pin_memory=True)
@@ -717,10 +740,10 @@ def run_gpu(args):
         up.wait_stream(main)
         with torch.cuda.stream(up):
             for i in range(L):
-                Bd[i].copy_(hB[i], non_blocking=True)
+                xfer(Bd[i], hB[i])
                 ev_b[i].record(up)
             for i in range(L):
-                dCd[i].copy_(hdC[i], non_blocking=True)
+                xfer(dCd[i], hdC[i])
             ev_dc.record(up)
         Bin, Cs = [], []
         for i in range(L):
@@ -732,7 +755,7 @@ def run_gpu(args):
             ev_c.record(main)
             down.wait_event(ev_c)
             with torch.cuda.stream(down):
-                hC[i].copy_(Cs[i].detach(), non_blocking=True)
+                xfer(hC[i], Cs[i].detach())
             Cs[i].record_stream(down)
         main.wait_event(ev_dc)
         grads = torch.autograd.grad(Cs, [v] + Bin, grad_outputs=dCd)
@@ -742,7 +765,7 @@ def run_gpu(args):
         with torch.cuda.stream(down):
             hdv.copy_(grads[0], non_blocking=True)
             for i in range(L):
-                hdB[i].copy_(grads[1 + i], non_blocking=True)
+                xfer(hdB[i], grads[1 + i])
         for g_ in grads:
             g_.record_stream(down)
         main.wait_stream(down)
@@ -753,8 +776,8 @@ def run_gpu(args):
     e2e_times, _ = timed(e2e_step, args.steps, host_sync=True)
     e2e_ms = max_over_ranks(float(np.sum(e2e_times)) / args.steps, dev)
     e2e_val = world * flops / (e2e_ms * 1e-3) / 1e9
-    h2d = sum(B.shape[0] * B.shape[1] * 4 + dC.shape[0] * dC.shape[1] * 4 for B, dC in layers)
-    d2h = sum(A.shape[0] * B.shape[1] * 4 + A.shape[1] * B.shape[1] * 4 for B, _ in layers) + A.nnz * 4
+    h2d = sum(padded(hB[i]).numel() * 4 + padded(hdC[i]).numel() * 4 for i in range(L))
+    d2h = sum(padded(hC[i]).numel() * 4 + padded(hdB[i]).numel() * 4 for i in range(L)) + A.nnz * 4
 
     train_ms = gcn_training_step_ms(st, dev, timed, args.steps)
     secondary = run_secondary_graph(dev, tc_mode, args.steps, timed, peak, args.plan_cache) if rank == 0 else None
