@@ -980,6 +980,21 @@ def run_config(args):
                     "roofline_forward": {"algorithmic_bytes": int(alg), "achieved_gbs": alg / (ms_fwd * 1e-3) / 1e9,
                                          "peak_gbs": peak, "frac": alg / (ms_fwd * 1e-3) / 1e9 / peak,
                                          "peak_source": peak_kind}})
+        # the operator left to choose its path (hybrid plan or plain CSR
+        # kernels, timed on these operands at the first call of each width)
+        op_a = SpmmOperator(A, N, PlanConfig(tc_mode=tc_mode, path="auto"), plan=op.plan)
+        Ca, dBa = torch.empty_like(C), torch.empty_like(dB)
+
+        def auto_step():
+            op_a(B, out=Ca)
+            op_a.backward(dC, B, dBa)
+        auto_step()
+        torch.cuda.synchronize()
+        out["auto_path"] = {"forward": op_a._fwd_choice.get(N), "backward": op_a._bwd_choice.get(N),
+                            "ms_per_step": timed(auto_step, args.steps),
+                            "forward_ms": timed(lambda: op_a(B, out=Ca), args.steps),
+                            "C_rel_fro": S.rel_fro(Ca.cpu().numpy(), S.spmm_fp64(A, B_np))}
+        op_a.handle.close()
         if args.workload.startswith("pruned"):
             # activations in bf16, as the configuration has them: read as is
             B16 = B.to(torch.bfloat16)
@@ -1060,6 +1075,10 @@ def run_config(args):
         plain = DeviceSddmmPlan(plain_dev)
         ms_plain = timed(lambda: plain.run(X, Y), args.steps)
         flops = 2 * A.nnz * F
+        op_a = SddmmOperator(A, F, PlanConfig(max_bucket_size=32, path="auto"), plan=op.plan)
+        op_a(X, Y)
+        torch.cuda.synchronize()
+        out["auto_path"] = {"choice": next(iter(op_a._choice.values())), "ms": timed(lambda: op_a(X, Y), args.steps)}
         alg = algorithmic_bytes_sddmm(A, F)
         out.update({"metric": "SDDMM GFLOP/s", "value": flops / (ms * 1e-3) / 1e9, "ms": ms,
                     "plain_list_ms": ms_plain, "speedup_over_plain_list": ms_plain / ms,

@@ -61,6 +61,18 @@ class PlanConfig:
     # tiles) or "auto" (the first backward of each width times both on its
     # own operands and keeps the faster)
     backward: str = "auto"
+    # what runs the operator: "hybrid" (the plan's tiles), "csr" (the plain
+    # kernels over A's CSR arrays: CSR-row SpMM for A and A^T, the entry-list
+    # SDDMM for value gradients and for SddmmOperator) or "auto" (the first
+    # call of each width times the candidates on its own operands and keeps
+    # the fastest; the plan is still searched and held)
+    path: str = "hybrid"
+
+    def __post_init__(self):
+        if self.path not in ("hybrid", "csr", "auto"):
+            raise ValueError(f"path must be 'hybrid', 'csr' or 'auto', not {self.path!r}")
+        if self.backward not in ("fused", "separate", "auto"):
+            raise ValueError(f"backward must be 'fused', 'separate' or 'auto', not {self.backward!r}")
 
     def search_kwargs(self):
         cost = self.cost_model
@@ -78,6 +90,21 @@ def _csr(A):
     A.sum_duplicates()
     A.sort_indices()
     return A
+
+
+def _median_ms(fn, reps=3):
+    """Median of ``reps`` CUDA-event timings of fn() after one warm-up call."""
+    import statistics
+    fn()
+    ts = []
+    for _ in range(reps):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        fn()
+        e.record()
+        e.synchronize()
+        ts.append(s.elapsed_time(e))
+    return statistics.median(ts)
 
 
 def _find_plan(op_type, A, width, kw, cfg, search):
@@ -112,13 +139,52 @@ class SpmmOperator:
         # (weak reference to the tensor, its version, its address) of the
         # values HybridSpMMFunction loaded last
         self._values_key = None
-        # backward variant chosen per dense width ("fused" / "separate")
+        # backward variant chosen per dense width ("fused" / "separate" /
+        # "csr"), forward path chosen per width ("hybrid" / "csr")
         self._bwd_choice = {}
+        self._fwd_choice = {}
+        # plain CSR kernels over A (built on first use): CSR SpMM of A and
+        # of A^T, the entry-list SDDMM over A's nonzeros
+        self._plain = None
+
+    def _plain_ops(self):
+        if self._plain is None:
+            from .ops import CsrMatrix, plain_sddmm_plan
+            csr = CsrMatrix(self.A)
+            opT, perm_t = self.transposed
+            csrT = CsrMatrix(opT.A)
+            if self._vals is not None:
+                csr.set_values(self._vals)
+                csrT.set_values(self._vals[perm_t])
+            self._plain = (csr, csrT, plain_sddmm_plan(self.A))
+        return self._plain
+
+    def forward_path(self, B: torch.Tensor, out: torch.Tensor | None = None) -> str:
+        """The forward path for B's width: the configured one, or with
+        path="auto" the faster of the hybrid plan and the CSR kernel on these
+        operands (timed once per width)."""
+        if self.cfg.path != "auto":
+            return self.cfg.path
+        N = int(B.shape[1])
+        choice = self._fwd_choice.get(N)
+        if choice is None:
+            csr = self._plain_ops()[0]
+            tmp = out if out is not None else torch.empty((self.shape[0], N), dtype=torch.float32, device=B.device)
+            times = {"hybrid": _median_ms(lambda: self.handle.run(B, tmp))}
+            if B.dtype == torch.float32:
+                times["csr"] = _median_ms(lambda: csr.spmm(B, tmp))
+            choice = min(times, key=times.get)
+            self._fwd_choice[N] = choice
+        return choice
 
     def __call__(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        if self.forward_path(B, out) == "csr":
+            return self._plain_ops()[0].spmm(B.float(), out)
         return self.handle.run(B, out)
 
     def dvals(self, dC: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+        if self.cfg.path == "csr" or (self.cfg.path == "auto" and self._bwd_choice.get(int(B.shape[1])) == "csr"):
+            return self._plain_ops()[2].run(dC, B)
         return self.handle.dvals(dC, B)
 
     def backward(self, dC: torch.Tensor, B: torch.Tensor, dB: torch.Tensor | None = None):
@@ -127,40 +193,45 @@ class SpmmOperator:
         separate (transposed product, then the value-gradient pass), as
         ``cfg.backward`` says; "auto" times both once per width."""
         opT, _ = self.transposed
-        choice = self.cfg.backward
-        if choice == "auto":
-            choice = self._bwd_choice.get(int(B.shape[1]))
-            if choice is None:
-                choice = self._tune_backward(opT, dC, B)
-                self._bwd_choice[int(B.shape[1])] = choice
+        if self.cfg.path == "csr":
+            choice = "csr"
+        else:
+            choice = self.cfg.backward
+            if choice == "auto" or self.cfg.path == "auto":
+                choice = self._bwd_choice.get(int(B.shape[1]))
+                if choice is None:
+                    choice = self._tune_backward(opT, dC, B)
+                    self._bwd_choice[int(B.shape[1])] = choice
+        if choice == "csr":
+            _, csrT, sd = self._plain_ops()
+            dvals = sd.run(dC, B)
+            return csrT.spmm(dC, dB), dvals
         if choice == "fused":
             return opT.handle.backward(dC, B, dB)
         dvals = self.handle.dvals(dC, B)
         return opT.handle.run(dC, dB), dvals
 
-    def _tune_backward(self, opT, dC, B, reps=3):
-        """The faster backward variant on these operands: each runs once to
-        warm up, then ``reps`` times between CUDA events; the median wins."""
-        import statistics
-
+    def _tune_backward(self, opT, dC, B):
+        """The fastest backward variant on these operands (the median of
+        three CUDA-event timings after a warm-up call): the hybrid variants
+        the config allows, and the plain CSR kernels with path="auto"."""
         def fused():
             opT.handle.backward(dC, B)
 
         def separate():
             self.handle.dvals(dC, B)
             opT.handle.run(dC)
-        times = {}
-        for name, fn in (("fused", fused), ("separate", separate)):
-            fn()
-            ts = []
-            for _ in range(reps):
-                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                s.record()
-                fn()
-                e.record()
-                e.synchronize()
-                ts.append(s.elapsed_time(e))
-            times[name] = statistics.median(ts)
+
+        def plain():
+            _, csrT, sd = self._plain_ops()
+            sd.run(dC, B)
+            csrT.spmm(dC)
+        cands = {"fused": fused, "separate": separate}
+        if self.cfg.backward != "auto":
+            cands = {self.cfg.backward: cands[self.cfg.backward]}
+        if self.cfg.path == "auto":
+            cands["csr"] = plain
+        times = {name: _median_ms(fn) for name, fn in cands.items()}
         return min(times, key=times.get)
 
     def batched(self, vals: torch.Tensor, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
@@ -176,6 +247,9 @@ class SpmmOperator:
         vals = vals.detach().float().contiguous()
         if vals.numel() != self.nnz:
             raise ValueError("vals must have one entry per nonzero")
+        if self._plain is not None:
+            self._plain[0].set_values(vals)
+            self._plain[1].set_values(vals[self.transposed[1]])
         self.handle.set_values(vals)
         self._vals = vals.clone()
         if self._transposed is not None:
@@ -226,8 +300,34 @@ class SddmmOperator:
         self.plan = plan
         self.device_layout = D.build_sddmm_device(plan.tiles, self.shape, self.nnz)
         self.handle = DeviceSddmmPlan(self.device_layout)
+        self._plain = None        # the entry-list SDDMM over every nonzero (first use)
+        self._choice = {}         # path chosen per (feature count, operand dtype)
+
+    def path(self, X, Y, out=None) -> str:
+        """The configured path, or with path="auto" the faster of the hybrid
+        plan and the plain entry list on these operands (timed once per
+        feature count and operand type)."""
+        if self.cfg.path != "auto":
+            return self.cfg.path
+        key = (int(X.shape[1]), X.dtype == torch.bfloat16 and Y.dtype == torch.bfloat16)
+        choice = self._choice.get(key)
+        if choice is None:
+            from .ops import plain_sddmm_plan
+            if self._plain is None:
+                self._plain = plain_sddmm_plan(self.A)
+            tmp = out if out is not None else torch.empty(self.nnz, dtype=torch.float32, device=X.device)
+            times = {"hybrid": _median_ms(lambda: self.handle.run(X, Y, tmp)),
+                     "csr": _median_ms(lambda: self._plain.run(X, Y, tmp))}
+            choice = min(times, key=times.get)
+            self._choice[key] = choice
+        return choice
 
     def __call__(self, X, Y, out=None):
+        if self.path(X, Y, out) == "csr":
+            if self._plain is None:
+                from .ops import plain_sddmm_plan
+                self._plain = plain_sddmm_plan(self.A)
+            return self._plain.run(X, Y, out)
         return self.handle.run(X, Y, out)
 
 

@@ -372,6 +372,12 @@ class CsrMatrix:
         rows = np.searchsorted(A.indptr, starts, side="right") - 1
         self.group_rows = torch.as_tensor(np.minimum(rows, max(A.shape[0] - 1, 0)).astype(np.int32), device=device)
 
+    def set_values(self, vals: torch.Tensor):
+        """New values in CSR order (one per nonzero)."""
+        if vals.numel() != self.nnz:
+            raise ValueError("vals must have one entry per nonzero")
+        self.vals.copy_(vals.detach().reshape(-1).float())
+
     def spmm(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         B, ldb = dense_operand(B, "B")
         N = B.shape[1]
@@ -383,6 +389,22 @@ class CsrMatrix:
                                                self.vals.data_ptr(), self.group_rows.data_ptr(), B.data_ptr(), ldb,
                                                out.data_ptr(), ldc, N, _stream()), "stile_csr_spmm_run")
         return out
+
+
+def plain_sddmm_plan(A) -> DeviceSddmmPlan:
+    """The entry-list SDDMM over every nonzero of A (CSR order): out[t] =
+    <X[row t], Y[col t]>, the plain comparator of the hybrid plans."""
+    import scipy.sparse as sp
+    from . import device as D
+    A = sp.csr_matrix(A)
+    A.sort_indices()
+    dev = D.SddmmDevice(M=A.shape[0], K=A.shape[1], nnz=A.nnz,
+                        mid_idx=np.repeat(np.arange(A.shape[0]), np.diff(A.indptr)).astype(np.int32),
+                        j_idx=A.indices.astype(np.int32), remap=np.arange(A.nnz, dtype=np.int32),
+                        bm=16, bn=16, blk_i=np.zeros(0, np.int32), blk_j=np.zeros(0, np.int32),
+                        blk_indptr=np.zeros(1, np.int32), blk_dense_pos=np.zeros(0, np.int32),
+                        blk_out=np.zeros(0, np.int32))
+    return DeviceSddmmPlan(dev)
 
 
 def launch_count() -> int:

@@ -295,3 +295,68 @@ def test_backward_auto_choice_is_timed_once_per_width_and_correct():
         assert S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC, B)) <= 1e-5
         assert S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(op.A.T.tocsr(), dC)) <= 1e-5
     assert list(op._bwd_choice) == [64]
+
+
+def test_csr_path_forward_backward_and_value_refresh():
+    """path="csr": the plain CSR kernels run the forward (A), the backward's
+    dB (A^T) and the value gradient (entry list), all in fp32 (<= 1e-5), and
+    they follow new values loaded through the autograd function."""
+    A = _graph(seed=11)
+    N = 41
+    op = plan_spmm(A, N, PlanConfig(path="csr"))
+    rng = np.random.default_rng(5)
+    B = rng.standard_normal((A.shape[1], N)).astype(np.float32)
+    dC = rng.standard_normal((A.shape[0], N)).astype(np.float32)
+    Bd, dCd = torch.as_tensor(B, device="cuda"), torch.as_tensor(dC, device="cuda")
+    assert S.rel_fro(op(Bd).cpu().numpy(), S.spmm_fp64(A, B)) <= 1e-5
+    dB, dv = op.backward(dCd, Bd)
+    assert S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(A.T.tocsr(), dC)) <= 1e-5
+    assert S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC, B)) <= 1e-5
+    new = rng.uniform(-1, 1, A.nnz)
+    A2 = sp.csr_matrix((new, A.indices, A.indptr), shape=A.shape)
+    vals = torch.as_tensor(new.astype(np.float32), device="cuda").requires_grad_(True)
+    Bt = Bd.clone().requires_grad_(True)
+    C = HybridSpMMFunction.apply(vals, Bt, op)
+    assert S.rel_fro(C.detach().cpu().numpy(), S.spmm_fp64(A2, B)) <= 1e-5
+    gv, gB = torch.autograd.grad(C, [vals, Bt], grad_outputs=dCd)
+    assert S.rel_fro(gB.cpu().numpy(), S.spmm_fp64(A2.T.tocsr(), dC)) <= 1e-5
+    assert S.rel_fro(gv.cpu().numpy(), S.sddmm_fp64(A2, dC, B)) <= 1e-5
+
+
+@pytest.mark.parametrize("N", [128, 41])
+def test_auto_path_times_the_candidates_once_and_stays_correct(N):
+    """path="auto": the first forward and backward of a width time the
+    hybrid plan against the plain CSR kernels and keep the faster; either
+    way the results match float64 within the hybrid bound, and later calls
+    reuse the choice."""
+    A = _graph(seed=12)
+    op = plan_spmm(A, N, PlanConfig(path="auto"))
+    rng = np.random.default_rng(6)
+    B = rng.standard_normal((A.shape[1], N)).astype(np.float32)
+    dC = rng.standard_normal((A.shape[0], N)).astype(np.float32)
+    Bd, dCd = torch.as_tensor(B, device="cuda"), torch.as_tensor(dC, device="cuda")
+    for _ in range(2):
+        C = op(Bd).cpu().numpy()
+        assert S.rel_fro(C, S.spmm_fp64(A, B)) <= 1e-2
+        dB, dv = op.backward(dCd, Bd)
+        assert S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(A.T.tocsr(), dC)) <= 1e-2
+        assert S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC, B)) <= 1e-5
+    assert op._fwd_choice[N] in ("hybrid", "csr")
+    assert op._bwd_choice[N] in ("fused", "separate", "csr")
+    assert len(op._fwd_choice) == 1 and len(op._bwd_choice) == 1
+
+
+@pytest.mark.parametrize("bf16", [False, True], ids=["fp32", "bf16"])
+def test_sddmm_auto_path(bf16):
+    mask = syn.community_graph(n=4096, target_nnz=60000, seed=13, max_deg=256)
+    F = 64
+    op = plan_sddmm(mask, F, PlanConfig(path="auto", max_bucket_size=32))
+    rng = np.random.default_rng(8)
+    X = torch.as_tensor(rng.standard_normal((mask.shape[0], F)).astype(np.float32), device="cuda")
+    Y = torch.as_tensor(rng.standard_normal((mask.shape[1], F)).astype(np.float32), device="cuda")
+    if bf16:
+        X, Y = X.to(torch.bfloat16), Y.to(torch.bfloat16)
+    out = op(X, Y).cpu().numpy()
+    assert op._choice and list(op._choice.values())[0] in ("hybrid", "csr")
+    ref = S.sddmm_fp64(sp.csr_matrix(mask), X.float().cpu().numpy(), Y.float().cpu().numpy())
+    assert S.rel_fro(out, ref) <= 1e-5
