@@ -299,13 +299,27 @@ int stile_csr_spmm_run_noalloc(int32_t M, int64_t nnz, const int32_t* indptr,
  *   dvals[s]  = <dC[row(s)], B[col(s)]>    for every nonzero s of A
  * in one pass over A^T's row tiles: each dC row gathered for dB also gives
  * the value gradients of its entries (B's row is held per row run); the
- * tensor-tile nonzeros take a second, row-run pass.  N > 128 runs the
- * product and the gradient pass one after the other.  dvals is fully
- * written when A^T's tiles hold every nonzero. */
+ * tensor-tile nonzeros take a second pass (see stile_spmm_plan_set_dvals_mode).
+ * N > 128 runs the product and the gradient pass one after the other.  dvals
+ * is fully written when A^T's tiles hold every nonzero. */
 int stile_spmm_plan_set_transpose_ids(StileSpmmPlan* planT, const int32_t* perm, int64_t nnz, void* stream);
 int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t lddc,
                         const float* B, int64_t ldb, float* dB, int64_t lddb,
                         float* dvals, int32_t N, void* stream);
+
+/* How stile_spmm_dvals and stile_spmm_backward compute the value gradients
+ * of the tensor-tile nonzeros (no counterpart in the reference, whose
+ * dvals is a separate SDDMM): mode 1 on the tensor cores (a unit of up to 8
+ * k-steps of one tile row block is one M = 128, N = 16 MMA chain over the
+ * gathered fp32 rows split into hi + lo bf16, hi.hi + hi.lo + lo.hi, fp32
+ * accumulation: the item's 16 rows are gathered once per unit and each
+ * k-step's 16 columns once, against one row per nonzero), mode 2 by the
+ * row runs of the entry list (fp32 on CUDA cores), mode 0 (the default at
+ * upload) mode 1 when the tensor tiles hold at least 20 nonzeros per k-step
+ * on average, else mode 2.  Row-tile nonzeros always take the row runs or
+ * the fused ELL pass.  A bf16 B (stile_spmm_dvals_bf16) always takes the
+ * row runs. */
+int stile_spmm_plan_set_dvals_mode(StileSpmmPlan* plan, int32_t mode);
 
 /* Refresh the tile values of a plan from vals[nnz] (device, CSR order of the
  * pattern the plan was built for); the pattern and index arrays are kept.
@@ -332,7 +346,7 @@ int stile_spmm_plan_set_wait_policy(StileSpmmPlan* plan, int32_t polls, int32_t 
 
 /* Tensor-core layout self-check (no counterpart in the reference): runs one
  * tcgen05.mma (M=128, N=16; kind = 0: kind::f16, K=16; kind = 1:
- * kind::tf32, K=8; kind = 2: kind::f8f6f4, K=32; fp32 accumulate) on two 8 KB shared-memory images copied
+ * kind::tf32, K=8; kind = 2: kind::f8f6f4, K=32; fp32 accumulate) on two 16 KB shared-memory images copied
  * verbatim from a_img / b_img, with descriptor fields desc6 = {a_lbo, a_sbo,
  * a_layout, b_lbo, b_sbo, b_layout} (bytes, multiples of 16, <= 2048) and
  * instruction descriptor idesc; writes the 128x16 fp32 accumulator row-major

@@ -156,6 +156,7 @@ EXPORTS = {
                                            ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                            ctypes.c_int32, ctypes.c_void_p]),
     "stile_spmm_plan_set_wait_policy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+    "stile_spmm_plan_set_dvals_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "stile_spmm_plan_error_flag": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, c_i32p]),
     "stile_sddmm_plan_error_flag": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, c_i32p]),
     "stile_debug_umma_probe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,

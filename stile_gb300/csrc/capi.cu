@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "common.cuh"
 #include "spmm.cuh"
 
 namespace {
@@ -58,7 +59,16 @@ struct StileSpmmPlan {
   long nnz = 0, ell_n_slots = 0;
   int n_zero_rows = 0;
   const int* zero_rows = nullptr;
+  long n_tc_dv = 0;  // tensor-tile nonzeros of the value-gradient list
 };
+
+// tensor cores for the tensor tiles' value gradients where the tiles are
+// dense enough that 16 + 16 / 8 row gathers per k-step beat the row runs'
+// one per nonzero with room to spare
+static int tcdv_auto(const StileSpmmPlan* plan) {
+  const stile::SpmmArgs& a = plan->args;
+  return (a.tcdv_n_units > 0 && plan->n_tc_dv >= 20L * a.tc_n_ksteps) ? 1 : 0;
+}
 
 struct StileSddmmPlan {
   void* arena = nullptr;
@@ -424,6 +434,17 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
     }
   }
   if (ndv > INT32_MAX) return fail(STILE_E_INVALID, "too many nonzeros for the value-gradient list");
+  // units of the tensor-tile value-gradient kernel: up to kTcDvUnit k-steps
+  // of one chunk (chunks are in schedule order here, their k-steps
+  // contiguous)
+  std::vector<int32_t> u_ks, u_meta;
+  if (h->tc_nnz_id && h->tc_n_items > 0)
+    for (long c = 0; c < nck; ++c)
+      for (int o = 0; o < ck_nk[c]; o += stile::kTcDvUnit) {
+        u_ks.push_back(ck_kbeg[c] + o);
+        u_meta.push_back(ck_item[c] * stile::kTcDvUnit + std::min(stile::kTcDvUnit, ck_nk[c] - o) - 1);
+      }
+  if ((long)h->tc_n_items * stile::kTcDvUnit > INT32_MAX) return fail(STILE_E_INVALID, "too many tensor-tile items");
 
   Arena ar;
   const long ti = h->tc_n_items, tk = h->tc_n_ksteps;
@@ -448,6 +469,8 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   size_t i_dvi = ar.add(dv_id.data(), (size_t)ndv * 4);
   size_t i_dvgp = ar.add(dv_gptr.data(), dv_gptr.size() * 4);
   size_t i_dvgr = ar.add(dv_grow.data(), dv_grow.size() * 4);
+  size_t i_uks = ar.add(u_ks.data(), u_ks.size() * 4);
+  size_t i_umeta = ar.add(u_meta.data(), u_meta.size() * 4);
   size_t i_err = ar.add(nullptr, 16);
   const bool fp8 = mode == STILE_TC_FP8 && h->tc_n_items > 0;
   size_t i_rsc = ar.add(fp8 ? h->tc_row_scale : nullptr, fp8 ? (size_t)h->tc_n_items * 16 * 4 : 0);
@@ -519,6 +542,12 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   a.tc_cta_chunk = (const int*)P(i_ctac);
   a.tc_chunk_item = (const int*)P(i_cki);
   a.tc_chunk_flags = (const int*)P(i_ckf);
+  a.tcdv_n_units = (int)u_ks.size();
+  a.tcdv_unit_ks = (const int*)P(i_uks);
+  a.tcdv_unit_meta = (const int*)P(i_umeta);
+  a.tcdv_id = a.tc_nnz_id;  // the plan's own numbering until set_transpose_ids
+  plan->n_tc_dv = n_tc_dv;
+  a.tcdv_use = tcdv_auto(plan);
   *out = plan;
   return STILE_OK;
 }
@@ -568,6 +597,7 @@ struct Heads {
 
 static int spmm_run(const StileSpmmPlan* plan, const void* B, bool b_bf16, int64_t ldb, float* C, int64_t ldc,
                     int32_t N, void* stream, const Heads& hd = Heads()) {
+  stile::begin_call();
   if (!plan) return fail(STILE_E_INVALID, "null plan");
   if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
   int rc;
@@ -660,6 +690,7 @@ int64_t stile_spmm_values_bytes(const StileSpmmPlan* plan, int32_t heads) {
 }
 
 int stile_spmm_values_pack(const StileSpmmPlan* plan, const float* vals, int32_t heads, void* packed, void* stream) {
+  stile::begin_call();
   if (!plan || heads < 0) return fail(STILE_E_INVALID, "bad arguments");
   if (plan->args.tc_n_chunks && plan->args.tc_mode == STILE_TC_FP8)
     return fail(STILE_E_UNSUPPORTED, "fp8 tensor tiles take one value set (their scales come with the plan)");
@@ -694,8 +725,12 @@ int stile_spmm_run_batched(const StileSpmmPlan* plan, const void* packed, int32_
   return spmm_run(plan, B, false, ldb, C, ldc, N, stream, hd);
 }
 
+static int tc_dvals(const stile::SpmmArgs& a, const int* run_ids, const float* X, long ldx, const float* Y, long ldy,
+                    float* out, int N, int ell, cudaStream_t st);
+
 static int spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, const void* B, bool b_bf16,
                       int64_t ldb, float* dvals, int32_t N, void* stream) {
+  stile::begin_call();
   if (!plan) return fail(STILE_E_INVALID, "null plan");
   if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
   if (!dvals) return fail(STILE_E_INVALID, "null dvals");
@@ -710,6 +745,13 @@ static int spmm_dvals(const StileSpmmPlan* plan, const float* dY, int64_t lddy, 
   a.b_bf16 = b_bf16 ? 1 : 0;
   a.ldb = ldb;
   a.N = N;
+  if (!b_bf16) {
+    // this plan's own numbering (set_transpose_ids renumbers for the fused
+    // backward only)
+    a.tcdv_id = a.tc_nnz_id;
+    return tc_dvals(a, a.dv_id, dY, lddy, static_cast<const float*>(B), ldb, dvals, N, 1,
+                    static_cast<cudaStream_t>(stream));
+  }
   cudaError_t e = stile::launch_dvals(a, dY, lddy, dvals, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
   g_launches += (a.dv_n > 0);
@@ -727,14 +769,16 @@ int stile_spmm_dvals_bf16(const StileSpmmPlan* plan, const float* dY, int64_t ld
 }
 
 int stile_spmm_plan_set_transpose_ids(StileSpmmPlan* plan, const int32_t* perm, int64_t nnz, void* stream) {
+  stile::begin_call();
   if (!plan || !perm) return fail(STILE_E_INVALID, "null argument");
   if (nnz != plan->nnz) return fail(STILE_E_INVALID, "perm must have one entry per nonzero of the plan");
   if ((plan->args.tc_n_items && !plan->args.tc_nnz_id) || (plan->args.ell_n_groups && !plan->args.ell_nnz_id))
     return fail(STILE_E_INVALID, "plan was uploaded without nonzero ids");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const long n_ell = plan->args.ell_n_groups ? plan->ell_n_slots : 0, n_dv = plan->args.dv_n;
+  const long n_tc = plan->args.tcdv_n_units ? (long)plan->args.tc_n_ksteps * 256 : 0;
   if (!plan->tid_buf) {
-    cudaError_t e = cudaMalloc(&plan->tid_buf, (size_t)(n_ell + n_dv + 1) * 4);
+    cudaError_t e = cudaMalloc(&plan->tid_buf, (size_t)(n_ell + n_dv + n_tc + 1) * 4);
     if (e != cudaSuccess) {
       plan->tid_buf = nullptr;
       return cuda_fail(e, "cudaMalloc(transpose ids)");
@@ -746,15 +790,57 @@ int stile_spmm_plan_set_transpose_ids(StileSpmmPlan* plan, const int32_t* perm, 
   cudaError_t e = stile::launch_record_ids(const_cast<int4*>(plan->args.ell_entry), plan->args.ell_nnz_id, n_ell,
                                            perm, st);
   if (e == cudaSuccess) e = stile::launch_permute_ids(plan->args.dv_id, n_dv, perm, ids + n_ell, st);
+  if (e == cudaSuccess && n_tc)
+    e = stile::launch_permute_ids(plan->args.tc_nnz_id, n_tc, perm, ids + n_ell + n_dv, st);
   if (e != cudaSuccess) return cuda_fail(e, "id permutation launch");
-  g_launches += (n_ell > 0) + (n_dv > 0);
+  g_launches += (n_ell > 0) + (n_dv > 0) + (n_tc > 0);
   plan->args.ell_ids_set = 1;
   plan->args.dvp_id = ids + n_ell;
+  if (n_tc) plan->args.tcdv_id = ids + n_ell + n_dv;
+  return STILE_OK;
+}
+
+// Value gradients out[id] = <X[row], Y[col]> over the plan's entry list (ids
+// `run_ids` in the run list's order, the tensor-tile ones in a.tcdv_id):
+// the tensor-tile nonzeros on the tensor cores when the plan uses them
+// (else by the run list's tensor-core prefix), then, with ell != 0, the
+// row-tile nonzeros by the rest of the run list.
+static int tc_dvals(const stile::SpmmArgs& a, const int* run_ids, const float* X, long ldx, const float* Y, long ldy,
+                    float* out, int N, int ell, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (a.tcdv_use) {
+    e = stile::launch_tc_dvals(a, X, ldx, Y, ldy, out, N, st);
+    if (e != cudaSuccess) return cuda_fail(e, "tensor-tile dvals launch");
+    g_launches += (a.tcdv_n_units > 0);
+    const int n = a.dv_n_groups - a.dv_n_groups_tc;
+    if (ell && n > 0) {
+      e = stile::launch_sddmm_runs(n, a.dv_gptr + a.dv_n_groups_tc, a.dv_grow + a.dv_n_groups_tc, a.dv_col, run_ids,
+                                   X, false, ldx, Y, false, ldy, out, N, st);
+      if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
+      g_launches++;
+    }
+    return STILE_OK;
+  }
+  const int n = ell ? a.dv_n_groups : a.dv_n_groups_tc;
+  e = stile::launch_sddmm_runs(n, a.dv_gptr, a.dv_grow, a.dv_col, run_ids, X, false, ldx, Y, false, ldy, out, N, st);
+  if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
+  g_launches += (n > 0);
+  return STILE_OK;
+}
+
+int stile_spmm_plan_set_dvals_mode(StileSpmmPlan* plan, int32_t mode) {
+  if (!plan) return fail(STILE_E_INVALID, "null plan");
+  if (mode < 0 || mode > 2) return fail(STILE_E_INVALID, "mode must be 0 (auto), 1 (tensor cores) or 2 (row runs)");
+  stile::SpmmArgs& a = plan->args;
+  if (mode == 1 && a.tc_n_ksteps > 0 && a.tcdv_n_units == 0)
+    return fail(STILE_E_INVALID, "plan was uploaded without nonzero ids");
+  a.tcdv_use = mode == 0 ? tcdv_auto(plan) : (mode == 1 && a.tcdv_n_units > 0) ? 1 : 0;
   return STILE_OK;
 }
 
 int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t lddc, const float* B, int64_t ldb,
                         float* dB, int64_t lddb, float* dvals, int32_t N, void* stream) {
+  stile::begin_call();
   if (!planT) return fail(STILE_E_INVALID, "null plan");
   if (N <= 0) return fail(STILE_E_INVALID, "N must be positive");
   if (!dvals) return fail(STILE_E_INVALID, "null dvals");
@@ -781,11 +867,7 @@ int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t ldd
     // wider than one feature pass (or no row tiles): the transposed product,
     // then the gradient of every nonzero from the run list
     if ((rc = spmm_run(planT, dC, false, lddc, dB, lddb, N, stream)) != 0) return rc;
-    e = stile::launch_sddmm_runs(a.dv_n_groups, a.dv_gptr, a.dv_grow, a.dv_col, a.dvp_id, B, false, ldb, dC, false,
-                                 lddc, dvals, N, st);
-    if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
-    g_launches += (a.dv_n_groups > 0);
-    return STILE_OK;
+    return tc_dvals(a, a.dvp_id, B, ldb, dC, lddc, dvals, N, 1, st);
   }
   bool zero_kernel = false;
   if (2L * planT->n_zero_rows >= planT->M) {
@@ -804,16 +886,14 @@ int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t ldd
   e = stile::launch_tc(a, st);
   if (e != cudaSuccess) return cuda_fail(e, "tensor-core SpMM launch");
   if (a.tc_n_chunks) g_launches++;
-  // the tensor-core nonzeros' gradients: the run list's tensor-core prefix
-  // (rows of A^T hold B's rows, columns dC's)
-  e = stile::launch_sddmm_runs(a.dv_n_groups_tc, a.dv_gptr, a.dv_grow, a.dv_col, a.dvp_id, B, false, ldb, dC, false,
-                               lddc, dvals, N, st);
-  if (e != cudaSuccess) return cuda_fail(e, "dvals launch");
-  g_launches += (a.dv_n_groups_tc > 0);
+  // the tensor-core nonzeros' gradients (rows of A^T hold B's rows,
+  // columns dC's): on the tensor cores, or the run list's tensor-core prefix
+  if ((rc = tc_dvals(a, a.dvp_id, B, ldb, dC, lddc, dvals, N, 0, st)) != 0) return rc;
   return STILE_OK;
 }
 
 int stile_spmm_plan_set_values(StileSpmmPlan* plan, const float* vals, void* stream) {
+  stile::begin_call();
   if (!plan || !vals) return fail(STILE_E_INVALID, "null argument");
   if (plan->args.tc_n_chunks && plan->args.tc_mode == STILE_TC_FP8)
     return fail(STILE_E_UNSUPPORTED, "fp8 tensor tiles: new values need a new upload (their row scales change)");
@@ -853,6 +933,7 @@ int stile_sparse_attention(int32_t n_rows, const int32_t* indptr, const int32_t*
                            int64_t q_head_stride, int64_t k_head_stride, int64_t v_head_stride, float* out,
                            int64_t ldo, int64_t out_head_stride, int32_t F, int32_t Fv, float scale, int32_t heads,
                            void* stream) {
+  stile::begin_call();
   if (n_rows < 0 || heads < 0) return fail(STILE_E_INVALID, "bad shape");
   if (F <= 0 || Fv <= 0 || F > 128 || Fv > 128)
     return fail(STILE_E_UNSUPPORTED, "fused attention takes 1..128 features for Q/K and for V");
@@ -888,6 +969,7 @@ int stile_sddmm_plan_error_flag(StileSddmmPlan* plan, void* stream, int32_t* fla
 
 int stile_csr_row_softmax(int32_t M, const int32_t* indptr, int64_t nnz, const float* x, float* out, float scale,
                           int32_t batch, void* stream) {
+  stile::begin_call();
   if (M < 0 || nnz < 0 || batch < 0) return fail(STILE_E_INVALID, "bad shape");
   if (M > 0 && !indptr) return fail(STILE_E_INVALID, "null indptr");
   if (nnz > 0 && batch > 0 && (!x || !out)) return fail(STILE_E_INVALID, "null values");
@@ -901,6 +983,7 @@ int stile_csr_row_softmax(int32_t M, const int32_t* indptr, int64_t nnz, const f
 int stile_csr_spmm_run(int32_t M, int64_t nnz, const int32_t* indptr, const int32_t* indices, const float* vals,
                        const int32_t* group_rows, const float* B, int64_t ldb, float* C, int64_t ldc, int32_t N,
                        void* stream) {
+  stile::begin_call();
   if (M < 0 || N <= 0) return fail(STILE_E_INVALID, "bad shape");
   if (M == 0) return STILE_OK;
   if (!indptr || !indices || !vals) return fail(STILE_E_INVALID, "null CSR array");
@@ -1021,6 +1104,7 @@ int stile_sddmm_plan_free(StileSddmmPlan* plan) {
 
 static int sddmm_run(const StileSddmmPlan* plan, const void* X, int64_t ldx, const void* Y, int64_t ldy, bool bf16,
                      float* out, int32_t F, void* stream) {
+  stile::begin_call();
   if (!plan) return fail(STILE_E_INVALID, "null plan");
   if (F <= 0) return fail(STILE_E_INVALID, "F must be positive");
   if (plan->nnz == 0) return STILE_OK;  // an empty mask: nothing to compute

@@ -85,8 +85,20 @@ __device__ __forceinline__ void griddep_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// The kernels of one C-API call chain as programmatic dependents, but the
+// first kernel a call launches is an ordinary launch: it starts only after
+// everything before it on the stream (the previous call's kernels) has
+// completed.  Blocks of the next operator launched early onto the SMs of
+// the previous operator's persistent tensor-core grid slowed that grid's
+// tail: the two-layer GCN step (four operator calls) took 2.26 ms with the
+// chain running across calls and 1.96 ms with it cut at every call.
+// Every entry point that launches kernels calls begin_call() first.
+inline thread_local bool t_call_start = false;
+inline void begin_call() { t_call_start = true; }
+
 // Launch with programmatic stream serialization (see griddep_wait): the
-// kernel may start while the previous kernel on the stream drains.
+// kernel may start while the previous kernel on the stream drains; the
+// first launch after begin_call() is an ordinary launch.
 template <typename... KArgs, typename... Args>
 static inline cudaError_t launch_dependent(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
                                     Args... args) {
@@ -99,7 +111,8 @@ static inline cudaError_t launch_dependent(void (*k)(KArgs...), dim3 grid, dim3 
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = t_call_start ? 0 : 1;
+  t_call_start = false;
   return cudaLaunchKernelEx(&cfg, k, args...);
 }
 

@@ -21,6 +21,7 @@
 #include <string>
 
 #include "../../include/stile_gb300.h"
+#include "common.cuh"
 #include "spmm.cuh"
 
 namespace stile {
@@ -79,6 +80,7 @@ extern "C" int stile_csr_spmm_run_noalloc(int32_t M, int64_t nnz, const int32_t*
     return stile::report_error(STILE_E_INVALID, "row strides must be >= N and multiples of 4");
   if ((reinterpret_cast<uintptr_t>(B) & 15) != 0 || (reinterpret_cast<uintptr_t>(C) & 15) != 0)
     return stile::report_error(STILE_E_INVALID, "B and C must be 16-byte aligned");
+  stile::begin_call();
   int* group_rows = nullptr;
   cudaError_t e = stile::scratch_for_current_device(&group_rows);
   if (e != cudaSuccess) return stile::report_error(STILE_E_CUDA, cudaGetErrorString(e));

@@ -1,21 +1,21 @@
 // Layout self-check for the tensor-core path: one CTA copies two operand
 // images verbatim into shared memory, issues one tcgen05.mma (M=128, N=16;
 // kind::f16 with K=16, kind::tf32 with K=8 or kind::f8f6f4 with K=32; fp32
-// accumulate) with
-// caller-chosen descriptor fields and
-// writes the 128x16 accumulator to global memory.  Every descriptor the
-// caller can pass stays inside the CTA's shared memory: each operand gets a
-// 32 KB zero-filled region, the image occupies its first 8 KB, and the host
-// limits strides to 2048 B so that even 16 groups along one direction times
-// the largest stride (plus one 1 KB atom) stay below 32 KB.  A wrong layout
-// yields wrong numbers, never an out-of-bounds access.
+// accumulate) with caller-chosen descriptor fields and writes the 128x16
+// accumulator to global memory.  Every descriptor the caller can pass stays
+// inside the CTA's shared memory: each operand gets a 48 KB zero-filled
+// region, the image occupies its first 16 KB (a 128-row K-major operand
+// with the 128-byte swizzle spans 16 KB), and the host limits strides to
+// 2048 B so that 16 groups along one direction times the largest stride
+// plus a 16 KB span stay below 48 KB.  A wrong layout yields wrong numbers,
+// never an out-of-bounds access.
 #include "common.cuh"
 #include "spmm.cuh"
 
 namespace stile {
 
-constexpr int kProbeImage = 8192;    // bytes of one operand image
-constexpr int kProbeRegion = 32768;  // shared-memory region per operand
+constexpr int kProbeImage = 16384;   // bytes of one operand image
+constexpr int kProbeRegion = 49152;  // shared-memory region per operand
 
 __global__ void __launch_bounds__(128) umma_probe_kernel(const uint4* __restrict__ a_img,
                                                          const uint4* __restrict__ b_img,

@@ -1335,6 +1335,176 @@ cudaError_t launch_ell_bwd(const SpmmArgs& p, cudaStream_t st) {
   }
 }
 
+// Value gradients of the tensor-tile nonzeros on the tensor cores.
+//
+// A unit is up to 8 k-steps of one chunk (one item): its 128 k-step columns
+// (16 per k-step) are the M = 128 rows of the MMA's A operand, the item's 16
+// rows its N = 16 B operand, the features its K, so
+//   D[16 j + k][r] = <Y[col(j, k)], X[row r]>
+// is the gradient of the nonzero (r, k) of k-step j.  The item's 16 X rows
+// are gathered once per unit, the columns once per k-step (the row-run
+// kernel gathers one row per nonzero: ~41 per k-step on the GCN graph).
+// Per 64-feature chunk every 16-lane half-warp gathers one row (a float4 a
+// lane, 256 contiguous bytes), splits it into hi = bf16(x) and
+// lo = bf16(x - hi), and stores both into K-major images with the 128-byte
+// swizzle (128-byte rows of 64 features, the 16-byte chunk q of row m at
+// q ^ (m % 8), 8-row atoms 1 KB apart), so each half-warp writes one
+// 128-byte row: no bank conflicts.  One thread issues hi.hi + hi.lo + lo.hi
+// per 16-feature slice (the K advance is 32 bytes inside the atom row) into
+// a 16-column TMEM accumulator; the epilogue reads lane m = 16 j + k and
+// writes the live entries through the k-step's id table.  The wait for the
+// MMAs is bounded; a wait that runs out sets the error flag and ends the
+// kernel's work.
+constexpr uint32_t kDvYImg = 16384;  // 128 rows x 64 bf16
+constexpr uint32_t kDvXImg = 2048;   // 16 rows x 64 bf16
+constexpr uint32_t kDvBytes = 1024 + 2 * kDvYImg + 2 * kDvXImg + 64 + 64;
+
+__device__ __forceinline__ uint32_t sw128_off(int row, int q) {
+  return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((q ^ (row & 7)) << 4));
+}
+
+__global__ void __launch_bounds__(128) spmm_tc_dvals_kernel(SpmmArgs p, const float* __restrict__ X, long ldx,
+                                                              const float* __restrict__ Y, long ldy,
+                                                              float* __restrict__ out, int F) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const uint32_t yhi = base, ylo = base + kDvYImg, xhi = base + 2 * kDvYImg, xlo = xhi + kDvXImg;
+  const uint32_t orow_s = xlo + kDvXImg, bar = orow_s + 64, tmem_slot = bar + 8;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, hw = lane >> 4, sl = lane & 15;
+  griddep_wait();  // X and Y may come from the previous kernel
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(tmem_slot, 32);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  uint32_t tmem;
+  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
+  // kind::f16, bf16 x bf16, M = 128, N = 16, both operands K-major
+  constexpr uint32_t idesc = make_idesc(1, 1, 0, 0, 128, 16);
+  uint32_t phase = 0;
+  bool ok = true;
+  // one float4 of a gathered row -> hi and lo bf16 halves of its 16-byte chunk
+  auto put = [&](uint32_t hi_img, uint32_t lo_img, int row, float4 v) {
+    const uint32_t o = sw128_off(row, sl >> 1) + (sl & 1) * 8;
+    const uint32_t h01 = pack_bf16x2(v.x, v.y), h23 = pack_bf16x2(v.z, v.w);
+    st_shared_v2(hi_img + o, h01, h23);
+    st_shared_v2(lo_img + o, pack_bf16x2(v.x - __uint_as_float(h01 << 16), v.y - __uint_as_float(h01 & 0xffff0000u)),
+                 pack_bf16x2(v.z - __uint_as_float(h23 << 16), v.w - __uint_as_float(h23 & 0xffff0000u)));
+  };
+#pragma unroll 1
+  for (int u = blockIdx.x; u < p.tcdv_n_units && ok; u += gridDim.x) {
+    const int ks0 = __ldg(p.tcdv_unit_ks + u);
+    const int meta = __ldg(p.tcdv_unit_meta + u);
+    const int item = meta >> 3, nks = (meta & 7) + 1;
+    // this half-warp's rows: 8 i + 2 warp + hw (16 of the 128 columns, 2 of
+    // the 16 item rows)
+    int ycol[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int m = 8 * i + 2 * warp + hw, j = m >> 4;
+      ycol[i] = j < nks ? __ldg(p.tc_cols + (long)(ks0 + j) * 16 + (m & 15)) : -1;
+    }
+    int xrow[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) xrow[i] = __ldg(p.tc_out_rows + (long)item * 16 + 8 * i + 2 * warp + hw);
+    if (sl == 0) {
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+        asm volatile("st.shared.b32 [%0], %1;" ::"r"(orow_s + 4 * (8 * i + 2 * warp + hw)), "r"(xrow[i]) : "memory");
+    }
+#pragma unroll 1
+    for (int fc = 0; fc < F; fc += 64) {
+      const int f = fc + 4 * sl;
+      // gather: 8 Y rows at a time in flight, then the 2 X rows
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        float4 v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int c = ycol[8 * h + i];
+          v[i] = c >= 0 ? ld4_live(Y + (long)c * ldy, f, F) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) put(yhi, ylo, 8 * (8 * h + i) + 2 * warp + hw, v[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const float4 v = xrow[i] >= 0 ? ld4_live(X + (long)xrow[i] * ldx, f, F) : make_float4(0.f, 0.f, 0.f, 0.f);
+        put(xhi, xlo, 8 * i + 2 * warp + hw, v);
+      }
+      fence_proxy_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      if (tid == 0) {
+        const int ns = min(4, (F - fc + 15) / 16);
+        for (int s = 0; s < ns; ++s) {
+          const uint64_t ah = smem_desc(yhi + 32 * s, 16, 1024, kSwizzle128B);
+          const uint64_t bh = smem_desc(xhi + 32 * s, 16, 1024, kSwizzle128B);
+          umma_f16(tmem, ah, bh, idesc, (fc > 0 || s > 0) ? 1u : 0u);
+          umma_f16(tmem, ah, smem_desc(xlo + 32 * s, 16, 1024, kSwizzle128B), idesc, 1u);
+          umma_f16(tmem, smem_desc(ylo + 32 * s, 16, 1024, kSwizzle128B), bh, idesc, 1u);
+        }
+        umma_commit(bar);
+      }
+      // the MMAs read the images: nobody rewrites them, or reads TMEM, first
+      const bool done = __syncthreads_and(tid == 0 ? mbar_wait_bounded(bar, phase) : true) != 0;
+      phase ^= 1u;
+      if (!done) {
+        ok = false;
+        break;
+      }
+      if (tid != 0) mbar_wait_bounded(bar, phase ^ 1u);  // completed: returns at once
+      tc_fence_after();
+    }
+    if (!ok) break;
+    // epilogue: warp w holds TMEM lanes m = 32 w .. 32 w + 31 (k-steps 2 w
+    // and 2 w + 1), columns r = 0..15
+    uint32_t v[16];
+    tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16), v);
+    tmem_wait_ld();
+    const int m = 32 * warp + lane, j = m >> 4, k = m & 15;
+    if (j < nks) {
+      const int* ids = p.tcdv_id + (long)(ks0 + j) * 256 + k;
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        int orow;
+        asm volatile("ld.shared.b32 %0, [%1];" : "=r"(orow) : "r"(orow_s + 4 * r) : "memory");
+        const int id = __ldcs(ids + 16 * r);
+        if (id >= 0 && orow >= 0) __stcs(out + id, __uint_as_float(v[r]));
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (!ok && tid == 0 && p.err_flag) atomicOr(p.err_flag, 1);
+  // every MMA this CTA issued has completed before TMEM is freed
+  if (!ok && tid == 0) mbar_wait_bounded(bar, phase ^ 1u);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, 32);
+}
+
+cudaError_t launch_tc_dvals(const SpmmArgs& p, const float* X, long ldx, const float* Y, long ldy, float* out, int F,
+                            cudaStream_t st) {
+  if (p.tcdv_n_units == 0) return cudaSuccess;
+  if (!p.tcdv_id) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(spmm_tc_dvals_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kDvBytes);
+  if (e != cudaSuccess) return e;
+  // 37 KB of shared memory and 32 TMEM columns per CTA: 4 CTAs per SM
+  const int grid = std::min(p.tcdv_n_units, device_sm_count() * 4);
+  return launch_dependent(spmm_tc_dvals_kernel, dim3((unsigned)grid), dim3(128), kDvBytes, st, p, X, ldx, Y, ldy,
+                          out, F);
+}
+
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {
   return launch_sddmm_runs(p.dv_n_groups, p.dv_gptr, p.dv_grow, p.dv_col, p.dv_id, dY, false, lddy, p.B,
                            p.b_bf16 != 0, p.ldb, dvals, p.N, st);

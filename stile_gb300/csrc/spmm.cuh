@@ -96,6 +96,17 @@ struct SpmmArgs {
   int ell_ids_set;
   const int* dvp_id;
   int dv_n_groups_tc;
+  // value gradients of the tensor-tile nonzeros on the tensor cores: units
+  // of up to 8 k-steps of one chunk (tcdv_unit_ks: first k-step in schedule
+  // order; tcdv_unit_meta: item * 8 + k-steps - 1); tcdv_id: the k-steps'
+  // nonzero ids ([tc_n_ksteps * 256], (row, column) order) in the numbering
+  // of the gradient (the plan's own, or the forward operator's after
+  // set_transpose_ids); tcdv_use: use them (else the row runs)
+  int tcdv_n_units;
+  const int* tcdv_unit_ks;
+  const int* tcdv_unit_meta;
+  const int* tcdv_id;
+  int tcdv_use;
 };
 
 cudaError_t launch_csr_spmm(int M, const int* indptr, const int* indices, const float* vals,
@@ -124,6 +135,12 @@ cudaError_t launch_permute_ids(const int* in, long n, const int* perm, int* out,
 // ent[i].w = ids[i] >= 0 ? perm[ids[i]] : -1
 cudaError_t launch_record_ids(int4* ent, const int* ids, long n, const int* perm, cudaStream_t st);
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st);
+// out[id] = <X[item row], Y[k-step column]> for the tensor-tile nonzeros
+// (fp32 X and Y, F features), on the tensor cores with hi + lo bf16
+// operands; ids from p.tcdv_id
+cudaError_t launch_tc_dvals(const SpmmArgs& p, const float* X, long ldx, const float* Y, long ldy, float* out, int F,
+                            cudaStream_t st);
+constexpr int kTcDvUnit = 8;  // k-steps per unit of the tensor-tile value-gradient kernel
 constexpr int kChunkSteps = 32;
 cudaError_t launch_pack_values(const SpmmArgs& p, const float* vals, long nnz, int heads, void* ell_out,
                                void* tc_out, long n_ell, long tc_head_bytes, cudaStream_t st);

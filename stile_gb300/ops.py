@@ -287,6 +287,11 @@ class DeviceSpmmPlan:
         _lib.check(self.lib.stile_spmm_plan_set_wait_policy(self.handle, int(polls), 1 if stall_test else 0),
                    "stile_spmm_plan_set_wait_policy")
 
+    def set_dvals_mode(self, mode: int):
+        """Value gradients of the tensor-tile nonzeros: 0 automatic, 1 on the
+        tensor cores, 2 by the row runs (stile_spmm_plan_set_dvals_mode)."""
+        _lib.check(self.lib.stile_spmm_plan_set_dvals_mode(self.handle, int(mode)), "stile_spmm_plan_set_dvals_mode")
+
     def error_flag(self) -> int:
         f = ctypes.c_int32(0)
         _lib.check(self.lib.stile_spmm_plan_error_flag(self.handle, _stream(), ctypes.byref(f)),

@@ -37,12 +37,26 @@ def b_image(Bm):
     return img
 
 
+PROBE_IMAGE_BYTES = 16384   # the probe copies this many bytes of each image
+
+
+def probe_image(img):
+    """A device copy of an operand image, zero-padded to the probe's image
+    size."""
+    import torch
+    raw = np.frombuffer(np.ascontiguousarray(img).tobytes(), dtype=np.uint8)
+    assert raw.size <= PROBE_IMAGE_BYTES
+    buf = np.zeros(PROBE_IMAGE_BYTES, dtype=np.uint8)
+    buf[:raw.size] = raw
+    return torch.as_tensor(buf, device="cuda")
+
+
 def run_probe(A, Bm, desc6):
     import torch
     from stile_gb300 import _lib
     lib = _lib.load()
-    ai = torch.as_tensor(a_image(A, desc6[0], desc6[1]).view(np.int16).copy(), device="cuda")
-    bi = torch.as_tensor(b_image(Bm).view(np.int16).copy(), device="cuda")
+    ai = probe_image(a_image(A, desc6[0], desc6[1]))
+    bi = probe_image(b_image(Bm))
     out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     d = (ctypes.c_uint32 * 6)(*desc6)
@@ -104,8 +118,8 @@ def run_probe_tf32(A, Bm, desc6=(128, 256, 0, 128, 256, 0), a_kmajor=True):
     lib = _lib.load()
     assert a_kmajor, "the kernels use K-major tf32 operands only"
     aimg = a_image_tf32_kmajor(A, desc6[0], desc6[1])
-    ai = torch.as_tensor(aimg.view(np.int32).copy(), device="cuda")
-    bi = torch.as_tensor(b_image_tf32(Bm, desc6[3], desc6[4]).view(np.int32).copy(), device="cuda")
+    ai = probe_image(aimg)
+    bi = probe_image(b_image_tf32(Bm, desc6[3], desc6[4]))
     out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     d = (ctypes.c_uint32 * 6)(*desc6)
@@ -147,8 +161,8 @@ def run_probe_f8(Abytes, Bbytes):
     import torch
     from stile_gb300 import _lib
     lib = _lib.load()
-    ai = torch.as_tensor(kmajor_image_8bit(Abytes), device="cuda")
-    bi = torch.as_tensor(kmajor_image_8bit(Bbytes), device="cuda")
+    ai = probe_image(kmajor_image_8bit(Abytes))
+    bi = probe_image(kmajor_image_8bit(Bbytes))
     out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     d = (ctypes.c_uint32 * 6)(128, 256, 0, 128, 256, 0)
@@ -180,11 +194,45 @@ def run_probe_bf16_kmajor(A, Bm):
     import torch
     from stile_gb300 import _lib
     lib = _lib.load()
-    ai = torch.as_tensor(kmajor_image_16bit(A).view(np.int16).copy(), device="cuda")
-    bi = torch.as_tensor(kmajor_image_16bit(Bm).view(np.int16).copy(), device="cuda")
+    ai = probe_image(kmajor_image_16bit(A))
+    bi = probe_image(kmajor_image_16bit(Bm))
     out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     d = (ctypes.c_uint32 * 6)(128, 256, 0, 128, 256, 0)
+    idesc = (1 << 4) | (1 << 7) | (1 << 10) | (0 << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
+    rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, 0, out.data_ptr(), err.data_ptr(),
+                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc, "probe")
+    torch.cuda.synchronize()
+    return out.cpu().numpy().reshape(128, 16), int(err.item())
+
+
+def kmajor_sw128_image_16bit(vals_rk):
+    """[rows, K <= 64] bf16 values -> K-major image with the 128-byte
+    swizzle: 128-byte rows of 64 k, 8-row atoms of 1 KB (SBO), the 16-byte
+    chunk c of row r stored at chunk c ^ (r % 8)."""
+    from stile_gb300.device import _to_bf16_bits
+    rows, K = vals_rk.shape
+    bits = _to_bf16_bits(np.asarray(vals_rk, np.float32))
+    img = np.zeros(rows * 64, dtype=np.uint16)
+    for r in range(rows):
+        for k in range(K):
+            off = (r // 8) * 1024 + (r % 8) * 128 + (((k // 8) ^ (r % 8)) << 4) + (k % 8) * 2
+            img[off // 2] = bits[r, k]
+    return img
+
+
+def run_probe_bf16_kmajor_sw128(A, Bm):
+    """One kind::f16 MMA (bf16, K = 16) with both operands K-major and the
+    128-byte swizzle (SBO 1024 B; LBO unused by this layout)."""
+    import torch
+    from stile_gb300 import _lib
+    lib = _lib.load()
+    ai = probe_image(kmajor_sw128_image_16bit(A))
+    bi = probe_image(kmajor_sw128_image_16bit(Bm))
+    out = torch.zeros(128 * 16, dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    d = (ctypes.c_uint32 * 6)(16, 1024, 2, 16, 1024, 2)
     idesc = (1 << 4) | (1 << 7) | (1 << 10) | (0 << 15) | (0 << 16) | ((16 >> 3) << 17) | ((128 >> 4) << 24)
     rc = lib.stile_debug_umma_probe(ai.data_ptr(), bi.data_ptr(), d, idesc, 0, out.data_ptr(), err.data_ptr(),
                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))

@@ -57,3 +57,16 @@ def test_umma_bf16_kmajor_layout():
     ref = A.astype(np.float64) @ Bm.astype(np.float64).T
     D, err = run_probe_bf16_kmajor(A, Bm)
     assert err == 0 and float(np.abs(D - ref).max()) < 1e-3
+
+
+def test_umma_bf16_kmajor_swizzled_layout():
+    """kind::f16 (bf16) with both operands K-major and the 128-byte swizzle
+    (128-byte rows of 64 k, 8-row atoms 1024 B apart): the layout of the
+    tensor-tile value-gradient kernel's gathered rows."""
+    from gpu_util import run_probe_bf16_kmajor_sw128
+    rng = np.random.default_rng(10)
+    A = bf16_round(rng.standard_normal((128, 16)))
+    Bm = bf16_round(rng.standard_normal((16, 16)))
+    ref = A.astype(np.float64) @ Bm.astype(np.float64).T
+    D, err = run_probe_bf16_kmajor_sw128(A, Bm)
+    assert err == 0 and float(np.abs(D - ref).max()) < 1e-3

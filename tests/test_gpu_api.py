@@ -251,17 +251,22 @@ def test_batched_heads_match_one_head_at_a_time(N, mode, knots):
 @pytest.mark.parametrize("N", [128, 41, 64, 200])
 @pytest.mark.parametrize("mode", [D.TC_BF16, D.TC_SPLIT_BF16], ids=["bf16", "split"])
 @pytest.mark.parametrize("pattern", ["graph", "rect"])
-def test_fused_backward_matches_separate_passes_and_fp64(N, mode, pattern):
+@pytest.mark.parametrize("dvmode", [1, 2], ids=["tc_dvals", "run_dvals"])
+def test_fused_backward_matches_separate_passes_and_fp64(N, mode, pattern, dvmode):
     """stile_spmm_backward: dB = A^T dC and dvals from one pass over the
-    transposed plan's row tiles (plus a row-run pass for its tensor tiles)
-    equal the separate transposed product and value-gradient pass, and
-    float64; on a symmetric community graph (the transposed plan reuses the
-    forward's) and a rectangular power-law matrix (its own plan)."""
+    transposed plan's row tiles (plus a pass for its tensor tiles: on the
+    tensor cores, hi + lo bf16, or by row runs) equal the separate
+    transposed product and value-gradient pass, and float64 (dvals within
+    1e-5 either way); on a symmetric community graph (the transposed plan
+    reuses the forward's) and a rectangular power-law matrix (its own
+    plan)."""
     if pattern == "graph":
         A = _graph(seed=15)
     else:
         A = syn.power_law_rows(3000, 2200, min_len=2, max_len=300, seed=16)
     op = plan_spmm(A, N, PlanConfig(tc_mode=mode, backward="fused"))
+    op.handle.set_dvals_mode(dvmode)
+    op.transposed[0].handle.set_dvals_mode(dvmode)
     rng = np.random.default_rng(17)
     B = rng.standard_normal((A.shape[1], N)).astype(np.float32)
     dC = rng.standard_normal((A.shape[0], N)).astype(np.float32)

@@ -85,16 +85,21 @@ def test_fused_spmm_feature_widths(name, N):
     assert np.all(C[empty] == 0)
 
 
+@pytest.mark.parametrize("dvmode", [1, 2], ids=["tc_dvals", "run_dvals"])
 @pytest.mark.parametrize("path", SPMM_FIXTURES, ids=lambda p: p.split("/")[-1][:-4])
-def test_dvals_matches_fp64_sddmm(path):
+def test_dvals_matches_fp64_sddmm(path, dvmode):
+    """Value gradients over the forward tiles, the tensor-tile nonzeros on
+    the tensor cores (hi + lo bf16) or by row runs: within 1e-5 of float64."""
     meta, plan, A = _case(path, seed=4)
     N = meta["N"]
     dev = D.build_spmm_device(plan.tiles, A, N=N)
     p = DeviceSpmmPlan(dev)
+    p.set_dvals_mode(dvmode)
     rng = np.random.default_rng(7)
     dY = rng.standard_normal((A.shape[0], N)).astype(np.float32)
     B = rng.standard_normal((A.shape[1], N)).astype(np.float32)
     dv = p.dvals(torch.as_tensor(dY, device="cuda"), torch.as_tensor(B, device="cuda")).cpu().numpy()
+    assert p.error_flag() == 0
     ref = S.sddmm_fp64(A, dY, B)
     assert S.rel_fro(dv, ref) <= 1e-5
 
@@ -169,3 +174,24 @@ def test_bf16_dense_operand_needs_bf16_tensor_tiles():
     B = torch.randn((A.shape[1], 64), device="cuda").to(torch.bfloat16)
     with pytest.raises(RuntimeError, match="bf16 tensor tiles"):
         op(B)
+
+
+@pytest.mark.parametrize("N", [41, 128, 200])
+def test_tensor_tile_dvals_on_wide_and_ragged_widths(N):
+    """The tensor-core value-gradient kernel at N not a multiple of 64 (a
+    partial feature chunk, masked loads) and N > 128 (several chunks), on a
+    plan with dense tensor tiles; the row-run result is the check."""
+    path = [p for p in SPMM_FIXTURES if "community_2048.npz" in p][0]
+    meta, plan, A = _case(path, seed=21)
+    dev = D.build_spmm_device(plan.tiles, A, N=N)
+    p = DeviceSpmmPlan(dev)
+    rng = np.random.default_rng(N + 3)
+    dY = torch.as_tensor(rng.standard_normal((A.shape[0], N)).astype(np.float32), device="cuda")
+    B = torch.as_tensor(rng.standard_normal((A.shape[1], N)).astype(np.float32), device="cuda")
+    p.set_dvals_mode(1)
+    tc = p.dvals(dY, B).cpu().numpy()
+    p.set_dvals_mode(2)
+    runs = p.dvals(dY, B).cpu().numpy()
+    assert p.error_flag() == 0
+    ref = S.sddmm_fp64(A, dY.cpu().numpy(), B.cpu().numpy())
+    assert S.rel_fro(tc, ref) <= 1e-5 and S.rel_fro(runs, ref) <= 1e-5
