@@ -315,8 +315,9 @@ int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t ldd
  * accumulation: the item's 16 rows are gathered once per unit and each
  * k-step's 16 columns once, against one row per nonzero), mode 2 by the
  * row runs of the entry list (fp32 on CUDA cores), mode 0 (the default at
- * upload) mode 1 when the tensor tiles hold at least 20 nonzeros per k-step
- * on average, else mode 2.  Row-tile nonzeros always take the row runs or
+ * upload) the row runs, which measured faster on the 232,965-node GCN
+ * graph; the operator API times both once per width.  Row-tile
+ * nonzeros always take the row runs or
  * the fused ELL pass.  A bf16 B (stile_spmm_dvals_bf16) always takes the
  * row runs. */
 int stile_spmm_plan_set_dvals_mode(StileSpmmPlan* plan, int32_t mode);

@@ -168,8 +168,9 @@ class SpmmOperator:
         N = int(B.shape[1])
         choice = self._fwd_choice.get(N)
         if choice is None:
+            from .ops import new_output
             csr = self._plain_ops()[0]
-            tmp = out if out is not None else torch.empty((self.shape[0], N), dtype=torch.float32, device=B.device)
+            tmp = out if out is not None else new_output(self.shape[0], N, B.device)[0]
             times = {"hybrid": _median_ms(lambda: self.handle.run(B, tmp))}
             if B.dtype == torch.float32:
                 times["csr"] = _median_ms(lambda: csr.spmm(B, tmp))
@@ -206,29 +207,45 @@ class SpmmOperator:
             _, csrT, sd = self._plain_ops()
             dvals = sd.run(dC, B)
             return csrT.spmm(dC, dB), dvals
-        if choice == "fused":
+        # "_tc": the tensor-tile nonzeros' gradients on the tensor cores
+        mode = 1 if choice.endswith("_tc") else 2
+        if choice.startswith("fused"):
+            opT.handle.set_dvals_mode(mode)
             return opT.handle.backward(dC, B, dB)
+        self.handle.set_dvals_mode(mode)
         dvals = self.handle.dvals(dC, B)
         return opT.handle.run(dC, dB), dvals
 
     def _tune_backward(self, opT, dC, B):
         """The fastest backward variant on these operands (the median of
-        three CUDA-event timings after a warm-up call): the hybrid variants
-        the config allows, and the plain CSR kernels with path="auto"."""
-        def fused():
-            opT.handle.backward(dC, B)
+        three CUDA-event timings after a warm-up call): fused or separate as
+        the config allows, each with the tensor-tile value gradients on the
+        tensor cores ("_tc") or by row runs, and the plain CSR kernels with
+        path="auto"."""
+        def fused(mode):
+            def run():
+                opT.handle.set_dvals_mode(mode)
+                opT.handle.backward(dC, B)
+            return run
 
-        def separate():
-            self.handle.dvals(dC, B)
-            opT.handle.run(dC)
+        def separate(mode):
+            def run():
+                self.handle.set_dvals_mode(mode)
+                self.handle.dvals(dC, B)
+                opT.handle.run(dC)
+            return run
 
         def plain():
             _, csrT, sd = self._plain_ops()
             sd.run(dC, B)
             csrT.spmm(dC)
-        cands = {"fused": fused, "separate": separate}
-        if self.cfg.backward != "auto":
-            cands = {self.cfg.backward: cands[self.cfg.backward]}
+        families = ["fused", "separate"] if self.cfg.backward == "auto" else [self.cfg.backward]
+        cands = {}
+        for fam in families:
+            make = fused if fam == "fused" else separate
+            cands[fam] = make(2)
+            if (opT if fam == "fused" else self).handle.has_tensor_tiles:
+                cands[fam + "_tc"] = make(1)
         if self.cfg.path == "auto":
             cands["csr"] = plain
         times = {name: _median_ms(fn) for name, fn in cands.items()}

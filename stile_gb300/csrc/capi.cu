@@ -62,12 +62,14 @@ struct StileSpmmPlan {
   long n_tc_dv = 0;  // tensor-tile nonzeros of the value-gradient list
 };
 
-// tensor cores for the tensor tiles' value gradients where the tiles are
-// dense enough that 16 + 16 / 8 row gathers per k-step beat the row runs'
-// one per nonzero with room to spare
+// default of the tensor tiles' value gradients: the row runs (measured
+// faster on the GCN graph, 40.7 nonzeros per k-step: the tensor-core kernel
+// gathers fewer rows, but each CTA waits for its loads, then its MMAs, per
+// 64-feature chunk); stile_spmm_plan_set_dvals_mode(1) and the operator's
+// backward tuning select the tensor cores
 static int tcdv_auto(const StileSpmmPlan* plan) {
-  const stile::SpmmArgs& a = plan->args;
-  return (a.tcdv_n_units > 0 && plan->n_tc_dv >= 20L * a.tc_n_ksteps) ? 1 : 0;
+  (void)plan;  // one rule for every plan
+  return 0;
 }
 
 struct StileSddmmPlan {
@@ -547,7 +549,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   a.tcdv_unit_meta = (const int*)P(i_umeta);
   a.tcdv_id = a.tc_nnz_id;  // the plan's own numbering until set_transpose_ids
   plan->n_tc_dv = n_tc_dv;
-  a.tcdv_use = tcdv_auto(plan);
+  a.tcdv_use = tcdv_auto(plan);  // the row runs until the caller selects the tensor cores
   *out = plan;
   return STILE_OK;
 }

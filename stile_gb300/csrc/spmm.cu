@@ -1344,8 +1344,9 @@ cudaError_t launch_ell_bwd(const SpmmArgs& p, cudaStream_t st) {
 // is the gradient of the nonzero (r, k) of k-step j.  The item's 16 X rows
 // are gathered once per unit, the columns once per k-step (the row-run
 // kernel gathers one row per nonzero: ~41 per k-step on the GCN graph).
-// Per 64-feature chunk every 16-lane half-warp gathers one row (a float4 a
-// lane, 256 contiguous bytes), splits it into hi = bf16(x) and
+// Per 64-feature chunk each of the 16 half-warps (256 threads) issues the
+// loads of its 8 columns and 1 item row at once (a float4 a lane, 256
+// contiguous bytes a row), then splits every row into hi = bf16(x) and
 // lo = bf16(x - hi), and stores both into K-major images with the 128-byte
 // swizzle (128-byte rows of 64 features, the 16-byte chunk q of row m at
 // q ^ (m % 8), 8-row atoms 1 KB apart), so each half-warp writes one
@@ -1363,7 +1364,9 @@ __device__ __forceinline__ uint32_t sw128_off(int row, int q) {
   return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((q ^ (row & 7)) << 4));
 }
 
-__global__ void __launch_bounds__(128) spmm_tc_dvals_kernel(SpmmArgs p, const float* __restrict__ X, long ldx,
+constexpr int kDvThreads = 256;
+
+__global__ void __launch_bounds__(kDvThreads, 3) spmm_tc_dvals_kernel(SpmmArgs p, const float* __restrict__ X, long ldx,
                                                               const float* __restrict__ Y, long ldy,
                                                               float* __restrict__ out, int F) {
   extern __shared__ uint8_t smem_raw[];
@@ -1402,42 +1405,29 @@ __global__ void __launch_bounds__(128) spmm_tc_dvals_kernel(SpmmArgs p, const fl
     const int ks0 = __ldg(p.tcdv_unit_ks + u);
     const int meta = __ldg(p.tcdv_unit_meta + u);
     const int item = meta >> 3, nks = (meta & 7) + 1;
-    // this half-warp's rows: 8 i + 2 warp + hw (16 of the 128 columns, 2 of
-    // the 16 item rows)
-    int ycol[16];
+    // this half-warp (hg = 0..15) gathers columns m = 16 i + hg (i < 8) and
+    // item row hg
+    const int hg = 2 * warp + hw;
+    int ycol[8];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const int m = 8 * i + 2 * warp + hw, j = m >> 4;
+    for (int i = 0; i < 8; ++i) {
+      const int m = 16 * i + hg, j = m >> 4;
       ycol[i] = j < nks ? __ldg(p.tc_cols + (long)(ks0 + j) * 16 + (m & 15)) : -1;
     }
-    int xrow[2];
-#pragma unroll
-    for (int i = 0; i < 2; ++i) xrow[i] = __ldg(p.tc_out_rows + (long)item * 16 + 8 * i + 2 * warp + hw);
-    if (sl == 0) {
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-        asm volatile("st.shared.b32 [%0], %1;" ::"r"(orow_s + 4 * (8 * i + 2 * warp + hw)), "r"(xrow[i]) : "memory");
-    }
+    const int xrow = __ldg(p.tc_out_rows + (long)item * 16 + hg);
+    if (sl == 0) asm volatile("st.shared.b32 [%0], %1;" ::"r"(orow_s + 4 * hg), "r"(xrow) : "memory");
 #pragma unroll 1
     for (int fc = 0; fc < F; fc += 64) {
       const int f = fc + 4 * sl;
-      // gather: 8 Y rows at a time in flight, then the 2 X rows
+      // every load of the chunk in flight at once, then the conversions
+      float4 v[8];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        float4 v[8];
+      for (int i = 0; i < 8; ++i)
+        v[i] = ycol[i] >= 0 ? ld4_live(Y + (long)ycol[i] * ldy, f, F) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 xv = xrow >= 0 ? ld4_live(X + (long)xrow * ldx, f, F) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int c = ycol[8 * h + i];
-          v[i] = c >= 0 ? ld4_live(Y + (long)c * ldy, f, F) : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-#pragma unroll
-        for (int i = 0; i < 8; ++i) put(yhi, ylo, 8 * (8 * h + i) + 2 * warp + hw, v[i]);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const float4 v = xrow[i] >= 0 ? ld4_live(X + (long)xrow[i] * ldx, f, F) : make_float4(0.f, 0.f, 0.f, 0.f);
-        put(xhi, xlo, 8 * i + 2 * warp + hw, v);
-      }
+      for (int i = 0; i < 8; ++i) put(yhi, ylo, 16 * i + hg, v[i]);
+      put(xhi, xlo, hg, xv);
       fence_proxy_async_smem();
       tc_fence_before();
       __syncthreads();
@@ -1464,13 +1454,15 @@ __global__ void __launch_bounds__(128) spmm_tc_dvals_kernel(SpmmArgs p, const fl
       tc_fence_after();
     }
     if (!ok) break;
-    // epilogue: warp w holds TMEM lanes m = 32 w .. 32 w + 31 (k-steps 2 w
-    // and 2 w + 1), columns r = 0..15
-    uint32_t v[16];
-    tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16), v);
-    tmem_wait_ld();
+    // epilogue (warps 0-3): warp w holds TMEM lanes m = 32 w .. 32 w + 31
+    // (k-steps 2 w and 2 w + 1), columns r = 0..15
     const int m = 32 * warp + lane, j = m >> 4, k = m & 15;
-    if (j < nks) {
+    uint32_t v[16];
+    if (warp < 4) {
+      tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16), v);
+      tmem_wait_ld();
+    }
+    if (warp < 4 && j < nks) {
       const int* ids = p.tcdv_id + (long)(ks0 + j) * 256 + k;
 #pragma unroll
       for (int r = 0; r < 16; ++r) {
@@ -1499,10 +1491,11 @@ cudaError_t launch_tc_dvals(const SpmmArgs& p, const float* X, long ldx, const f
   cudaError_t e = cudaFuncSetAttribute(spmm_tc_dvals_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kDvBytes);
   if (e != cudaSuccess) return e;
-  // 37 KB of shared memory and 32 TMEM columns per CTA: 4 CTAs per SM
-  const int grid = std::min(p.tcdv_n_units, device_sm_count() * 4);
-  return launch_dependent(spmm_tc_dvals_kernel, dim3((unsigned)grid), dim3(128), kDvBytes, st, p, X, ldx, Y, ldy,
-                          out, F);
+  // 37 KB of shared memory, 256 threads at 80 registers and 32 TMEM columns
+  // per CTA: 3 CTAs per SM
+  const int grid = std::min(p.tcdv_n_units, device_sm_count() * 3);
+  return launch_dependent(spmm_tc_dvals_kernel, dim3((unsigned)grid), dim3(kDvThreads), kDvBytes, st, p, X, ldx, Y,
+                          ldy, out, F);
 }
 
 cudaError_t launch_dvals(const SpmmArgs& p, const float* dY, long lddy, float* dvals, cudaStream_t st) {

@@ -175,6 +175,9 @@ class DeviceSpmmPlan:
                    "stile_spmm_plan_upload")
         self.handle = handle
         self._dvals_cover_all = _tiles_cover_every_nonzero(dev)
+        # tensor tiles with nonzero ids: their value gradients can run on the
+        # tensor cores (stile_spmm_plan_set_dvals_mode)
+        self.has_tensor_tiles = len(dev.tc_cols) > 0 and len(dev.tc_nnz_id) > 0
 
     def run(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """C = A @ B in fp32; B is fp32 or bf16 (a bf16 B is read as is:

@@ -277,7 +277,9 @@ def test_fused_backward_matches_separate_passes_and_fp64(N, mode, pattern, dvmod
     dB_sep = opT(dCt)
     torch.cuda.synchronize()
     assert op.handle.error_flag() == 0 and opT.handle.error_flag() == 0
-    assert torch.allclose(dv, dv_sep, rtol=1e-5, atol=1e-5)
+    if dvmode == 2:
+        # the same fp32 arithmetic per nonzero: equal up to summation order
+        assert torch.allclose(dv, dv_sep, rtol=1e-5, atol=1e-5)
     assert torch.allclose(dB, dB_sep, rtol=1e-5, atol=1e-5)
     tol = 1e-2 if mode == D.TC_BF16 else 1e-5
     assert S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC, B)) <= 1e-5
@@ -296,7 +298,7 @@ def test_backward_auto_choice_is_timed_once_per_width_and_correct():
     Bt, dCt = torch.as_tensor(B, device="cuda"), torch.as_tensor(dC, device="cuda")
     for _ in range(2):
         dB, dv = op.backward(dCt, Bt)
-        assert op._bwd_choice[64] in ("fused", "separate")
+        assert op._bwd_choice[64] in ("fused", "separate", "fused_tc", "separate_tc")
         assert S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC, B)) <= 1e-5
         assert S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(op.A.T.tocsr(), dC)) <= 1e-5
     assert list(op._bwd_choice) == [64]
@@ -347,7 +349,7 @@ def test_auto_path_times_the_candidates_once_and_stays_correct(N):
         assert S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(A.T.tocsr(), dC)) <= 1e-2
         assert S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC, B)) <= 1e-5
     assert op._fwd_choice[N] in ("hybrid", "csr")
-    assert op._bwd_choice[N] in ("fused", "separate", "csr")
+    assert op._bwd_choice[N] in ("fused", "separate", "fused_tc", "separate_tc", "csr")
     assert len(op._fwd_choice) == 1 and len(op._bwd_choice) == 1
 
 
