@@ -65,8 +65,13 @@ class PlanConfig:
     # kernels over A's CSR arrays: CSR-row SpMM for A and A^T, the entry-list
     # SDDMM for value gradients and for SddmmOperator) or "auto" (the first
     # call of each width times the candidates on its own operands and keeps
-    # the fastest; the plan is still searched and held)
+    # the fastest; the plan is still searched and held).  With bf16 tensor
+    # tiles "auto" also times the forward as a dense bf16 GEMM of the
+    # zero-filled matrix (cuBLAS, fp32 accumulation, bf16 operands; A at most
+    # dense_limit elements): the choice for a weight whose 16x16 blocks
+    # nearly all hold a nonzero
     path: str = "hybrid"
+    dense_limit: int = 1 << 26
 
     def __post_init__(self):
         if self.path not in ("hybrid", "csr", "auto"):
@@ -146,6 +151,9 @@ class SpmmOperator:
         # plain CSR kernels over A (built on first use): CSR SpMM of A and
         # of A^T, the entry-list SDDMM over A's nonzeros
         self._plain = None
+        # (bf16 zero-filled A, nonzero rows, nonzero columns) of the dense
+        # forward (built on first use)
+        self._dense = None
 
     def _plain_ops(self):
         if self._plain is None:
@@ -174,13 +182,36 @@ class SpmmOperator:
             times = {"hybrid": _median_ms(lambda: self.handle.run(B, tmp))}
             if B.dtype == torch.float32:
                 times["csr"] = _median_ms(lambda: csr.spmm(B, tmp))
+            if self.cfg.tc_mode == D.TC_BF16 and self.shape[0] * self.shape[1] <= self.cfg.dense_limit:
+                times["dense"] = _median_ms(lambda: self._dense_forward(B, tmp))
             choice = min(times, key=times.get)
             self._fwd_choice[N] = choice
         return choice
 
+    def _dense_forward(self, B, out=None):
+        """C = A B as a dense bf16 GEMM of the zero-filled A (cuBLAS through
+        torch.matmul, fp32 accumulation), C in fp32."""
+        if self._dense is None:
+            vals = self._vals if self._vals is not None else torch.as_tensor(self.A.data.astype(np.float32),
+                                                                             device="cuda")
+            W = torch.zeros(self.shape, dtype=torch.float32, device="cuda")
+            rows = torch.as_tensor(np.repeat(np.arange(self.shape[0]), np.diff(self.A.indptr)), device="cuda")
+            cols = torch.as_tensor(self.A.indices.astype(np.int64), device="cuda")
+            W[rows, cols] = vals
+            self._dense = (W.to(torch.bfloat16), rows, cols)
+        Wd = self._dense[0]
+        C = torch.matmul(Wd, B.to(torch.bfloat16))
+        if out is None:
+            return C.float()
+        out.copy_(C)
+        return out
+
     def __call__(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
-        if self.forward_path(B, out) == "csr":
+        path = self.forward_path(B, out)
+        if path == "csr":
             return self._plain_ops()[0].spmm(B.float(), out)
+        if path == "dense":
+            return self._dense_forward(B, out)
         return self.handle.run(B, out)
 
     def dvals(self, dC: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
@@ -267,6 +298,9 @@ class SpmmOperator:
         if self._plain is not None:
             self._plain[0].set_values(vals)
             self._plain[1].set_values(vals[self.transposed[1]])
+        if self._dense is not None:
+            W, rows, cols = self._dense
+            W[rows, cols] = vals.to(torch.bfloat16)
         self.handle.set_values(vals)
         self._vals = vals.clone()
         if self._transposed is not None:

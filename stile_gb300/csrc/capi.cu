@@ -102,7 +102,7 @@ int stile_spmm_plan_upload(const StileSpmmPlanHost* h, StileSpmmPlan** out) {
   const int mode = h->tc_mode;
   if (h->tc_n_items > 0) {
     if (mode != STILE_TC_BF16 && mode != STILE_TC_F16 && mode != STILE_TC_SPLIT_BF16 && mode != STILE_TC_FP8)
-      return fail(STILE_E_UNSUPPORTED, "tensor-tile mode not supported by this build");
+      return fail(STILE_E_UNSUPPORTED, "unknown tensor-tile mode");
     if (mode == STILE_TC_FP8) {
       if (!h->tc_row_scale) return fail(STILE_E_INVALID, "fp8 tensor tiles need tc_row_scale");
       for (long i = 0; i < (long)h->tc_n_items * 16; ++i)

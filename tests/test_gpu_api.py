@@ -367,3 +367,25 @@ def test_sddmm_auto_path(bf16):
     assert op._choice and list(op._choice.values())[0] in ("hybrid", "csr")
     ref = S.sddmm_fp64(sp.csr_matrix(mask), X.float().cpu().numpy(), Y.float().cpu().numpy())
     assert S.rel_fro(out, ref) <= 1e-5
+
+
+def test_auto_path_on_the_pruned_weight_considers_the_dense_gemm():
+    """The pruned weight (3072 x 768 at 90% sparsity, N = 4096, bf16 tiles):
+    path="auto" times the hybrid plan, the CSR kernel and a dense bf16 GEMM
+    of the zero-filled weight, keeps the fastest, and its forward stays
+    within the tensor-tile bound; new values reach whichever path runs."""
+    from stile_gb300 import workloads as W
+    w = W.pruned(False)
+    op = plan_spmm(w.A, w.width, PlanConfig(path="auto"))
+    B = torch.as_tensor(w.dense["B"], device="cuda")
+    C = op(B).cpu().numpy()
+    assert op._fwd_choice[w.width] in ("hybrid", "csr", "dense")
+    assert S.rel_fro(C, S.spmm_fp64(op.A, w.dense["B"])) <= 1e-2
+    # the dense candidate on its own, and after new values
+    Cd = op._dense_forward(B).cpu().numpy()
+    assert S.rel_fro(Cd, S.spmm_fp64(op.A, w.dense["B"])) <= 1e-2
+    new = np.random.default_rng(23).standard_normal(op.nnz) * 0.02
+    op.set_values(torch.as_tensor(new.astype(np.float32), device="cuda"))
+    A2 = sp.csr_matrix((new, op.A.indices, op.A.indptr), shape=op.A.shape)
+    assert S.rel_fro(op(B).cpu().numpy(), S.spmm_fp64(A2, w.dense["B"])) <= 1e-2
+    assert S.rel_fro(op._dense_forward(B).cpu().numpy(), S.spmm_fp64(A2, w.dense["B"])) <= 1e-2
