@@ -83,7 +83,7 @@ SPMM_CASES = [
     # (case id, device-layout corruption, host-struct corruption, code, message fragment)
     ("negative_shape", None, lambda h: setattr(h, "M", -1), INVALID, "negative shape"),
     ("negative_count", None, lambda h: setattr(h, "ell_n_slots", -3), INVALID, "negative count"),
-    ("unknown_tc_mode", None, lambda h: setattr(h, "tc_mode", 99), UNSUPPORTED, "mode not supported"),
+    ("unknown_tc_mode", None, lambda h: setattr(h, "tc_mode", 99), UNSUPPORTED, "unknown tensor-tile mode"),
     ("fp8_without_row_scales", None, lambda h: setattr(h, "tc_mode", 3), INVALID, "need tc_row_scale"),
     ("fp8_bad_row_scale", lambda d: dataclasses.replace(d, tc_mode=3, tc_row_scale=np.full(
         len(d.tc_item_flags) * 16, -1.0, np.float32)), None, INVALID, "positive and finite"),
