@@ -362,14 +362,18 @@ template <int L, bool kYb, bool kXb = false>
 static cudaError_t launch_runs_t(int grid, bool one, bool full, cudaStream_t st, int n_groups, const int* gptr,
                                  const int* grow, const int* cols, const int* outs, const void* X, long ldx,
                                  const void* Y, long ldy, float* out, int F) {
+  // narrow rows (8 lanes or fewer: 64 features or fewer) keep 4 Y rows in
+  // flight per group at 5 blocks per SM: a narrow row is few bytes, and the
+  // gathers are bound by the bytes in flight
+  constexpr int U = L <= 8 ? 4 : kRunU, MINB = L <= 8 ? 5 : kRunBlocks;
   if (full)
-    return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, true, true, kXb>, dim3((unsigned)grid),
-                            dim3(256), 0, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+    return launch_dependent(sddmm_run_kernel<L, 2, U, MINB, kYb, true, true, kXb>, dim3((unsigned)grid), dim3(256), 0,
+                            st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
   if (one)
-    return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, true, false, kXb>, dim3((unsigned)grid),
-                            dim3(256), 0, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
-  return launch_dependent(sddmm_run_kernel<L, 2, kRunU, kRunBlocks, kYb, false, false, kXb>, dim3((unsigned)grid),
-                          dim3(256), 0, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+    return launch_dependent(sddmm_run_kernel<L, 2, U, MINB, kYb, true, false, kXb>, dim3((unsigned)grid), dim3(256),
+                            0, st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
+  return launch_dependent(sddmm_run_kernel<L, 2, U, MINB, kYb, false, false, kXb>, dim3((unsigned)grid), dim3(256), 0,
+                          st, n_groups, gptr, grow, cols, outs, X, ldx, Y, ldy, out, F);
 }
 
 cudaError_t launch_sddmm_runs(int n_groups, const int* gptr, const int* grow, const int* cols, const int* outs,
