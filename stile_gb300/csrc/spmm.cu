@@ -443,8 +443,9 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
                        make_uint4(wd[j][0], wd[j][1], wd[j][2], wd[j][3]));
         }
       }
+      if (!dead) {  // (a guard around the loop keeps it unrolled)
 #pragma unroll
-      for (int r = 0; r < (MODE == STILE_TC_FP8 ? 0 : 16) && !dead; ++r) {
+      for (int r = 0; r < (MODE == STILE_TC_FP8 ? 0 : 16); ++r) {
         const uint4 raw = ld_shared_v4(stage + r * 512 + lane * 16);
         const float4 v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y), __uint_as_float(raw.z),
                                      __uint_as_float(raw.w));
@@ -461,6 +462,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
             st_shared_v2(sa + kAStage + o, pack_bf16x2(v.x - hf.x, v.y - hf.y), pack_bf16x2(v.z - hf.z, v.w - hf.w));
           }
         }
+      }
       }
 #pragma unroll
       for (int c = lane; c < (int)(W::kVals / 16); c += 32)
@@ -1265,13 +1267,10 @@ struct EllNarrowLaunch {
     if (grid.y > 1)
       return full ? launch_dependent(spmm_ell_seg_kernel<LPR, 2, true, false, true>, grid, dim3(256), 0, st, p)
                   : launch_dependent(spmm_ell_seg_kernel<LPR, 2, false, false, true>, grid, dim3(256), 0, st, p);
-    // one head, one feature pass: 4 entries per batch (8 float4 in flight
-    // per lane: a narrow row is few bytes, and these gathers are bound by
-    // the bytes in flight)
-    constexpr int kB = LPR >= 4 ? 4 : 2;
-    return full ? launch_dependent(spmm_ell_seg_kernel<LPR, 2, true, false, false, false, kB>, grid, dim3(256), 0, st, p)
-                : launch_dependent(spmm_ell_seg_kernel<LPR, 2, false, false, false, false, kB>, grid, dim3(256), 0, st,
-                                   p);
+    // (4 entries per batch at 4 blocks per SM measured slower at N = 41:
+    // 159 against 154 us on the GCN graph)
+    return full ? launch_dependent(spmm_ell_seg_kernel<LPR, 2, true, false>, grid, dim3(256), 0, st, p)
+                : launch_dependent(spmm_ell_seg_kernel<LPR, 2, false, false>, grid, dim3(256), 0, st, p);
   }
 };
 
