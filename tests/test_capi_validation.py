@@ -158,6 +158,10 @@ def test_run_entry_points_validate_before_launching():
     assert lib.stile_sddmm_run(None, fake, 64, fake, 64, fake, 64, None) == INVALID
     assert lib.stile_spmm_dvals(None, fake, 64, fake, 64, fake, 64, None) == INVALID
     assert lib.stile_spmm_plan_set_wait_policy(None, 10, 1) == INVALID
+    assert lib.stile_spmm_plan_set_dvals_mode(None, 1) == INVALID
+    assert "null plan" in _lib.last_error()
+    assert lib.stile_spmm_backward(None, fake, 64, fake, 64, fake, 64, fake, 64, None) == INVALID
+    assert lib.stile_spmm_plan_set_transpose_ids(None, fake, 10, None) == INVALID
     # plain CSR kernel: shape, null arrays, strides, alignment, nnz
     csr = lib.stile_csr_spmm_run
     assert csr(4, 8, fake, fake, fake, None, fake, 64, fake, 64, 0, None) == INVALID
