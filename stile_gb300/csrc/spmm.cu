@@ -252,17 +252,9 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
     mbar_init(drain, 1);
     fence_mbar_init();
   }
-  // a single partial slice (N < 128) skips the features wholly past N:
-  // their copies (bf16 B: their 16-byte chunks of the A image; fp32 B: the
-  // producer lanes past N copy and convert nothing), so those parts of the
-  // A images keep the zeros written here (with several slices a slot also
-  // holds full slices, so everything is copied, the part past N
-  // zero-filled)
-  const bool keep_zero = !kFull && p.n_fchunks == 1;
-  if (MODE == STILE_TC_FP8 || keep_zero) {
-    // fp8: the A images' upper k halves stay zero (each k-step fills the
-    // lower half of a K = 32 operand); made visible to the tensor core's
-    // proxy
+  if constexpr (MODE == STILE_TC_FP8) {
+    // the A images' upper k halves stay zero (each k-step fills the lower
+    // half of a K = 32 operand); made visible to the tensor core's proxy
     for (int i = tid; i < (int)(kWsSlots * W::kAImg / 16); i += kWsThreads)
       st_shared_v4(slots + W::a_off(0) + 16 * i, make_uint4(0u, 0u, 0u, 0u));
     fence_proxy_async_smem();
@@ -329,8 +321,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
           const int r = 2 * j + rh;
           const int col = __shfl_sync(0xffffffffu, cols, r);
           const uint16_t* row = B16 + (long)col * p.ldb;
-          if (bytes || !keep_zero)
-            cp_async16(sa + a_img_off(8 * ch, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
+          cp_async16(sa + a_img_off(8 * ch, r), bytes ? (const void*)(row + f) : (const void*)row, bytes);
         }
         cp_async16(slots + W::v_off(slot) + lane * 16, vals + (long)(s_beg + l) * kBStage + lane * 16, 16u);
         cp_async_commit();
@@ -382,9 +373,6 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
       const float amax = __uint_as_float(*p.tc_xamax);
       xinv = amax > 0.f ? kE4m3Max / amax : 0.f;
     }
-    // this lane's features all past N in every step (single partial
-    // slice): it copies and converts nothing
-    const bool dead = keep_zero && 4 * lane >= N;
     auto issue = [&](int cols, int l, int ff) {
       const int f = ff + 4 * lane;
       const uint32_t bytes = kFull ? 16u : ((f + 4 <= N) ? 16u : (f < N ? (uint32_t)(N - f) * 4u : 0u));
@@ -392,7 +380,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
       for (int r = 0; r < 16; ++r) {
         const int col = __shfl_sync(0xffffffffu, cols, r);
         const float* row = p.B + blockIdx.z * p.b_head_stride + (long)col * p.ldb;
-        if (!dead) cp_async16(stage + r * 512 + lane * 16, bytes ? (const void*)(row + f) : (const void*)row, bytes);
+        cp_async16(stage + r * 512 + lane * 16, bytes ? (const void*)(row + f) : (const void*)row, bytes);
       }
 #pragma unroll
       for (int c = lane; c < (int)(W::kVals / 16); c += 32)
@@ -420,7 +408,7 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
         if (lane != 0) mbar_wait_bounded(empty0 + 8 * slot, par, polls);  // completed: returns at once
       }
       const uint32_t sa = slots + W::a_off(slot);
-      if (MODE == STILE_TC_FP8 && !dead) {
+      if constexpr (MODE == STILE_TC_FP8) {
         // this lane's 4 features x the step's 16 rows -> four K-major
         // 16-byte rows of the A image (feature m: the e4m3 bytes of x / s_x
         // for k = 0..15), core matrices of 8 features x 16 bytes
@@ -443,7 +431,6 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
                        make_uint4(wd[j][0], wd[j][1], wd[j][2], wd[j][3]));
         }
       }
-      if (!dead) {  // (a guard around the loop keeps it unrolled)
 #pragma unroll
       for (int r = 0; r < (MODE == STILE_TC_FP8 ? 0 : 16); ++r) {
         const uint4 raw = ld_shared_v4(stage + r * 512 + lane * 16);
@@ -462,7 +449,6 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
             st_shared_v2(sa + kAStage + o, pack_bf16x2(v.x - hf.x, v.y - hf.y), pack_bf16x2(v.z - hf.z, v.w - hf.w));
           }
         }
-      }
       }
 #pragma unroll
       for (int c = lane; c < (int)(W::kVals / 16); c += 32)
@@ -616,12 +602,9 @@ __global__ void __launch_bounds__(kWsThreads, WsCfg<MODE, kIn16>::kCtas) spmm_tc
 // kSpanY: blockIdx.y takes features [y span, (y + 1) span) (a wide B over
 // few groups; span = p.ell_fc_span, a multiple of the pass width).
 // kHeads: a batched run (blockIdx.z = head offsets B, C and the records).
-// BATCH: entries per batch (0: 4 / VEC, i.e. 4 float4 in flight per lane;
-// more take 4 blocks per SM instead of 5).
-template <int LPR, int VEC, bool kFull, bool kOff32, bool kSpanY = false, bool kHeads = false, int BATCH = 0>
-__global__ void __launch_bounds__(256, (BATCH && BATCH * VEC > 4) ? 4 : 5) spmm_ell_seg_kernel(SpmmArgs p) {
-  constexpr int kBatch = BATCH ? BATCH : 4 / VEC;  // entries per batch
-  static_assert(LPR % kBatch == 0, "batches stay inside one record block");
+template <int LPR, int VEC, bool kFull, bool kOff32, bool kSpanY = false, bool kHeads = false>
+__global__ void __launch_bounds__(256, 5) spmm_ell_seg_kernel(SpmmArgs p) {
+  constexpr int kBatch = 4 / VEC;  // entries per batch: 4 float4 in flight per lane
   // Launched dependent on the previous kernel.  When that is the zero-rows
   // kernel (p.ell_lazy_wait), only the atomic adds (into rows it zeroes)
   // wait for it, and every thread waits before it exits, so that this
@@ -1267,7 +1250,7 @@ struct EllNarrowLaunch {
     if (grid.y > 1)
       return full ? launch_dependent(spmm_ell_seg_kernel<LPR, 2, true, false, true>, grid, dim3(256), 0, st, p)
                   : launch_dependent(spmm_ell_seg_kernel<LPR, 2, false, false, true>, grid, dim3(256), 0, st, p);
-    // (4 entries per batch at 4 blocks per SM measured slower at N = 41:
+    // (4 entries per batch at 4 blocks per SM measured slower at N = 41,
     // 159 against 154 us on the GCN graph)
     return full ? launch_dependent(spmm_ell_seg_kernel<LPR, 2, true, false>, grid, dim3(256), 0, st, p)
                 : launch_dependent(spmm_ell_seg_kernel<LPR, 2, false, false>, grid, dim3(256), 0, st, p);
