@@ -735,16 +735,19 @@ def run_gpu(args):
     v = vals.detach().requires_grad_(True)
 
     def e2e_step():
+        # up: every layer's operand in forward order, then the output
+        # gradients in the order the backward needs them (last layer first),
+        # so each layer's backward starts as soon as its own dC has landed
         ev_b = [torch.cuda.Event() for _ in range(L)]
-        ev_dc = torch.cuda.Event()
+        ev_dc = [torch.cuda.Event() for _ in range(L)]
         up.wait_stream(main)
         with torch.cuda.stream(up):
             for i in range(L):
                 xfer(Bd[i], hB[i])
                 ev_b[i].record(up)
-            for i in range(L):
+            for i in reversed(range(L)):
                 xfer(dCd[i], hdC[i])
-            ev_dc.record(up)
+                ev_dc[i].record(up)
         Bin, Cs = [], []
         for i in range(L):
             main.wait_event(ev_b[i])
@@ -757,17 +760,26 @@ def run_gpu(args):
             with torch.cuda.stream(down):
                 xfer(hC[i], Cs[i].detach())
             Cs[i].record_stream(down)
-        main.wait_event(ev_dc)
-        grads = torch.autograd.grad(Cs, [v] + Bin, grad_outputs=dCd)
-        ev_bw = torch.cuda.Event()
-        ev_bw.record(main)
-        down.wait_event(ev_bw)
+        # backward layer by layer (last first): each dB_l goes down while the
+        # next layer's backward runs; the value gradient (shared by the
+        # layers) is summed on the device and goes down last
+        dv = None
+        for i in reversed(range(L)):
+            main.wait_event(ev_dc[i])
+            g_v, g_b = torch.autograd.grad(Cs[i], [v, Bin[i]], grad_outputs=dCd[i])
+            dv = g_v if dv is None else dv.add_(g_v)
+            ev_bw = torch.cuda.Event()
+            ev_bw.record(main)
+            down.wait_event(ev_bw)
+            with torch.cuda.stream(down):
+                xfer(hdB[i], g_b)
+            g_b.record_stream(down)
+        ev_dv = torch.cuda.Event()
+        ev_dv.record(main)
+        down.wait_event(ev_dv)
         with torch.cuda.stream(down):
-            hdv.copy_(grads[0], non_blocking=True)
-            for i in range(L):
-                xfer(hdB[i], grads[1 + i])
-        for g_ in grads:
-            g_.record_stream(down)
+            hdv.copy_(dv, non_blocking=True)
+        dv.record_stream(down)
         main.wait_stream(down)
 
     for _ in range(2):
@@ -801,9 +813,10 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic", "config": cfg,
             "e2e": {"value": e2e_val, "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
-                    "path": "HybridSpMMFunction forward of both layers + torch.autograd.grad, pinned host "
-                            "buffers; copies on two side streams (up: B_l, dC_l; down: C_l during the rest, "
-                            "then the value gradient and dB_l)"},
+                    "path": "HybridSpMMFunction forward of both layers, torch.autograd.grad per layer (last "
+                            "first), pinned host buffers; copies on two side streams (up: B_l, then dC_l last "
+                            "layer first; down: C_l during the rest, dB_l after its layer's backward, the "
+                            "summed value gradient last)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "layer-1 forward SpMM (N = 128)",
