@@ -222,8 +222,12 @@ class SpmmOperator:
     def backward(self, dC: torch.Tensor, B: torch.Tensor, dB: torch.Tensor | None = None):
         """(dB = A^T @ dC, dvals = <dC[row], B[col]> on A's pattern), fp32 dC
         and B: fused (one pass over the transposed plan's row tiles) or
-        separate (transposed product, then the value-gradient pass), as
-        ``cfg.backward`` says; "auto" times both once per width."""
+        separate (transposed product, then the value-gradient pass), each
+        with the tensor-tile nonzeros' gradients on the tensor cores or by
+        row runs, or the plain CSR kernels (path="csr").  With
+        ``cfg.backward="auto"`` or ``cfg.path="auto"`` the first backward of
+        each width times the allowed variants on its operands and keeps the
+        fastest."""
         opT, _ = self.transposed
         if self.cfg.path == "csr":
             choice = "csr"
