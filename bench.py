@@ -324,7 +324,9 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GFLOP/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": base_config(A, layers, WORKLOAD),
+           "config": {**base_config(A, layers, WORKLOAD),
+                      "l2": "not applicable (host CPU path; each step reads its operands from host memory)",
+                      "parallelism": f"{threads} host threads"},
            "cpu_baseline": {"value": val, "unit": "GFLOP/s", "cores": threads, "kind": "port",
                             "sample": "the whole fwd+bwd step of both layers per iteration (C restatement of "
                                       "the reference's CPU path: CSR SpMM x2 + gather-dot SDDMM per layer)"},
@@ -802,15 +804,15 @@ def run_gpu(args):
 
     if rank == 0:
         cfg = base_config(A, layers, WORKLOAD)
-        cfg.update({"tc_tiles": "bf16 operands, fp32 accumulate (tcgen05, TMEM)", "row_tiles": "fp32 (CUDA cores)",
-                    "plans": st.plan_summary(), "plan_search_s": round(st.plan_s, 2),
-                    "cost_model": st.ops[0].plan.meta.get("cost_model"),
-                    "l2": "flushed between steps (256 MiB write, untimed)",
+        cfg.update({"l2": "flushed between steps (256 MiB write, untimed)",
                     "parallelism": "replicas" if world > 1 else "single GPU"})
+        plan_info = {"tc_tiles": "bf16 operands, fp32 accumulate (tcgen05, TMEM)", "row_tiles": "fp32 (CUDA cores)",
+                     "plans": st.plan_summary(), "plan_search_s": round(st.plan_s, 2),
+                     "cost_model": st.ops[0].plan.meta.get("cost_model")}
         out = {
             "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic", "config": cfg,
+            "vs_baseline": None, "dtype": "f32+bf16", "data": "synthetic", "config": cfg, "plan": plan_info,
             "e2e": {"value": e2e_val, "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
                     "path": "HybridSpMMFunction forward of both layers, torch.autograd.grad per layer (last "
