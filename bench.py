@@ -953,8 +953,8 @@ def run_config(args):
         B_np, dC_np = w.dense["B"], w.dense["dC"]
         B = torch.as_tensor(B_np, device=dev)
         dC = torch.as_tensor(dC_np, device=dev)
-        C = torch.empty((A.shape[0], N), device=dev)
-        dB = torch.empty((A.shape[1], N), device=dev)
+        C = aligned_empty(A.shape[0], N, dev)
+        dB = aligned_empty(A.shape[1], N, dev)
         AT = opT.A
 
         def step():
@@ -998,7 +998,7 @@ def run_config(args):
         # the operator left to choose its path (hybrid plan or plain CSR
         # kernels, timed on these operands at the first call of each width)
         op_a = SpmmOperator(A, N, PlanConfig(tc_mode=tc_mode, path="auto"), plan=op.plan)
-        Ca, dBa = torch.empty_like(C), torch.empty_like(dB)
+        Ca, dBa = aligned_empty(C.shape[0], C.shape[1], dev), aligned_empty(dB.shape[0], dB.shape[1], dev)
 
         def auto_step():
             op_a(B, out=Ca)
@@ -1013,7 +1013,7 @@ def run_config(args):
         if args.workload.startswith("pruned"):
             # activations in bf16, as the configuration has them: read as is
             B16 = B.to(torch.bfloat16)
-            C16 = torch.empty_like(C)
+            C16 = aligned_empty(C.shape[0], C.shape[1], dev)
             op(B16, out=C16)
             torch.cuda.synchronize()
             out["bf16_B"] = {"forward_ms": timed(lambda: op(B16, out=C16), args.steps),
@@ -1025,7 +1025,7 @@ def run_config(args):
             t0 = time.time()
             op_b = SpmmOperator(A, N, PlanConfig(tc_mode=tc_mode, tc_k_notsorted=True))
             t_b = time.time() - t0
-            Cb = torch.empty_like(C)
+            Cb = aligned_empty(C.shape[0], C.shape[1], dev)
             op_b(B, out=Cb)
             torch.cuda.synchronize()
             out["column_blocks"] = {"plan": plan_summary(op_b.plan), "plan_search_s": round(t_b, 2),
@@ -1037,7 +1037,7 @@ def run_config(args):
             # fp8 e4m3 tensor tiles (per tile-row weight scales, per-tensor
             # activation scale), the same plan, fp32 activations
             op_f8 = SpmmOperator(A, N, PlanConfig(tc_mode=D.TC_FP8), plan=op.plan)
-            C8 = torch.empty_like(C)
+            C8 = aligned_empty(C.shape[0], C.shape[1], dev)
             op_f8(B, out=C8)
             torch.cuda.synchronize()
             out["fp8_tiles"] = {"forward_ms": timed(lambda: op_f8(B, out=C8), args.steps),
@@ -1059,7 +1059,7 @@ def run_config(args):
                 t0 = time.time()
                 op_l = SpmmOperator(A, N, PlanConfig(tc_mode=tc_mode, learned=True))
                 t_l = time.time() - t0
-                Cl = torch.empty_like(C)
+                Cl = aligned_empty(C.shape[0], C.shape[1], dev)
                 ms_l = timed(lambda: op_l(B, out=Cl), args.steps)
                 out["learned_cost_model"] = {"plan": plan_summary(op_l.plan), "plan_search_s": round(t_l, 2),
                                              "forward_ms": ms_l, "analytic_forward_ms": ms_fwd,

@@ -70,6 +70,31 @@ def new_output(rows, cols, device):
     return buf[:, :cols], ldp
 
 
+def output_operand(out: torch.Tensor | None, rows: int, cols: int, device):
+    """(buffer the kernels write, its row stride, the caller's out or None):
+    the caller's fp32 [rows, cols] out when the kernels can write it in place
+    (row stride a multiple of 4, 16-byte aligned base), else a padded buffer
+    whose result finish_output copies into out."""
+    if out is None:
+        buf, ld = new_output(rows, cols, device)
+        return buf, ld, None
+    _require_cuda(out, "out")
+    if out.dtype != torch.float32 or tuple(out.shape) != (rows, cols):
+        raise ValueError(f"out must be a float32 tensor of shape ({rows}, {cols})")
+    ld = out.stride(0)
+    if out.stride(1) == 1 and ld >= cols and ld % 4 == 0 and out.data_ptr() % 16 == 0:
+        return out, ld, None
+    buf, ld = new_output(rows, cols, device)
+    return buf, ld, out
+
+
+def finish_output(buf: torch.Tensor, target: torch.Tensor | None) -> torch.Tensor:
+    if target is None:
+        return buf
+    target.copy_(buf)
+    return target
+
+
 class PackedValues:
     """H value sets of one plan packed on the device (pack_values)."""
 
@@ -187,14 +212,11 @@ class DeviceSpmmPlan:
         if B.shape[0] != self.K:
             raise ValueError(f"B has {B.shape[0]} rows, the plan has K={self.K}")
         N = B.shape[1]
-        if out is None:
-            out, ldc = new_output(self.M, N, B.device)
-        else:
-            ldc = out.stride(0)
+        out, ldc, target = output_operand(out, self.M, N, B.device)
         fn = self.lib.stile_spmm_run_bf16 if bf16 else self.lib.stile_spmm_run
         _lib.check(fn(self.handle, B.data_ptr(), ldb, out.data_ptr(), ldc, N, _stream()),
                    "stile_spmm_run_bf16" if bf16 else "stile_spmm_run")
-        return out
+        return finish_output(out, target)
 
     def pack_values(self, vals: torch.Tensor) -> "PackedValues":
         """Pack H value sets (vals [H, nnz], CSR order) for run_batched."""
@@ -265,15 +287,12 @@ class DeviceSpmmPlan:
         dC, lddc = dense_operand(dC, "dC")
         B, ldb = dense_operand(B, "B")
         N = dC.shape[1]
-        if dB is None:
-            dB, lddb = new_output(self.M, N, dC.device)
-        else:
-            lddb = dB.stride(0)
+        dB, lddb, target = output_operand(dB, self.M, N, dC.device)
         alloc = torch.empty if self._dvals_cover_all else torch.zeros
         dvals = alloc(self.nnz, dtype=torch.float32, device=dC.device)
         _lib.check(self.lib.stile_spmm_backward(self.handle, dC.data_ptr(), lddc, B.data_ptr(), ldb, dB.data_ptr(),
                                                 lddb, dvals.data_ptr(), N, _stream()), "stile_spmm_backward")
-        return dB, dvals
+        return finish_output(dB, target), dvals
 
     def set_values(self, vals: torch.Tensor):
         _require_cuda(vals, "vals")
@@ -389,14 +408,11 @@ class CsrMatrix:
     def spmm(self, B: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         B, ldb = dense_operand(B, "B")
         N = B.shape[1]
-        if out is None:
-            out, ldc = new_output(self.shape[0], N, B.device)
-        else:
-            ldc = out.stride(0)
+        out, ldc, target = output_operand(out, self.shape[0], N, B.device)
         _lib.check(self.lib.stile_csr_spmm_run(self.shape[0], self.nnz, self.indptr.data_ptr(), self.indices.data_ptr(),
                                                self.vals.data_ptr(), self.group_rows.data_ptr(), B.data_ptr(), ldb,
                                                out.data_ptr(), ldc, N, _stream()), "stile_csr_spmm_run")
-        return out
+        return finish_output(out, target)
 
 
 def plain_sddmm_plan(A) -> DeviceSddmmPlan:

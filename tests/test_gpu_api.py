@@ -389,3 +389,27 @@ def test_auto_path_on_the_pruned_weight_considers_the_dense_gemm():
     A2 = sp.csr_matrix((new, op.A.indices, op.A.indptr), shape=op.A.shape)
     assert S.rel_fro(op(B).cpu().numpy(), S.spmm_fp64(A2, w.dense["B"])) <= 1e-2
     assert S.rel_fro(op._dense_forward(B).cpu().numpy(), S.spmm_fp64(A2, w.dense["B"])) <= 1e-2
+
+
+def test_outputs_with_unaligned_row_stride_are_filled():
+    """An out / dB tensor whose row stride the kernels cannot write (41
+    floats: not a multiple of 4) is computed into a padded buffer and copied
+    into the caller's tensor."""
+    A = _graph(seed=24)
+    N = 41
+    op = plan_spmm(A, N, PlanConfig(backward="fused"))
+    rng = np.random.default_rng(25)
+    B = rng.standard_normal((A.shape[1], N)).astype(np.float32)
+    dC = rng.standard_normal((A.shape[0], N)).astype(np.float32)
+    Bt, dCt = torch.as_tensor(B, device="cuda"), torch.as_tensor(dC, device="cuda")
+    C = torch.empty((A.shape[0], N), device="cuda")
+    assert C.stride(0) == N
+    r = op(Bt, out=C)
+    assert r.data_ptr() == C.data_ptr()
+    assert S.rel_fro(C.cpu().numpy(), S.spmm_fp64(A, B)) <= 1e-2
+    dB = torch.empty((A.shape[1], N), device="cuda")
+    r, dv = op.backward(dCt, Bt, dB)
+    assert r.data_ptr() == dB.data_ptr()
+    assert S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(op.A.T.tocsr(), dC)) <= 1e-2
+    with pytest.raises(ValueError):
+        op(Bt, out=torch.empty((A.shape[0], N + 1), device="cuda"))
