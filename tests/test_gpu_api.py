@@ -333,8 +333,9 @@ def test_csr_path_forward_backward_and_value_refresh():
 @pytest.mark.parametrize("N", [128, 41])
 def test_auto_path_times_the_candidates_once_and_stays_correct(N):
     """path="auto": the first forward and backward of a width time the
-    hybrid plan against the plain CSR kernels and keep the faster; either
-    way the results match float64 within the hybrid bound, and later calls
+    hybrid plan against the plain CSR kernels (and, for the forward, a dense
+    bf16 GEMM of this small matrix) and keep the fastest; either way the
+    results match float64 within the tensor-tile bound, and later calls
     reuse the choice."""
     A = _graph(seed=12)
     op = plan_spmm(A, N, PlanConfig(path="auto"))
@@ -348,7 +349,8 @@ def test_auto_path_times_the_candidates_once_and_stays_correct(N):
         dB, dv = op.backward(dCd, Bd)
         assert S.rel_fro(dB.cpu().numpy(), S.spmm_fp64(A.T.tocsr(), dC)) <= 1e-2
         assert S.rel_fro(dv.cpu().numpy(), S.sddmm_fp64(A, dC, B)) <= 1e-5
-    assert op._fwd_choice[N] in ("hybrid", "csr")
+    # (a 2048-node graph is small enough for the dense GEMM candidate too)
+    assert op._fwd_choice[N] in ("hybrid", "csr", "dense")
     assert op._bwd_choice[N] in ("fused", "separate", "fused_tc", "separate_tc", "csr")
     assert len(op._fwd_choice) == 1 and len(op._bwd_choice) == 1
 
