@@ -319,7 +319,8 @@ int stile_spmm_backward(const StileSpmmPlan* planT, const float* dC, int64_t ldd
  * graph; the operator API times both once per width.  Row-tile
  * nonzeros always take the row runs or
  * the fused ELL pass.  A bf16 B (stile_spmm_dvals_bf16) always takes the
- * row runs. */
+ * row runs.  The mode is read when a call is enqueued; setting it is not
+ * thread-safe against calls on the same plan from other host threads. */
 int stile_spmm_plan_set_dvals_mode(StileSpmmPlan* plan, int32_t mode);
 
 /* Refresh the tile values of a plan from vals[nnz] (device, CSR order of the
